@@ -1,0 +1,841 @@
+// Host runtime of libatpm: the C ABI of include/atpm.h.
+//
+// It plays the part of the reference Thermal driver's single_model
+// (3905/Thermal/NominalPole/main.cpp:2417-2590) for a smooth shape: one solve
+// handle holds the shape, its view-factor lists and the whole thermal state
+// resident in device memory; the per-revolution work is one captured CUDA
+// graph (self-heating gather, conduction sweep, convergence, advance) that is
+// replayed in chunks with a single host synchronisation per chunk.
+//
+// Scalars that the reference computes in float are computed here in float in
+// the same operand order (this file is built with -ffp-contract=off).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/atpm.h"
+#include "atpm_internal.h"
+
+using namespace atpm;
+
+namespace {
+
+thread_local std::string g_err;
+
+atpm_status fail(atpm_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+atpm_status fail(atpm_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return s;
+}
+
+#define CK(call)                                                                      \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(ATPM_E_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                          \
+    } while (0)
+
+const double kPI = 4.0 * std::atan(1.0);   // main.cpp:12
+const double kAU = 149.6e6;                // main.cpp:13
+const float kSIGMA = 5.67e-8f;             // main.cpp:15
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct atpm_context {
+    int device = 0;
+    std::mutex mu;
+    bool tables = false;
+    HostPowTab p4, p3;
+};
+
+struct atpm_solve {
+    atpm_context* ctx = nullptr;
+    atpm_params P{};
+    int nf = 0, nv = 0, nnz = 0;
+    size_t rs = 4;  // bytes per state scalar
+    cudaStream_t st = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    DevSolve ds{};
+    DevSolve* ds_dev = nullptr;
+    int4* wmap = nullptr;
+    int2* fmap = nullptr;
+    int nw = 0, nfb = 0;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<double> vert_h;
+    std::vector<int32_t> fac_h;
+    bool have_forcing = false, have_temps = false;
+    float ti = 0.0f;
+    double last_ms = 0.0;
+    int64_t last_launches = 0, last_facet_steps = 0;
+    int last_nrev = 0;
+};
+
+namespace {
+
+atpm_status ensure_tables(atpm_context* c) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (c->tables) return ATPM_OK;
+    char err[256];
+    CK(cudaSetDevice(c->device));
+    if (build_pow_table(4, &c->p4, err, sizeof err)) return fail(ATPM_E_CUDA, "%s", err);
+    if (build_pow_table(3, &c->p3, err, sizeof err)) return fail(ATPM_E_CUDA, "%s", err);
+    c->tables = true;
+    return ATPM_OK;
+}
+
+PowTab view(const HostPowTab& h) {
+    PowTab t;
+    t.slots = h.slots_dev;
+    t.log2slots = h.log2slots;
+    t.lo_bits = h.lo_bits;
+    t.hi_bits = h.hi_bits;
+    return t;
+}
+
+struct Layout {
+    size_t off[24];
+    size_t total;
+};
+
+enum {
+    B_VERT, B_FAC, B_DPTR, B_DIDX, B_DVF, B_SHADOW, B_COS, B_EFM, B_E, B_S0, B_S1, B_TEMP, B_Q, B_W,
+    B_CONV, B_HOT, B_COUNTS, B_STATUS, B_CTL, B_DIAG, B_MEAN, B_N
+};
+
+Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
+    const size_t rs = (P.precision == ATPM_FP64) ? 8 : 4;
+    const size_t nt = (size_t)nf * P.ntau;
+    size_t sz[B_N];
+    sz[B_VERT] = (size_t)nv * 3 * 8;
+    sz[B_FAC] = (size_t)nf * 3 * 4;
+    sz[B_DPTR] = (size_t)(nf + 1) * 4;
+    sz[B_DIDX] = (size_t)std::max(nnz, 1) * 4;
+    sz[B_DVF] = (size_t)std::max(nnz, 1) * 4;
+    sz[B_SHADOW] = nt;
+    sz[B_COS] = nt * rs;
+    sz[B_EFM] = nt * rs;
+    sz[B_E] = nt * rs;
+    sz[B_S0] = nt * rs;
+    sz[B_S1] = nt * rs;
+    sz[B_TEMP] = (size_t)(P.nx + 1) * nf * rs;
+    sz[B_Q] = nt * rs;
+    sz[B_W] = nt * rs;
+    sz[B_CONV] = nf;
+    sz[B_HOT] = nf;
+    sz[B_COUNTS] = (size_t)std::max(P.revcap, 1) * 4;
+    sz[B_STATUS] = 4;
+    sz[B_CTL] = sizeof(Ctl);
+    sz[B_DIAG] = 4 * 8;
+    sz[B_MEAN] = (size_t)nf * rs;
+    Layout L;
+    size_t o = 0;
+    for (int i = 0; i < B_N; ++i) {
+        L.off[i] = o;
+        o += align256(sz[i]);
+    }
+    L.total = o;
+    return L;
+}
+
+atpm_status check_shape(const atpm_shape* sh, const atpm_params* P) {
+    if (!sh || !P) return fail(ATPM_E_INVALID, "null shape or params");
+    if (sh->nv < 3 || sh->nf < 1 || !sh->vertices || !sh->facets || !sh->dep_ptr)
+        return fail(ATPM_E_INVALID, "shape needs nv>=3, nf>=1, vertices, facets, dep_ptr");
+    if (P->ntau < 1 || P->nx < 2 || P->revcap < 1)
+        return fail(ATPM_E_INVALID, "ntau>=1, nx>=2, revcap>=1 required");
+    if (P->precision < 0 || P->precision > 2) return fail(ATPM_E_INVALID, "unknown precision %d", P->precision);
+    if (!conduction_nx_supported(P->nx))
+        return fail(ATPM_E_UNSUPPORTED, "nx=%d not built (supported: 8,12,16,24,32,40,48,56,64)", P->nx);
+    if (sh->dep_ptr[0] != 0) return fail(ATPM_E_INVALID, "dep_ptr[0] must be 0");
+    for (int f = 0; f < sh->nf; ++f)
+        if (sh->dep_ptr[f + 1] < sh->dep_ptr[f]) return fail(ATPM_E_INVALID, "dep_ptr not monotone at %d", f);
+    const int nnz = sh->dep_ptr[sh->nf];
+    if (nnz > 0 && (!sh->dep_idx || !sh->dep_vf)) return fail(ATPM_E_INVALID, "dep_idx/dep_vf missing");
+    for (int k = 0; k < nnz; ++k)
+        if (sh->dep_idx[k] < 0 || sh->dep_idx[k] >= sh->nf)
+            return fail(ATPM_E_INVALID, "dep_idx[%d]=%d out of range", k, sh->dep_idx[k]);
+    for (int i = 0; i < 3 * sh->nf; ++i)
+        if (sh->facets[i] < 0 || sh->facets[i] >= sh->nv)
+            return fail(ATPM_E_INVALID, "facet vertex index %d out of range", sh->facets[i]);
+    return ATPM_OK;
+}
+
+// Scalars of the reference in its float operand order (main.cpp:1477-1541).
+void set_scalars(atpm_solve* s, float ti) {
+    const atpm_params& P = s->P;
+    DevSolve& d = s->ds;
+    const float PIf = (float)kPI;
+    const float DZ = 8.0f / P.nx;
+    const float DTAU = 2.0f * PIf / P.ntau;
+    d.ti = ti;
+    d.r = DTAU / (DZ * DZ);
+    d.m1 = ti * std::sqrt(2.0f * PIf / P.rotation_period_s) / DZ;
+    d.es = P.emissivity * kSIGMA;
+    d.es4 = 4.0f * P.emissivity * kSIGMA;
+    d.oma = 1.0f - P.albedo;
+    d.tacc = P.tacc;
+    const double t10 = (double)P.tacc / 10.0;
+    float c = (float)t10;
+    if ((double)c < t10) c = std::nextafter(c, 1e30f);
+    d.tacc10 = c;  // DT >= c  <=>  (double)DT >= TACC/10.0 for every float DT
+    d.alb = P.albedo;
+    d.solar = (float)(1367.0 / (P.polar[0] * P.polar[0]));
+    d.sacc = P.scattering_accuracy;
+    // FP64 state: the same expressions with double operands
+    const double PId = (double)PIf;
+    const double DZd = 8.0 / P.nx;
+    const double DTAUd = 2.0 * PId / P.ntau;
+    d.ti_d = ti;
+    d.r_d = DTAUd / (DZd * DZd);
+    d.m1_d = (double)ti * std::sqrt(2.0 * PId / (double)P.rotation_period_s) / DZd;
+    d.es_d = (double)P.emissivity * (double)kSIGMA;
+    d.es4_d = 4.0 * (double)P.emissivity * (double)kSIGMA;
+    d.oma_d = 1.0 - (double)P.albedo;
+    d.tacc_d = (double)P.tacc;
+    d.tacc10_d = t10;
+    d.alb_d = (double)P.albedo;
+    d.solar_d = (double)d.solar;
+    d.sacc_d = (double)P.scattering_accuracy;
+    d.newton_cap = 200;
+}
+
+atpm_status upload_table(atpm_solve* s) {
+    CK(cudaMemcpyAsync(s->ds_dev, &s->ds, sizeof(DevSolve), cudaMemcpyHostToDevice, s->st));
+    return ATPM_OK;
+}
+
+void build_maps(int nf, int ntau, int solve, std::vector<int4>& w, std::vector<int2>& fm) {
+    for (int f0 = 0; f0 < nf; f0 += 32)
+        for (int s0 = 0; s0 < ntau; s0 += 32) w.push_back(make_int4(solve, f0, s0, 0));
+    for (int f0 = 0; f0 < nf; f0 += 128) fm.push_back(make_int2(solve, f0));
+}
+
+Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, int nw, const int2* fm,
+                 int nfb, int mode, int nx) {
+    Batch b;
+    b.tab = tab;
+    b.n = n;
+    b.wmap = wm;
+    b.nw = nw;
+    b.fmap = fm;
+    b.nfb = nfb;
+    b.mode = mode;
+    b.nx = nx;
+    b.p4 = view(ctx->p4);
+    b.p3 = view(ctx->p3);
+    return b;
+}
+
+atpm_status capture_graph(atpm_solve* s, const Batch& b, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_revolution(b, s->st);
+    cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return fail(ATPM_E_CUDA, "revolution launch failed during capture (rc=%d)", rc);
+    }
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    return ATPM_OK;
+}
+
+int64_t facet_steps_from_counts(const int32_t* counts, int nrev, int nf, int ntau, bool inst) {
+    int64_t fs = 0;
+    for (int r = 0; r < nrev; ++r) {
+        int active = nf;
+        if (!inst && r - 1 > 5) active = nf - counts[r - 1];
+        fs += (int64_t)active * ntau;
+    }
+    return fs;
+}
+
+atpm_status check_status(atpm_solve* s, int st) {
+    if (st & ST_NONFINITE) return fail(ATPM_E_NONFINITE, "a surface temperature became non-finite");
+    if (st & ST_NEWTON_CAP) return fail(ATPM_E_ITERATION, "Newton iteration cap reached");
+    if (st & ST_SCATTER_CAP) return fail(ATPM_E_ITERATION, "scattering iteration cap reached");
+    (void)s;
+    return ATPM_OK;
+}
+
+}  // namespace
+
+namespace {
+template <class R>
+atpm_status get_transposed(atpm_solve* s, const void* dev, size_t rows, size_t cols, float* out, double* out64) {
+    // dev is [rows][cols]; out is [cols][rows]
+    std::vector<R> h(rows * cols);
+    CK(cudaMemcpyAsync(h.data(), dev, h.size() * sizeof(R), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    for (size_t i = 0; i < rows; ++i)
+        for (size_t j = 0; j < cols; ++j) {
+            if (out) out[j * rows + i] = (float)h[i * cols + j];
+            if (out64) out64[j * rows + i] = (double)h[i * cols + j];
+        }
+    return ATPM_OK;
+}
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+ATPM_API const char* atpm_status_string(atpm_status s) {
+    switch (s) {
+        case ATPM_OK: return "ok";
+        case ATPM_E_INVALID: return "invalid argument";
+        case ATPM_E_CUDA: return "CUDA error";
+        case ATPM_E_NOMEM: return "out of memory";
+        case ATPM_E_UNSUPPORTED: return "unsupported";
+        case ATPM_E_STATE: return "call out of order";
+        case ATPM_E_NONFINITE: return "non-finite temperature";
+        case ATPM_E_ITERATION: return "iteration cap reached";
+        case ATPM_E_BUDGET: return "over HBM budget";
+        case ATPM_E_CANCELLED: return "cancelled";
+    }
+    return "unknown status";
+}
+
+ATPM_API const char* atpm_last_error(void) { return g_err.c_str(); }
+ATPM_API int32_t atpm_version(void) { return 100; }
+
+ATPM_API atpm_status atpm_context_create(int32_t device, atpm_context** out) {
+    if (!out) return fail(ATPM_E_INVALID, "null out");
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(ATPM_E_INVALID, "device %d of %d", device, n);
+    CK(cudaSetDevice(device));
+    auto* c = new atpm_context();
+    c->device = device;
+    *out = c;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_context_destroy(atpm_context* c) {
+    if (!c) return ATPM_OK;
+    cudaSetDevice(c->device);
+    if (c->p4.slots_dev) cudaFree(c->p4.slots_dev);
+    if (c->p3.slots_dev) cudaFree(c->p3.slots_dev);
+    delete c;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* sh, const atpm_params* P, uint64_t* bytes) {
+    atpm_status r = check_shape(sh, P);
+    if (r) return r;
+    Layout L = layout(sh->nv, sh->nf, sh->dep_ptr[sh->nf], *P);
+    const size_t nt = (size_t)sh->nf * P->ntau;
+    const size_t rs = (P->precision == ATPM_FP64) ? 8 : 4;
+    // transient peak: geometry (hp, hm, nrm, dist) or scattering work
+    const size_t geo = (size_t)sh->nv * P->ntau * 24 + nt * 56 + (size_t)P->ntau * 16;
+    const size_t sct = 3 * nt * rs;
+    *bytes = (uint64_t)(L.total + std::max(geo, sct) + 64 * 1024);
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, const atpm_params* P,
+                                       atpm_solve** out) {
+    if (!ctx || !out) return fail(ATPM_E_INVALID, "null context or out");
+    atpm_status r = check_shape(sh, P);
+    if (r) return r;
+    CK(cudaSetDevice(ctx->device));
+    if (P->precision == ATPM_REFERENCE) {
+        r = ensure_tables(ctx);
+        if (r) return r;
+    }
+    auto* s = new atpm_solve();
+    s->ctx = ctx;
+    s->P = *P;
+    s->nf = sh->nf;
+    s->nv = sh->nv;
+    s->nnz = sh->dep_ptr[sh->nf];
+    s->rs = (P->precision == ATPM_FP64) ? 8 : 4;
+    Layout L = layout(s->nv, s->nf, s->nnz, *P);
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
+    e = cudaMalloc(&s->arena, L.total);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s->st);
+        delete s;
+        return fail(ATPM_E_NOMEM, "cudaMalloc(%zu): %s", L.total, cudaGetErrorString(e));
+    }
+    s->arena_bytes = L.total;
+    char* a = static_cast<char*>(s->arena);
+    DevSolve& d = s->ds;
+    d.nf = s->nf; d.nv = s->nv; d.ntau = P->ntau; d.nx = P->nx; d.revcap = P->revcap;
+    d.mode = P->precision; d.nnz = s->nnz;
+    d.vert = reinterpret_cast<double*>(a + L.off[B_VERT]);
+    d.fac = reinterpret_cast<int*>(a + L.off[B_FAC]);
+    d.dep_ptr = reinterpret_cast<int*>(a + L.off[B_DPTR]);
+    d.dep_idx = reinterpret_cast<int*>(a + L.off[B_DIDX]);
+    d.dep_vf = reinterpret_cast<float*>(a + L.off[B_DVF]);
+    d.shadow = reinterpret_cast<uint8_t*>(a + L.off[B_SHADOW]);
+    d.cosil = a + L.off[B_COS];
+    d.Efm = a + L.off[B_EFM];
+    d.E = a + L.off[B_E];
+    d.stemp0 = a + L.off[B_S0];
+    d.stemp1 = a + L.off[B_S1];
+    d.temp = a + L.off[B_TEMP];
+    d.Q = a + L.off[B_Q];
+    d.W = a + L.off[B_W];
+    d.conv = reinterpret_cast<uint8_t*>(a + L.off[B_CONV]);
+    d.hot = reinterpret_cast<uint8_t*>(a + L.off[B_HOT]);
+    d.counts = reinterpret_cast<int*>(a + L.off[B_COUNTS]);
+    d.status = reinterpret_cast<int*>(a + L.off[B_STATUS]);
+    d.ctl = reinterpret_cast<Ctl*>(a + L.off[B_CTL]);
+    d.diag = reinterpret_cast<double*>(a + L.off[B_DIAG]);
+    set_scalars(s, 0.0f);
+    s->vert_h.assign(sh->vertices, sh->vertices + 3 * (size_t)s->nv);
+    s->fac_h.assign(sh->facets, sh->facets + 3 * (size_t)s->nf);
+#define UP(dst, src, bytes) \
+    if (bytes) { e = cudaMemcpyAsync((void*)(dst), (src), (bytes), cudaMemcpyHostToDevice, s->st); if (e != cudaSuccess) goto cuda_fail; }
+    UP(d.vert, sh->vertices, (size_t)s->nv * 24);
+    UP(d.fac, sh->facets, (size_t)s->nf * 12);
+    UP(d.dep_ptr, sh->dep_ptr, (size_t)(s->nf + 1) * 4);
+    UP(d.dep_idx, sh->dep_idx, (size_t)s->nnz * 4);
+    UP(d.dep_vf, sh->dep_vf, (size_t)s->nnz * 4);
+#undef UP
+    e = cudaMemsetAsync(a + L.off[B_CONV], 0, L.off[B_MEAN] - L.off[B_CONV], s->st);
+    if (e != cudaSuccess) goto cuda_fail;
+    e = cudaMalloc(&s->ds_dev, sizeof(DevSolve));
+    if (e != cudaSuccess) goto cuda_fail;
+    {
+        std::vector<int4> wm;
+        std::vector<int2> fm;
+        build_maps(s->nf, P->ntau, 0, wm, fm);
+        s->nw = s->nnz > 0 ? (int)wm.size() : 0;
+        s->nfb = (int)fm.size();
+        e = cudaMalloc(&s->wmap, std::max<size_t>(wm.size(), 1) * sizeof(int4));
+        if (e != cudaSuccess) goto cuda_fail;
+        e = cudaMalloc(&s->fmap, fm.size() * sizeof(int2));
+        if (e != cudaSuccess) goto cuda_fail;
+        e = cudaMemcpyAsync(s->wmap, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice, s->st);
+        if (e != cudaSuccess) goto cuda_fail;
+        e = cudaMemcpyAsync(s->fmap, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice, s->st);
+        if (e != cudaSuccess) goto cuda_fail;
+        // host staging must stay alive until the copies complete
+        e = cudaStreamSynchronize(s->st);
+        if (e != cudaSuccess) goto cuda_fail;
+    }
+    if ((r = upload_table(s)) != ATPM_OK) { atpm_solve_destroy(s); return r; }
+    e = cudaEventCreate(&s->ev0);
+    if (e != cudaSuccess) goto cuda_fail;
+    e = cudaEventCreate(&s->ev1);
+    if (e != cudaSuccess) goto cuda_fail;
+    *out = s;
+    return ATPM_OK;
+cuda_fail:
+    atpm_solve_destroy(s);
+    return fail(ATPM_E_CUDA, "solve setup: %s", cudaGetErrorString(e));
+}
+
+ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
+    if (!s) return ATPM_OK;
+    cudaSetDevice(s->ctx->device);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->wmap) cudaFree(s->wmap);
+    if (s->fmap) cudaFree(s->fmap);
+    if (s->ds_dev) cudaFree(s->ds_dev);
+    if (s->arena) cudaFree(s->arena);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    CK(cudaSetDevice(s->ctx->device));
+    const atpm_params& P = s->P;
+    const int ntau = P.ntau;
+    // host: pole matrix, heliocentric centre, rotation table (main.cpp:894-958)
+    GeomWork g{};
+    const double r0 = P.pole[0], r1 = P.pole[1];
+    const double gamma = std::acos(std::cos(r0) * std::sin(std::fabs(r1)));
+    double tm[3][3];
+    tm[0][0] = std::sin(r0) / std::sin(gamma);
+    tm[0][1] = -1.0 * std::cos(r0) * std::cos(r0) * std::sin(r1) * std::cos(r1) / std::sin(gamma);
+    tm[0][2] = std::cos(r0) * std::cos(r1);
+    tm[1][0] = 0.0;
+    tm[1][1] = ((std::sin(r0) * std::sin(r0)) + (std::cos(r0) * std::cos(r0) * std::cos(r1) * std::cos(r1))) /
+               std::sin(gamma);
+    tm[1][2] = std::cos(r0) * std::sin(r1);
+    tm[2][0] = -1.0 * std::cos(r0) * std::cos(r1) / std::sin(gamma);
+    tm[2][1] = -1.0 * std::sin(r0) * std::cos(r0) * std::sin(r1) / std::sin(gamma);
+    tm[2][2] = std::sin(r0);
+    for (int i = 0; i < 9; ++i) g.tm[i] = tm[i / 3][i % 3];
+    g.car[0] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::cos(P.polar[2]);
+    g.car[1] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::sin(P.polar[2]);
+    g.car[2] = kAU * P.polar[0] * std::sin(P.polar[1]);
+    std::vector<double> rot(2 * (size_t)ntau);
+    for (int step = 0; step < ntau; ++step) {
+        const double ang = 2.0 * kPI * step / ntau;
+        rot[2 * step] = std::cos(ang);
+        rot[2 * step + 1] = std::sin(ang);
+    }
+    const size_t nt = (size_t)s->nf * ntau;
+    const size_t bytes = align256((size_t)s->nv * ntau * 24) + align256(nt * 24) * 2 + align256(nt * 8) +
+                         align256((size_t)ntau * 16);
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, bytes, s->st));
+    char* t = static_cast<char*>(tmp);
+    g.hp = reinterpret_cast<double*>(t);
+    t += align256((size_t)s->nv * ntau * 24);
+    g.hm = reinterpret_cast<double*>(t);
+    t += align256(nt * 24);
+    g.nrm = reinterpret_cast<double*>(t);
+    t += align256(nt * 24);
+    g.dist = reinterpret_cast<double*>(t);
+    t += align256(nt * 8);
+    g.rot = reinterpret_cast<double*>(t);
+    cudaError_t e = cudaMemcpyAsync((void*)g.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, s->st);
+    int rc = 0;
+    if (e == cudaSuccess) rc = launch_geometry(s->ds, g, s->st);
+    if (e == cudaSuccess && !rc && P.shadowing == 1 && s->nnz > 0) rc = launch_shadow_deplist(s->ds, g, s->st);
+    if (e == cudaSuccess && !rc && P.shadowing == 2) rc = launch_shadow_allpairs(s->ds, g, s->st);
+    cudaFreeAsync(tmp, s->st);
+    cudaError_t e2 = cudaStreamSynchronize(s->st);  // `rot` must outlive the copy
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "geometry upload: %s", cudaGetErrorString(e));
+    if (rc) return fail(ATPM_E_CUDA, "geometry launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "geometry: %s", cudaGetErrorString(e2));
+    s->have_forcing = false;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_scattering(atpm_solve* s) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    CK(cudaSetDevice(s->ctx->device));
+    if (launch_single_scattering(s->ds, s->st)) return fail(ATPM_E_CUDA, "single scattering launch");
+    if (s->P.multiple_scattering) {
+        void* work = nullptr;
+        CK(cudaMallocAsync(&work, multiple_scattering_work_bytes(s->ds), s->st));
+        int rc = launch_multiple_scattering(s->ds, work, s->st);
+        cudaFreeAsync(work, s->st);
+        if (rc) return fail(ATPM_E_CUDA, "multiple scattering launch");
+    }
+    if (launch_forcing_transpose(s->ds, s->st)) return fail(ATPM_E_CUDA, "forcing transpose launch");
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, s->ds.status, 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    atpm_status r = check_status(s, st);
+    if (r) return r;
+    s->have_forcing = true;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_set_forcing(atpm_solve* s, const int32_t* shadow, const float* illum) {
+    if (!s || !shadow || !illum) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, nt * 8, s->st));
+    int32_t* sd = static_cast<int32_t*>(tmp);
+    float* id = reinterpret_cast<float*>(sd + nt);
+    cudaError_t e = cudaMemcpyAsync(sd, shadow, nt * 4, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(id, illum, nt * 4, cudaMemcpyHostToDevice, s->st);
+    int rc = (e == cudaSuccess) ? launch_set_forcing(s->ds, sd, id, s->st) : 0;
+    if (e == cudaSuccess && !rc) rc = launch_forcing_transpose(s->ds, s->st);
+    cudaFreeAsync(tmp, s->st);
+    cudaError_t e2 = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess || rc || e2 != cudaSuccess)
+        return fail(ATPM_E_CUDA, "set_forcing: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    s->have_forcing = true;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (!(ti >= 0.0f) || !std::isfinite(ti)) return fail(ATPM_E_INVALID, "thermal inertia %g", (double)ti);
+    CK(cudaSetDevice(s->ctx->device));
+    s->ti = ti;
+    set_scalars(s, ti);
+    atpm_status r = upload_table(s);
+    if (r) return r;
+    // reset_asteroid_status (main.cpp:477-485)
+    Ctl c{0, 1, 0, 0};
+    CK(cudaMemcpyAsync(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemsetAsync(s->ds.conv, 0, s->nf, s->st));
+    CK(cudaMemsetAsync(s->ds.hot, 0, s->nf, s->st));
+    CK(cudaMemsetAsync(s->ds.counts, 0, (size_t)s->P.revcap * 4, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_initialise_temperatures(atpm_solve* s) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (!s->have_forcing) return fail(ATPM_E_STATE, "no forcing: call atpm_scattering or atpm_set_forcing");
+    CK(cudaSetDevice(s->ctx->device));
+    const int nf = s->nf;
+    void* mean = static_cast<char*>(s->arena) + layout(s->nv, s->nf, s->nnz, s->P).off[B_MEAN];
+    if (launch_initial_mean(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "initial mean launch");
+    const atpm_params& P = s->P;
+    if (P.precision == ATPM_FP64) {
+        std::vector<double> m(nf);
+        CK(cudaMemcpyAsync(m.data(), mean, nf * 8, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        const double alb = P.albedo, es = (double)P.emissivity * (double)kSIGMA;
+        for (int f = 0; f < nf; ++f) m[f] = std::pow((1.0 - alb) * m[f] / es, 0.25);
+        CK(cudaMemcpyAsync(mean, m.data(), nf * 8, cudaMemcpyHostToDevice, s->st));
+        if (launch_fill_initial(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "fill launch");
+        CK(cudaStreamSynchronize(s->st));
+    } else {
+        std::vector<float> m(nf);
+        CK(cudaMemcpyAsync(m.data(), mean, nf * 4, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        const float es = P.emissivity * kSIGMA;
+        // main.cpp:1458, with this host's libm powf
+        for (int f = 0; f < nf; ++f) m[f] = std::pow((1.0f - P.albedo) * m[f] / es, 0.25f);
+        CK(cudaMemcpyAsync(mean, m.data(), nf * 4, cudaMemcpyHostToDevice, s->st));
+        if (launch_fill_initial(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "fill launch");
+        CK(cudaStreamSynchronize(s->st));
+    }
+    s->have_temps = true;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_revolution(atpm_solve* s, int32_t rev, int32_t* numconv, int32_t* converged) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (!s->have_forcing || (!s->have_temps && s->ti != 0.0f))
+        return fail(ATPM_E_STATE, "forcing and initial temperatures required");
+    if (rev < 0 || rev >= s->P.revcap) return fail(ATPM_E_INVALID, "rev %d outside [0, revcap)", rev);
+    CK(cudaSetDevice(s->ctx->device));
+    Ctl c;
+    CK(cudaMemcpyAsync(&c, s->ds.ctl, sizeof c, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    c.rev = rev;
+    c.active = 1;
+    CK(cudaMemcpyAsync(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    Batch b = make_batch(s->ctx, s->ds_dev, 1, s->wmap, s->nw, s->fmap, s->nfb, s->P.precision, s->P.nx);
+    if (launch_revolution(b, s->st)) return fail(ATPM_E_CUDA, "revolution launch");
+    int st = 0;
+    CK(cudaMemcpyAsync(&c, s->ds.ctl, sizeof c, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaMemcpyAsync(&st, s->ds.status, 4, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    if (numconv) *numconv = c.numconv;
+    if (converged) *converged = c.converged;
+    return check_status(s, st);
+}
+
+ATPM_API atpm_status atpm_run(atpm_solve* s, int32_t* nrev, int32_t* counts) {
+    atpm_solve* one[1] = {s};
+    return atpm_batch_run(one, 1, nrev, counts);
+}
+
+ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_t* nrev, int32_t* counts) {
+    if (!solves || n < 1) return fail(ATPM_E_INVALID, "empty batch");
+    atpm_solve* s0 = solves[0];
+    for (int i = 0; i < n; ++i) {
+        atpm_solve* s = solves[i];
+        if (!s) return fail(ATPM_E_INVALID, "null solve %d", i);
+        if (s->ctx != s0->ctx || s->P.precision != s0->P.precision || s->P.nx != s0->P.nx)
+            return fail(ATPM_E_INVALID, "batch solves must share context, precision and nx");
+        if (!s->have_forcing || (!s->have_temps && s->ti != 0.0f))
+            return fail(ATPM_E_STATE, "solve %d: forcing and initial temperatures required", i);
+    }
+    CK(cudaSetDevice(s0->ctx->device));
+    // all solves must be ready before s0's stream runs the batch
+    for (int i = 1; i < n; ++i) CK(cudaStreamSynchronize(solves[i]->st));
+    Batch b;
+    void* tmp = nullptr;
+    if (n == 1) {
+        b = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
+    } else {
+        std::vector<DevSolve> tab(n);
+        std::vector<int4> wm;
+        std::vector<int2> fm;
+        for (int i = 0; i < n; ++i) {
+            tab[i] = solves[i]->ds;
+            std::vector<int4> w1;
+            build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, fm);
+            if (solves[i]->nnz > 0) wm.insert(wm.end(), w1.begin(), w1.end());
+        }
+        const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
+        const size_t bf = align256(fm.size() * sizeof(int2));
+        CK(cudaMalloc(&tmp, bt + bw + bf));
+        char* t = static_cast<char*>(tmp);
+        CK(cudaMemcpy(t, tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice));
+        if (!wm.empty()) CK(cudaMemcpy(t + bt, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(t + bt + bw, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        b = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + bt), (int)wm.size(),
+                       reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
+    }
+    cudaGraphExec_t gx = nullptr;
+    atpm_status r = capture_graph(s0, b, &gx);
+    if (r) { if (tmp) cudaFree(tmp); return r; }
+    int maxcap = 0;
+    for (int i = 0; i < n; ++i) maxcap = std::max(maxcap, solves[i]->P.revcap);
+    std::vector<Ctl> ctl(n);
+    int done_revs = 0;
+    int chunk = 4;
+    cudaError_t e = cudaEventRecord(s0->ev0, s0->st);
+    int64_t launches = 0;
+    while (e == cudaSuccess && done_revs < maxcap) {
+        const int k = std::min(chunk, maxcap - done_revs);
+        for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaGraphLaunch(gx, s0->st);
+        launches += (int64_t)k * (b.nw > 0 ? 5 : 3);
+        done_revs += k;
+        if (e != cudaSuccess) break;
+        e = cudaEventRecord(s0->ev1, s0->st);
+        bool any = false;
+        for (int i = 0; i < n && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(&ctl[i], solves[i]->ds.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s0->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s0->st);
+        for (int i = 0; i < n; ++i) any = any || ctl[i].active;
+        if (!any) break;
+        chunk = std::min(chunk * 2, 32);
+    }
+    cudaGraphExecDestroy(gx);
+    if (tmp) cudaFree(tmp);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "revolution loop: %s", cudaGetErrorString(e));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, s0->ev0, s0->ev1));
+    int64_t fsteps_total = 0;
+    atpm_status worst = ATPM_OK;
+    for (int i = 0; i < n; ++i) {
+        atpm_solve* s = solves[i];
+        std::vector<int32_t> cnt(s->P.revcap);
+        int st = 0;
+        CK(cudaMemcpy(cnt.data(), s->ds.counts, (size_t)s->P.revcap * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&st, s->ds.status, 4, cudaMemcpyDeviceToHost));
+        const int nr = ctl[i].rev;
+        if (nrev) nrev[i] = nr;
+        if (counts) std::memcpy(counts + (size_t)i * maxcap, cnt.data(), (size_t)s->P.revcap * 4);
+        const int64_t fs = facet_steps_from_counts(cnt.data(), nr, s->nf, s->P.ntau, s->ti == 0.0f);
+        s->last_nrev = nr;
+        s->last_facet_steps = fs;
+        fsteps_total += fs;
+        atpm_status r2 = check_status(s, st);
+        if (r2 && !worst) worst = r2;
+    }
+    s0->last_ms = ms;
+    s0->last_launches = launches;
+    s0->last_facet_steps = fsteps_total;
+    return worst;
+}
+
+ATPM_API atpm_status atpm_single_model(atpm_solve* s, const float* ti, int32_t nti, int32_t* nrev,
+                                       int32_t* counts, float* stemp1_out) {
+    if (!s || !ti || nti < 1) return fail(ATPM_E_INVALID, "bad arguments");
+    atpm_status r = atpm_geometry_shadow(s);
+    if (r) return r;
+    r = atpm_scattering(s);
+    if (r) return r;
+    bool initialised = false;
+    for (int k = 0; k < nti; ++k) {
+        r = atpm_set_thermal_inertia(s, ti[k]);
+        if (r) return r;
+        if (ti[k] != 0.0f && !initialised) {
+            r = atpm_initialise_temperatures(s);
+            if (r) return r;
+            initialised = true;
+        }
+        r = atpm_run(s, nrev ? nrev + k : nullptr, counts ? counts + (size_t)k * s->P.revcap : nullptr);
+        if (r) return r;
+    }
+    if (stemp1_out) return atpm_get_surface_temperature(s, stemp1_out, nullptr);
+    return ATPM_OK;
+}
+
+// --------------------------------------------------------------- getters
+
+ATPM_API atpm_status atpm_get_shadow(atpm_solve* s, int32_t* out) {
+    if (!s || !out) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    std::vector<uint8_t> h(nt);
+    CK(cudaMemcpyAsync(h.data(), s->ds.shadow, nt, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    for (size_t i = 0; i < nt; ++i) out[i] = h[i];
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out) {
+    if (!s || !out) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    if (s->rs == 8) {
+        std::vector<double> h(nt);
+        CK(cudaMemcpyAsync(h.data(), s->ds.Efm, nt * 8, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        for (size_t i = 0; i < nt; ++i) out[i] = (float)h[i];
+    } else {
+        CK(cudaMemcpyAsync(out, s->ds.Efm, nt * 4, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+    }
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    CK(cudaSetDevice(s->ctx->device));
+    const size_t nt = s->P.ntau, nf = s->nf;
+    atpm_status r = ATPM_OK;
+    if (s->rs == 8) {
+        if (stemp1) r = get_transposed<double>(s, s->ds.stemp1, nt, nf, stemp1, nullptr);
+        if (!r && stemp0) r = get_transposed<double>(s, s->ds.stemp0, nt, nf, stemp0, nullptr);
+    } else {
+        if (stemp1) r = get_transposed<float>(s, s->ds.stemp1, nt, nf, stemp1, nullptr);
+        if (!r && stemp0) r = get_transposed<float>(s, s->ds.stemp0, nt, nf, stemp0, nullptr);
+    }
+    return r;
+}
+
+ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp1) {
+    if (!s || !stemp1) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    if (s->rs == 8) return get_transposed<double>(s, s->ds.stemp1, s->P.ntau, s->nf, nullptr, stemp1);
+    return get_transposed<float>(s, s->ds.stemp1, s->P.ntau, s->nf, nullptr, stemp1);
+}
+
+ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp) {
+    if (!s || !temp) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    if (s->rs == 8) return get_transposed<double>(s, s->ds.temp, s->P.nx + 1, s->nf, temp, nullptr);
+    return get_transposed<float>(s, s->ds.temp, s->P.nx + 1, s->nf, temp, nullptr);
+}
+
+ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted, double* mean_t) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    CK(cudaSetDevice(s->ctx->device));
+    CK(cudaMemsetAsync(s->ds.diag, 0, 32, s->st));
+    if (launch_energy_balance(s->ds, s->st)) return fail(ATPM_E_CUDA, "energy launch");
+    double d[4];
+    CK(cudaMemcpyAsync(d, s->ds.diag, 32, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    const double n = (double)s->nf * s->P.ntau;
+    if (absorbed) *absorbed = d[0];
+    if (emitted) *emitted = d[1];
+    if (mean_t) *mean_t = d[2] / n;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_last_run_stats(atpm_solve* s, double* ms, int64_t* launches, int64_t* fsteps) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (ms) *ms = s->last_ms;
+    if (launches) *launches = s->last_launches;
+    if (fsteps) *fsteps = s->last_facet_steps;
+    return ATPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Internal declarations shared by the CUDA kernels and the host runtime of
+// libatpm.  Device layouts (all per solve, resident for the solve's life):
+//
+//   E, Q, stemp0, stemp1   [ntau][nf]   step-major: thread f reads step s of
+//                                       consecutive facets -> coalesced
+//   temp                   [nx+1][nf]   depth-major, read once per revolution
+//   W                      [nf][ntau]   facet-major eps*sigma*T^4 of the
+//                                       previous revolution: the self-heating
+//                                       gather reads 32 consecutive steps
+//   shadow, cosil          [nf][ntau]   facet-major (scattering gathers)
+//   dep_ptr/idx/vf         CSR view-factor lists in file order
+//
+// Scalar precision: MODE 0 = reference FP32 (exact operand order), MODE 1 =
+// FP64, MODE 2 = fast FP32.
+#pragma once
+#include <cstdint>
+#include <cstddef>
+
+namespace atpm {
+
+enum : int { MODE_REF = 0, MODE_FP64 = 1, MODE_FAST = 2 };
+
+// status bits written by kernels into DevSolve::status
+enum : int {
+    ST_NONFINITE = 1,     // a surface temperature became NaN/Inf
+    ST_NEWTON_CAP = 2,    // Newton iteration cap reached
+    ST_POW_RANGE = 4,     // REFERENCE mode: pow argument outside the exact table range
+    ST_SCATTER_CAP = 8,   // scattering iteration cap reached
+};
+
+// exception table: glibc powf(x, e) where it differs from the device's
+// double-float evaluation of x^e; open addressing on the float's bits
+struct PowTab {
+    const uint2* slots;   // {key bits, value bits}; key 0xFFFFFFFF = empty
+    uint32_t log2slots;
+    uint32_t lo_bits;     // first float (bits) covered
+    uint32_t hi_bits;     // one past the last float covered
+};
+
+// per-solve control words (device memory, updated by the advance kernel)
+struct Ctl {
+    int rev;        // next revolution index
+    int active;     // 1 while the revolution loop runs
+    int converged;  // reference `converged` flag
+    int numconv;    // facets converged after the last revolution
+};
+
+struct DevSolve {
+    int nf, nv, ntau, nx, revcap, mode;
+    int nnz;
+    // shape
+    const double* vert;      // [nv][3]
+    const int* fac;          // [nf][3]
+    const int* dep_ptr;      // [nf+1]
+    const int* dep_idx;      // [nnz]
+    const float* dep_vf;     // [nnz]
+    // forcing
+    uint8_t* shadow;         // [nf][ntau]
+    void* cosil;             // [nf][ntau] float (modes 0,2) / double (mode 1)
+    void* Efm;               // [nf][ntau] R: scattering output, facet-major
+    void* E;                 // [ntau][nf] R
+    // state
+    void* stemp0;            // [ntau][nf] R
+    void* stemp1;            // [ntau][nf] R
+    void* temp;              // [nx+1][nf] R
+    void* Q;                 // [ntau][nf] R
+    void* W;                 // [nf][ntau] R
+    uint8_t* conv;           // [nf] frozen (reference astconverged)
+    uint8_t* hot;            // [nf] some |stemp1-stemp0| >= TACC this revolution
+    int* counts;             // [revcap] numconverged after each revolution
+    int* status;             // ST_* bits
+    Ctl* ctl;
+    double* diag;            // [4] FP64 energy-balance accumulators
+    // scalars (float for modes 0/2, double for mode 1), computed on the host
+    // in the reference's operand order
+    float ti, oma, es, es4, m1, r, tacc, tacc10, alb, solar, sacc;
+    double ti_d, oma_d, es_d, es4_d, m1_d, r_d, tacc_d, tacc10_d, alb_d, solar_d, sacc_d;
+    int newton_cap;
+};
+
+// ---------------------------------------------------------------- launchers
+// (definitions in the .cu files; `stream` is a cudaStream_t)
+using stream_t = void*;
+
+// geometry + shadowing (atpm_geom.cu)
+struct GeomWork {
+    double* hp;      // [nv][ntau][3] heliocentric vertex positions
+    double* hm;      // [nf][ntau][3] heliocentric facet midpoints
+    double* nrm;     // [nf][ntau][3] unit normals
+    double* dist;    // [nf][ntau] |hm|
+    const double* rot;  // [ntau][2] cos, sin of the rotation angle (host libm)
+    double tm[9];    // pole transformation matrix
+    double car[3];   // heliocentric centre (km)
+};
+int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t st);
+int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t st);
+int launch_shadow_allpairs(const DevSolve& s, const GeomWork& g, stream_t st);
+
+// scattering (atpm_scatter.cu)
+int launch_single_scattering(const DevSolve& s, stream_t st);
+int launch_multiple_scattering(const DevSolve& s, void* work, stream_t st);
+size_t multiple_scattering_work_bytes(const DevSolve& s);
+int launch_forcing_transpose(const DevSolve& s, stream_t st);
+int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* illum_d, stream_t st);
+
+// thermal (atpm_thermal.cu); batched over `n` solves in `tab` (device array)
+struct Batch {
+    const DevSolve* tab;     // device [n]
+    int n;
+    const int4* wmap;        // W/Q tile map: {solve, f0, s0, 0}
+    int nw;
+    const int2* fmap;        // facet-block map: {solve, f0}
+    int nfb;
+    int mode, nx;
+    PowTab p4, p3;
+};
+int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
+int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);
+int launch_fill_initial(const DevSolve& s, const void* t_init, stream_t st);
+int launch_energy_balance(const DevSolve& s, stream_t st);
+bool conduction_nx_supported(int nx);
+
+// pow exception tables (atpm_powtab.cpp)
+struct HostPowTab {
+    uint2* slots_dev = nullptr;
+    uint32_t log2slots = 0, lo_bits = 0, hi_bits = 0;
+    int64_t exceptions = 0;
+};
+// builds the table for exponent e in {3, 4} over [2^-4, 2^12) and uploads it
+int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen);
+// host emulation of the device's double-float x^e (exact IEEE ops)
+float emu_pow3(float x);
+float emu_pow4(float x);
+
+}  // namespace atpm

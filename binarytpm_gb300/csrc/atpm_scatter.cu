@@ -1,0 +1,212 @@
+// Scattered-sunlight kernels (reference singlescattering / multiplescattering,
+// 3905/Thermal/NominalPole/main.cpp:1321-1433).
+//
+//   k_single_scatter  E[f][s] = S cos_f shadow_f + sum_k vf_k S A cos_g shadow_g
+//                     warp = 32 steps of one facet: the list loop is uniform
+//                     and every gather of cos/shadow is one coalesced segment
+//   k_multi_gs        the reference's per-step Gauss-Seidel sweep in facet
+//                     order (values of facets before f in this sweep, after f
+//                     from the last sweep) until every |change| <= accuracy;
+//                     one warp per step, lanes fetch 32 list entries at once
+//                     and the two partial sums are accumulated in list order
+//   k_forcing_t       [nf][ntau] -> [ntau][nf] for the conduction sweep
+#include <cuda_runtime.h>
+
+#include "atpm_internal.h"
+
+namespace atpm {
+
+template <int MODE> struct Sa;
+template <> struct Sa<MODE_REF> {
+    using R = float;
+    static __device__ __forceinline__ R add(R a, R b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ R sub(R a, R b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ R mul(R a, R b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ R div(R a, R b) { return __fdiv_rn(a, b); }
+};
+template <> struct Sa<MODE_FP64> {
+    using R = double;
+    static __device__ __forceinline__ R add(R a, R b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ R sub(R a, R b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ R mul(R a, R b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ R div(R a, R b) { return __ddiv_rn(a, b); }
+};
+template <> struct Sa<MODE_FAST> {
+    using R = float;
+    static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+    static __device__ __forceinline__ R sub(R a, R b) { return a - b; }
+    static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
+    static __device__ __forceinline__ R div(R a, R b) { return a / b; }
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_single_scatter(DevSolve sv) {
+    using A = Sa<MODE>;
+    using R = typename A::R;
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int f = blockIdx.y * blockDim.y + threadIdx.y;
+    const int s = blockIdx.x * 32 + threadIdx.x;
+    if (f >= nf) return;
+    const R* cs = static_cast<const R*>(sv.cosil);
+    const R solar = (MODE == MODE_FP64) ? (R)sv.solar_d : (R)sv.solar;
+    const R alb = (MODE == MODE_FP64) ? (R)sv.alb_d : (R)sv.alb;
+    const bool ok = s < ntau;
+    const int sc = ok ? s : 0;
+    R e = A::mul(A::mul(solar, cs[(size_t)f * ntau + sc]), (R)sv.shadow[(size_t)f * ntau + sc]);
+    const int k1 = sv.dep_ptr[f + 1];
+    for (int k = sv.dep_ptr[f]; k < k1; ++k) {
+        const int g = __ldg(&sv.dep_idx[k]);
+        const R v = (R)__ldg(&sv.dep_vf[k]);
+        const size_t o = (size_t)g * ntau + sc;
+        e = A::add(e, A::mul(A::mul(A::mul(A::mul(v, solar), alb), cs[o]), (R)sv.shadow[o]));
+    }
+    if (ok) static_cast<R*>(sv.Efm)[(size_t)f * ntau + s] = e;
+}
+
+// Gauss-Seidel multiple scattering, one warp per step.  `work` holds three
+// [ntau][nf] arrays: solar power, previous sweep, current sweep.
+template <int MODE>
+__global__ void __launch_bounds__(32) k_multi_gs(DevSolve sv, void* work, int cap) {
+    using A = Sa<MODE>;
+    using R = typename A::R;
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int s = blockIdx.x;
+    const int lane = threadIdx.x;
+    if (s >= ntau) return;
+    R* sp = static_cast<R*>(work) + (size_t)s * nf;
+    R* po = sp + (size_t)ntau * nf;
+    R* pn = po + (size_t)ntau * nf;
+    const R* cs = static_cast<const R*>(sv.cosil);
+    R* Efm = static_cast<R*>(sv.Efm);
+    const R solar = (MODE == MODE_FP64) ? (R)sv.solar_d : (R)sv.solar;
+    const R alb = (MODE == MODE_FP64) ? (R)sv.alb_d : (R)sv.alb;
+    const R acc = (MODE == MODE_FP64) ? (R)sv.sacc_d : (R)sv.sacc;
+    for (int c = lane; c < nf; c += 32) {
+        const size_t o = (size_t)c * ntau + s;
+        sp[c] = A::mul(A::mul(solar, cs[o]), (R)sv.shadow[o]);
+        po[c] = A::mul(alb, Efm[o]);
+    }
+    __syncwarp();
+    bool more = true;
+    int it = 0;
+    while (more) {
+        if (it == cap) {
+            if (lane == 0) atomicOr(sv.status, ST_SCATTER_CAP);
+            break;
+        }
+        for (int c = 0; c < nf; ++c) {
+            const int d0 = sv.dep_ptr[c], d1 = sv.dep_ptr[c + 1];
+            R val;
+            if (d1 == d0) {
+                val = po[c];
+            } else {
+                R after = R(0), before = R(0);
+                for (int base = d0; base < d1; base += 32) {
+                    const int k = base + lane;
+                    R term = R(0);
+                    int isafter = 0;
+                    if (k < d1) {
+                        const int g = __ldg(&sv.dep_idx[k]);
+                        const R v = (R)__ldg(&sv.dep_vf[k]);
+                        isafter = g > c;
+                        term = A::mul(v, isafter ? po[g] : pn[g]);
+                    }
+                    const int n = min(32, d1 - base);
+                    for (int j = 0; j < n; ++j) {
+                        const R tj = __shfl_sync(0xffffffffu, term, j);
+                        const int aj = __shfl_sync(0xffffffffu, isafter, j);
+                        if (aj) after = A::add(after, tj);
+                        else before = A::add(before, tj);
+                    }
+                }
+                val = A::mul(alb, A::add(A::add(sp[c], after), before));
+            }
+            if (lane == 0) pn[c] = val;
+            __syncwarp();
+        }
+        int test = 0;
+        for (int c = lane; c < nf; c += 32) {
+            const R d = A::sub(pn[c], po[c]);
+            if ((d < R(0) ? -d : d) > acc) test = 1;
+            po[c] = pn[c];
+        }
+        more = __any_sync(0xffffffffu, test) != 0;
+        __syncwarp();
+        ++it;
+    }
+    for (int c = lane; c < nf; c += 32) Efm[(size_t)c * ntau + s] = A::div(pn[c], alb);
+}
+
+// [nf][ntau] -> [ntau][nf]
+template <class R>
+__global__ void __launch_bounds__(256) k_forcing_t(const R* src, R* dst, int nf, int ntau) {
+    __shared__ R sm[32][33];
+    const int f0 = blockIdx.y * 32, s0 = blockIdx.x * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int f = f0 + j, s = s0 + threadIdx.x;
+        sm[j][threadIdx.x] = (f < nf && s < ntau) ? src[(size_t)f * ntau + s] : R(0);
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int s = s0 + j, f = f0 + threadIdx.x;
+        if (f < nf && s < ntau) dst[(size_t)s * nf + f] = sm[threadIdx.x][j];
+    }
+}
+
+template <class R>
+__global__ void k_set_forcing(DevSolve sv, const int32_t* shadow, const float* illum) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n = (size_t)sv.nf * sv.ntau;
+    if (i >= n) return;
+    sv.shadow[i] = shadow[i] ? 1 : 0;
+    static_cast<R*>(sv.Efm)[i] = (R)illum[i];
+}
+
+// ------------------------------------------------------------------ launchers
+int launch_single_scattering(const DevSolve& s, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
+    switch (s.mode) {
+        case MODE_REF: k_single_scatter<MODE_REF><<<grd, blk, 0, st>>>(s); break;
+        case MODE_FP64: k_single_scatter<MODE_FP64><<<grd, blk, 0, st>>>(s); break;
+        default: k_single_scatter<MODE_FAST><<<grd, blk, 0, st>>>(s); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+size_t multiple_scattering_work_bytes(const DevSolve& s) {
+    const size_t rs = (s.mode == MODE_FP64) ? 8 : 4;
+    return 3 * (size_t)s.ntau * s.nf * rs;
+}
+
+int launch_multiple_scattering(const DevSolve& s, void* work, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const int cap = 1000;  // the reference iterates unbounded; real cases need < 50 sweeps
+    switch (s.mode) {
+        case MODE_REF: k_multi_gs<MODE_REF><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
+        case MODE_FP64: k_multi_gs<MODE_FP64><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
+        default: k_multi_gs<MODE_FAST><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_forcing_transpose(const DevSolve& s, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 31) / 32);
+    if (s.mode == MODE_FP64)
+        k_forcing_t<double><<<grd, blk, 0, st>>>(static_cast<const double*>(s.Efm), static_cast<double*>(s.E), s.nf, s.ntau);
+    else
+        k_forcing_t<float><<<grd, blk, 0, st>>>(static_cast<const float*>(s.Efm), static_cast<float*>(s.E), s.nf, s.ntau);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* illum_d, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t n = (size_t)s.nf * s.ntau;
+    const int g = (int)((n + 255) / 256);
+    if (s.mode == MODE_FP64) k_set_forcing<double><<<g, 256, 0, st>>>(s, shadow_d, illum_d);
+    else k_set_forcing<float><<<g, 256, 0, st>>>(s, shadow_d, illum_d);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+}  // namespace atpm

@@ -1,0 +1,436 @@
+// Per-revolution thermal kernels, batched over solves.
+//
+// One revolution of the reference (inertiadifference,
+// 3905/Thermal/NominalPole/main.cpp:1473-1557) advances every non-converged
+// facet through NTAU steps of FTCS conduction + a Newton-Raphson radiative
+// surface boundary.  Its self-heating flux reads only previous-revolution
+// surface temperatures (main.cpp:1505-1527), so the revolution splits into
+//
+//   k_selfheat_w   W[f][s] = eps*sigma*T_{r-1}[s][f]^4          (transpose)
+//   k_selfheat_q   Q[s][f] = sum_k W[g_k][s] * vf_k  (list order)  -- A6
+//   k_conduction   depth column in registers, NTAU steps, Newton BC -- A1
+//   k_converge     shape_converged (main.cpp:1876-1909)             -- A4
+//   k_advance      revolution counter / stop rule (main.cpp:2522-2539)
+//
+// All five read the per-solve control word and return at once for solves
+// that have stopped, so the same launch sequence (or a captured graph of it)
+// can be replayed until every solve in the batch is done.
+#include <cuda_runtime.h>
+
+#include "atpm_internal.h"
+
+namespace atpm {
+
+// ------------------------------------------------------------------ arithmetic
+template <int MODE> struct Ar;
+template <> struct Ar<MODE_REF> {
+    using R = float;
+    static __device__ __forceinline__ R add(R a, R b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ R sub(R a, R b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ R mul(R a, R b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ R div(R a, R b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ R fabs_(R a) { return fabsf(a); }
+};
+template <> struct Ar<MODE_FP64> {
+    using R = double;
+    static __device__ __forceinline__ R add(R a, R b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ R sub(R a, R b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ R mul(R a, R b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ R div(R a, R b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ R fabs_(R a) { return fabs(a); }
+};
+template <> struct Ar<MODE_FAST> {
+    using R = float;
+    static __device__ __forceinline__ R add(R a, R b) { return a + b; }
+    static __device__ __forceinline__ R sub(R a, R b) { return a - b; }
+    static __device__ __forceinline__ R mul(R a, R b) { return a * b; }
+    static __device__ __forceinline__ R div(R a, R b) { return a / b; }
+    static __device__ __forceinline__ R fabs_(R a) { return fabsf(a); }
+};
+
+// double-float x^4 / x^3 (bit-identical to emu_pow4 / emu_pow3 on the host)
+__device__ __forceinline__ float dev_pow4(float x) {
+    float h = __fmul_rn(x, x);
+    float l = __fmaf_rn(x, x, -h);
+    float p = __fmul_rn(h, h);
+    float e = __fmaf_rn(h, h, -p);
+    float c = __fmaf_rn(__fmul_rn(2.0f, h), l, e);
+    return __fadd_rn(p, c);
+}
+__device__ __forceinline__ float dev_pow3(float x) {
+    float h = __fmul_rn(x, x);
+    float l = __fmaf_rn(x, x, -h);
+    float p = __fmul_rn(h, x);
+    float e = __fmaf_rn(h, x, -p);
+    float c = __fmaf_rn(l, x, e);
+    return __fadd_rn(p, c);
+}
+
+// libm-exact result: table hit -> libm's value, miss -> the double-float value
+__device__ __forceinline__ float pow_fix(const PowTab& t, float x, float v, int* status) {
+    uint32_t b = __float_as_uint(x);
+    if (b - t.lo_bits < t.hi_bits - t.lo_bits) {
+        const uint32_t mask = (1u << t.log2slots) - 1u;
+        uint32_t h = (b * 2654435761u) >> (32 - t.log2slots);
+        for (int probe = 0; probe < 1024; ++probe) {
+            uint2 kv = __ldg(&t.slots[h]);
+            if (kv.x == b) return __uint_as_float(kv.y);
+            if (kv.x == 0xFFFFFFFFu) return v;
+            h = (h + 1u) & mask;
+        }
+        return v;
+    }
+    if (x != 0.0f) atomicOr(status, ST_POW_RANGE);
+    return v;
+}
+
+template <int MODE> struct Pw;
+template <> struct Pw<MODE_REF> {
+    static __device__ __forceinline__ float p4(const PowTab& t, float x, int* st) { return pow_fix(t, x, dev_pow4(x), st); }
+    static __device__ __forceinline__ float p3(const PowTab& t, float x, int* st) { return pow_fix(t, x, dev_pow3(x), st); }
+};
+template <> struct Pw<MODE_FP64> {
+    static __device__ __forceinline__ double p4(const PowTab&, double x, int*) {
+        double t2 = __dmul_rn(x, x);
+        return __dmul_rn(t2, t2);
+    }
+    static __device__ __forceinline__ double p3(const PowTab&, double x, int*) { return __dmul_rn(__dmul_rn(x, x), x); }
+};
+template <> struct Pw<MODE_FAST> {
+    static __device__ __forceinline__ float p4(const PowTab&, float x, int*) { float t2 = x * x; return t2 * t2; }
+    static __device__ __forceinline__ float p3(const PowTab&, float x, int*) { return x * x * x; }
+};
+
+// per-mode scalar views of DevSolve
+template <int MODE> struct Sc {
+    using R = typename Ar<MODE>::R;
+    R ti, oma, es, es4, m1, r, tacc, tacc10;
+    __device__ __forceinline__ void load(const DevSolve& s) {
+        if constexpr (MODE == MODE_FP64) {
+            ti = s.ti_d; oma = s.oma_d; es = s.es_d; es4 = s.es4_d; m1 = s.m1_d; r = s.r_d;
+            tacc = s.tacc_d; tacc10 = s.tacc10_d;
+        } else {
+            ti = s.ti; oma = s.oma; es = s.es; es4 = s.es4; m1 = s.m1; r = s.r;
+            tacc = s.tacc; tacc10 = s.tacc10;
+        }
+    }
+};
+
+// ------------------------------------------------------------- self-heating
+// W[f][s] = (eps*sigma) * T[s][f]^4 over a 32x32 tile, transposed in shared memory
+template <int MODE>
+__global__ void __launch_bounds__(256) k_selfheat_w(Batch b) {
+    using A = Ar<MODE>;
+    using R = typename A::R;
+    const int4 t = b.wmap[blockIdx.x];
+    const DevSolve& sv = b.tab[t.x];
+    if (!sv.ctl->active || sv.nnz == 0) return;
+    __shared__ R sm[32][33];
+    const int nf = sv.nf, ntau = sv.ntau;
+    const R* T = static_cast<const R*>(sv.stemp1);
+    R* W = static_cast<R*>(sv.W);
+    Sc<MODE> c;
+    c.load(sv);
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int s = t.z + j, f = t.y + threadIdx.x;
+        R v = R(0);
+        if (s < ntau && f < nf) v = A::mul(c.es, Pw<MODE>::p4(b.p4, T[(size_t)s * nf + f], sv.status));
+        sm[j][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int f = t.y + j, s = t.z + threadIdx.x;
+        if (f < nf && s < ntau) W[(size_t)f * ntau + s] = sm[threadIdx.x][j];
+    }
+}
+
+// Q[s][f] = sum over f's list of W[g][s] * vf, accumulated in list order
+// (main.cpp:1519-1529).  Warp w of the block owns facet f0+w, lane l owns
+// step s0+l, so the list loop is warp-uniform and every W load is a
+// coalesced 128-byte row segment.
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_selfheat_q(Batch b) {
+    using A = Ar<MODE>;
+    using R = typename A::R;
+    const int4 t = b.wmap[blockIdx.x];
+    const DevSolve& sv = b.tab[t.x];
+    if (!sv.ctl->active) return;
+    __shared__ R sm[32][33];
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int f = t.y + threadIdx.y, s = t.z + threadIdx.x;
+    const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
+    R q = R(0);
+    if (f < nf && s < ntau && (inst || !sv.conv[f])) {
+        const R* W = static_cast<const R*>(sv.W);
+        const int k1 = sv.dep_ptr[f + 1];
+        for (int k = sv.dep_ptr[f]; k < k1; ++k) {
+            const int g = __ldg(&sv.dep_idx[k]);
+            const R v = (R)__ldg(&sv.dep_vf[k]);
+            q = A::add(q, A::mul(W[(size_t)g * ntau + s], v));
+        }
+    }
+    sm[threadIdx.y][threadIdx.x] = q;
+    __syncthreads();
+    const int so = t.z + threadIdx.y, fo = t.y + threadIdx.x;
+    if (so < ntau && fo < nf) static_cast<R*>(sv.Q)[(size_t)so * nf + fo] = sm[threadIdx.x][threadIdx.y];
+}
+
+// --------------------------------------------------------------- conduction
+// One thread owns one facet's depth column (NX+1 nodes in registers) for a
+// whole revolution.  Per step it reads E, Q and the previous-revolution
+// surface temperature (coalesced across the warp), applies the FTCS update of
+// main.cpp:1510-1515, the Newton boundary of main.cpp:1533-1542 and the
+// Neumann bottom of main.cpp:1549, and records whether |stemp1-stemp0| >= TACC
+// (the shape_converged test) so no stemp history has to be re-read.
+template <int MODE, int NX>
+__device__ __forceinline__ void column_revolution(const DevSolve& sv, const Batch& b, int f) {
+    using A = Ar<MODE>;
+    using R = typename A::R;
+    const int nf = sv.nf, ntau = sv.ntau;
+    Sc<MODE> c;
+    c.load(sv);
+    R* temp = static_cast<R*>(sv.temp);
+    const R* E = static_cast<const R*>(sv.E);
+    const R* Q = static_cast<const R*>(sv.Q);
+    R* S0 = static_cast<R*>(sv.stemp0);
+    R* S1 = static_cast<R*>(sv.stemp1);
+    R T[NX + 1];
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) T[i] = temp[(size_t)i * nf + f];
+    bool hot = false;
+    const int cap = sv.newton_cap;
+    int flags = 0;
+    for (int s = 0; s < ntau; ++s) {
+        const size_t o = (size_t)s * nf + f;
+        const R old = S1[o];
+        S0[o] = old;
+        R t0 = T[0];
+#pragma unroll
+        for (int i = 1; i < NX; ++i) {
+            const R t1 = T[i];
+            T[i] = A::add(T[i], A::mul(c.r, A::add(A::sub(T[i + 1], A::mul(R(2), T[i])), t0)));
+            t0 = t1;
+        }
+        const R a = A::add(A::mul(c.oma, E[o]), Q[o]);
+        R TR0 = T[0], TR1 = T[0], DT = R(1);
+        int it = 0;
+        while (DT >= c.tacc10) {
+            if (it == cap) { flags |= ST_NEWTON_CAP; break; }
+            const R sbc = A::sub(A::add(a, A::mul(c.m1, A::sub(T[1], TR0))),
+                                 A::mul(c.es, Pw<MODE>::p4(b.p4, TR0, sv.status)));
+            const R sbcd = A::add(c.m1, A::mul(c.es4, Pw<MODE>::p3(b.p3, TR0, sv.status)));
+            TR1 = A::add(TR0, A::div(sbc, sbcd));
+            DT = A::fabs_(A::sub(TR1, TR0));
+            TR0 = TR1;
+            ++it;
+        }
+        T[0] = TR1;
+        S1[o] = TR1;
+        T[NX] = T[NX - 1];
+        hot = hot || (A::fabs_(A::sub(TR1, old)) >= c.tacc);
+        if (!isfinite(TR1)) flags |= ST_NONFINITE;
+    }
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = T[i];
+    sv.hot[f] = hot ? 1 : 0;
+    if (flags) atomicOr(sv.status, flags);
+}
+
+// instequilibrium (main.cpp:1563-1612): every facet, every step, no depth
+template <int MODE>
+__device__ __forceinline__ void column_equilibrium(const DevSolve& sv, int f) {
+    using A = Ar<MODE>;
+    using R = typename A::R;
+    const int nf = sv.nf, ntau = sv.ntau;
+    Sc<MODE> c;
+    c.load(sv);
+    const R* E = static_cast<const R*>(sv.E);
+    const R* Q = static_cast<const R*>(sv.Q);
+    R* S0 = static_cast<R*>(sv.stemp0);
+    R* S1 = static_cast<R*>(sv.stemp1);
+    bool hot = false;
+    for (int s = 0; s < ntau; ++s) {
+        const size_t o = (size_t)s * nf + f;
+        const R old = S1[o];
+        S0[o] = old;
+        const R x = A::div(A::add(A::mul(c.oma, E[o]), Q[o]), c.es);
+        R tn;
+        if constexpr (MODE == MODE_FP64) tn = sqrt(sqrt(x));
+        else tn = (float)sqrt(sqrt((double)x));
+        S1[o] = tn;
+        hot = hot || (A::fabs_(A::sub(tn, old)) >= c.tacc);
+    }
+    sv.hot[f] = hot ? 1 : 0;
+}
+
+template <int MODE, int NX>
+__global__ void __launch_bounds__(128) k_conduction(Batch b) {
+    const int2 fb = b.fmap[blockIdx.x];
+    const DevSolve& sv = b.tab[fb.x];
+    if (!sv.ctl->active) return;
+    const int f = fb.y + threadIdx.x;
+    if (f >= sv.nf) return;
+    const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
+    if (inst) { column_equilibrium<MODE>(sv, f); return; }
+    if (sv.conv[f]) return;
+    column_revolution<MODE, NX>(sv, b, f);
+}
+
+// -------------------------------------------------------------- convergence
+__global__ void __launch_bounds__(128) k_converge(Batch b) {
+    const int2 fb = b.fmap[blockIdx.x];
+    const DevSolve& sv = b.tab[fb.x];
+    if (!sv.ctl->active) return;
+    const int rev = sv.ctl->rev;
+    if (rev <= 5) return;
+    const int f = fb.y + threadIdx.x;
+    int c = 0;
+    if (f < sv.nf) {
+        const bool ok = !sv.hot[f];
+        if (ok) { sv.conv[f] = 1; c = 1; }
+    }
+    c = __syncthreads_count(c);
+    if (threadIdx.x == 0 && c) atomicAdd(&sv.counts[rev], c);
+}
+
+__global__ void k_advance(Batch b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    const DevSolve& sv = b.tab[i];
+    Ctl* ctl = sv.ctl;
+    if (!ctl->active) return;
+    const int rev = ctl->rev;
+    if (rev > 5) {
+        const int n = sv.counts[rev];
+        ctl->numconv = n;
+        ctl->converged = (n == sv.nf) ? 1 : 0;
+    } else {
+        sv.counts[rev] = ctl->numconv;
+    }
+    ctl->rev = rev + 1;
+    if (ctl->converged || rev + 1 >= sv.revcap || (*sv.status & ST_NONFINITE)) ctl->active = 0;
+}
+
+// ------------------------------------------------------------- initial state
+template <int MODE>
+__global__ void k_initial_mean(DevSolve sv, void* out) {
+    using A = Ar<MODE>;
+    using R = typename A::R;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= sv.nf) return;
+    const R* E = static_cast<const R*>(sv.E);
+    const R inv = A::div(R(1), (R)sv.ntau);
+    R t = R(0);
+    for (int s = 0; s < sv.ntau; ++s) t = A::add(t, A::mul(inv, E[(size_t)s * sv.nf + f]));
+    static_cast<R*>(out)[f] = t;
+}
+
+template <class R>
+__global__ void k_fill_initial(DevSolve sv, const R* t0) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= sv.nf) return;
+    const R v = t0[f];
+    R* temp = static_cast<R*>(sv.temp);
+    R* S0 = static_cast<R*>(sv.stemp0);
+    R* S1 = static_cast<R*>(sv.stemp1);
+    for (int i = 0; i <= sv.nx; ++i) temp[(size_t)i * sv.nf + f] = v;
+    for (int s = 0; s < sv.ntau; ++s) { S0[(size_t)s * sv.nf + f] = v; S1[(size_t)s * sv.nf + f] = v; }
+}
+
+// FP64 energy balance of the current revolution: sums over facets and steps
+// of absorbed flux (1-A)E + Q, emitted eps*sigma*T^4 and T.
+template <int MODE>
+__global__ void k_energy(DevSolve sv) {
+    using R = typename Ar<MODE>::R;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    double ab = 0.0, em = 0.0, tm = 0.0;
+    if (f < sv.nf) {
+        const R* E = static_cast<const R*>(sv.E);
+        const R* Q = static_cast<const R*>(sv.Q);
+        const R* S1 = static_cast<const R*>(sv.stemp1);
+        const double oma = 1.0 - (double)sv.alb_d, es = sv.es_d;
+        for (int s = 0; s < sv.ntau; ++s) {
+            const size_t o = (size_t)s * sv.nf + f;
+            const double T = (double)S1[o];
+            ab += oma * (double)E[o] + (double)Q[o];
+            em += es * (T * T) * (T * T);
+            tm += T;
+        }
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        ab += __shfl_down_sync(0xffffffffu, ab, d);
+        em += __shfl_down_sync(0xffffffffu, em, d);
+        tm += __shfl_down_sync(0xffffffffu, tm, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&sv.diag[0], ab);
+        atomicAdd(&sv.diag[1], em);
+        atomicAdd(&sv.diag[2], tm);
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+#define NX_LIST(X) X(8) X(12) X(16) X(24) X(32) X(40) X(48) X(56) X(64)
+
+bool conduction_nx_supported(int nx) {
+#define NX_CASE(n) if (nx == n) return true;
+    NX_LIST(NX_CASE)
+#undef NX_CASE
+    return false;
+}
+
+template <int MODE>
+static int launch_rev_mode(const Batch& b, cudaStream_t st) {
+    if (b.nw > 0) {
+        k_selfheat_w<MODE><<<b.nw, dim3(32, 8), 0, st>>>(b);
+        k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b);
+    }
+    switch (b.nx) {
+#define NX_CASE(n) case n: k_conduction<MODE, n><<<b.nfb, 128, 0, st>>>(b); break;
+        NX_LIST(NX_CASE)
+#undef NX_CASE
+        default: return 1;
+    }
+    k_converge<<<b.nfb, 128, 0, st>>>(b);
+    k_advance<<<(b.n + 127) / 128, 128, 0, st>>>(b);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_revolution(const Batch& b, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    switch (b.mode) {
+        case MODE_REF: return launch_rev_mode<MODE_REF>(b, st);
+        case MODE_FP64: return launch_rev_mode<MODE_FP64>(b, st);
+        case MODE_FAST: return launch_rev_mode<MODE_FAST>(b, st);
+    }
+    return 1;
+}
+
+int launch_initial_mean(const DevSolve& s, void* out, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const int g = (s.nf + 127) / 128;
+    switch (s.mode) {
+        case MODE_REF: k_initial_mean<MODE_REF><<<g, 128, 0, st>>>(s, out); break;
+        case MODE_FP64: k_initial_mean<MODE_FP64><<<g, 128, 0, st>>>(s, out); break;
+        default: k_initial_mean<MODE_FAST><<<g, 128, 0, st>>>(s, out); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_fill_initial(const DevSolve& s, const void* t0, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const int g = (s.nf + 127) / 128;
+    if (s.mode == MODE_FP64) k_fill_initial<double><<<g, 128, 0, st>>>(s, static_cast<const double*>(t0));
+    else k_fill_initial<float><<<g, 128, 0, st>>>(s, static_cast<const float*>(t0));
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_energy_balance(const DevSolve& s, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const int g = (s.nf + 127) / 128;
+    if (s.mode == MODE_FP64) k_energy<MODE_FP64><<<g, 128, 0, st>>>(s);
+    else k_energy<MODE_REF><<<g, 128, 0, st>>>(s);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+}
+
+}  // namespace atpm

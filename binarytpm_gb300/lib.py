@@ -1,0 +1,268 @@
+"""ctypes binding of libatpm (include/atpm.h) and a thin Python mirror of the
+reference driver's single_model flow (3905/Thermal/NominalPole/main.cpp:2417-2590).
+
+The CUDA library is the only compute path: if ``libatpm.so`` is missing or
+fails to load, :func:`load` raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libatpm.so"
+
+REFERENCE, FP64, FAST = 0, 1, 2
+PRECISIONS = {"reference": REFERENCE, "fp64": FP64, "fast": FAST}
+
+
+class AtpmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"atpm status {status}: {msg}")
+        self.status = status
+
+
+class Shape(C.Structure):
+    _fields_ = [("nv", C.c_int32), ("nf", C.c_int32),
+                ("vertices", C.c_void_p), ("facets", C.c_void_p),
+                ("dep_ptr", C.c_void_p), ("dep_idx", C.c_void_p), ("dep_vf", C.c_void_p)]
+
+
+class Params(C.Structure):
+    _fields_ = [("ntau", C.c_int32), ("nx", C.c_int32),
+                ("polar", C.c_double * 3), ("pole", C.c_double * 2),
+                ("rotation_period_s", C.c_float), ("albedo", C.c_float), ("emissivity", C.c_float),
+                ("tacc", C.c_float), ("scattering_accuracy", C.c_float),
+                ("shadowing", C.c_int32), ("multiple_scattering", C.c_int32),
+                ("revcap", C.c_int32), ("precision", C.c_int32)]
+
+
+_lib = None
+
+_SIGS = {
+    "atpm_status_string": (C.c_char_p, [C.c_int]),
+    "atpm_last_error": (C.c_char_p, []),
+    "atpm_version": (C.c_int32, []),
+    "atpm_context_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "atpm_context_destroy": (C.c_int, [C.c_void_p]),
+    "atpm_solve_create": (C.c_int, [C.c_void_p, C.POINTER(Shape), C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "atpm_solve_destroy": (C.c_int, [C.c_void_p]),
+    "atpm_solve_footprint": (C.c_int, [C.POINTER(Shape), C.POINTER(Params), C.POINTER(C.c_uint64)]),
+    "atpm_geometry_shadow": (C.c_int, [C.c_void_p]),
+    "atpm_scattering": (C.c_int, [C.c_void_p]),
+    "atpm_set_forcing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_set_thermal_inertia": (C.c_int, [C.c_void_p, C.c_float]),
+    "atpm_initialise_temperatures": (C.c_int, [C.c_void_p]),
+    "atpm_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "atpm_run": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_single_model": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "atpm_get_shadow": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_get_illumination": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_get_surface_temperature": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_get_surface_temperature64": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+
+def load(path: Path | None = None):
+    """Load libatpm.so (raises if it is absent: no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} not built; run __graft_entry__.build() or python -m binarytpm_gb300.build")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _ck(rc: int):
+    if rc != 0:
+        lib = load()
+        raise AtpmError(rc, lib.atpm_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        _ck(lib.atpm_context_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load().atpm_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_params(problem, precision: int, revcap: int = 301) -> Params:
+    p = Params()
+    p.ntau, p.nx = problem.ntau, problem.nx
+    for i in range(3):
+        p.polar[i] = problem.polar[i]
+    p.pole[0], p.pole[1] = problem.pole
+    p.rotation_period_s = problem.rotation_period_s
+    p.albedo = problem.albedo
+    p.emissivity = problem.emissivity
+    p.tacc = problem.tacc
+    p.scattering_accuracy = problem.scattering_accuracy
+    p.shadowing = problem.shadowing
+    p.multiple_scattering = problem.multiple_scattering
+    p.revcap = revcap
+    p.precision = precision
+    return p
+
+
+class Solve:
+    """One resident solve (shape + state on the device)."""
+
+    def __init__(self, ctx: Context, problem, precision: int = REFERENCE, revcap: int = 301):
+        lib = load()
+        self.ctx, self.problem, self.precision, self.revcap = ctx, problem, precision, revcap
+        self._keep = [np.ascontiguousarray(problem.vertices, np.float64),
+                      np.ascontiguousarray(problem.facets, np.int32),
+                      np.ascontiguousarray(problem.dep_ptr, np.int32),
+                      np.ascontiguousarray(problem.dep_idx, np.int32),
+                      np.ascontiguousarray(problem.dep_vf, np.float32)]
+        v, f, dp, di, dv = self._keep
+        sh = Shape(len(v), len(f), v.ctypes.data, f.ctypes.data, dp.ctypes.data,
+                   di.ctypes.data if len(di) else None, dv.ctypes.data if len(dv) else None)
+        self.shape = sh
+        self.params = make_params(problem, precision, revcap)
+        h = C.c_void_p()
+        _ck(lib.atpm_solve_create(ctx.h, C.byref(sh), C.byref(self.params), C.byref(h)))
+        self.h = h
+        self.nf, self.ntau, self.nx = len(f), problem.ntau, problem.nx
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().atpm_solve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # stages -----------------------------------------------------------
+    def geometry_shadow(self):
+        _ck(load().atpm_geometry_shadow(self.h))
+
+    def scattering(self):
+        _ck(load().atpm_scattering(self.h))
+
+    def set_forcing(self, shadow, illumination):
+        s = np.ascontiguousarray(shadow, np.int32)
+        e = np.ascontiguousarray(illumination, np.float32)
+        _ck(load().atpm_set_forcing(self.h, _p(s), _p(e)))
+
+    def set_thermal_inertia(self, ti: float):
+        _ck(load().atpm_set_thermal_inertia(self.h, float(ti)))
+
+    def initialise_temperatures(self):
+        _ck(load().atpm_initialise_temperatures(self.h))
+
+    def revolution(self, rev: int):
+        n, c = C.c_int32(), C.c_int32()
+        _ck(load().atpm_revolution(self.h, rev, C.byref(n), C.byref(c)))
+        return n.value, c.value
+
+    def run(self):
+        nrev = np.zeros(1, np.int32)
+        counts = np.zeros(self.revcap, np.int32)
+        _ck(load().atpm_run(self.h, _p(nrev), _p(counts)))
+        return counts[: nrev[0]].copy()
+
+    def single_model(self, ti_list):
+        ti = np.ascontiguousarray(np.atleast_1d(ti_list), np.float32)
+        nrev = np.zeros(len(ti), np.int32)
+        counts = np.zeros((len(ti), self.revcap), np.int32)
+        _ck(load().atpm_single_model(self.h, _p(ti), len(ti), _p(nrev), _p(counts), None))
+        return [counts[k, : nrev[k]].copy() for k in range(len(ti))]
+
+    # getters ------------------------------------------------------------
+    def shadow(self):
+        out = np.zeros((self.nf, self.ntau), np.int32)
+        _ck(load().atpm_get_shadow(self.h, _p(out)))
+        return out
+
+    def illumination(self):
+        out = np.zeros((self.nf, self.ntau), np.float32)
+        _ck(load().atpm_get_illumination(self.h, _p(out)))
+        return out
+
+    def surface_temperature(self):
+        s1 = np.zeros((self.nf, self.ntau), np.float32)
+        s0 = np.zeros((self.nf, self.ntau), np.float32)
+        _ck(load().atpm_get_surface_temperature(self.h, _p(s1), _p(s0)))
+        return s1, s0
+
+    def surface_temperature64(self):
+        s1 = np.zeros((self.nf, self.ntau), np.float64)
+        _ck(load().atpm_get_surface_temperature64(self.h, _p(s1)))
+        return s1
+
+    def depth_temperature(self):
+        t = np.zeros((self.nf, self.nx + 1), np.float32)
+        _ck(load().atpm_get_depth_temperature(self.h, _p(t)))
+        return t
+
+    def energy_balance(self):
+        a, e, m = C.c_double(), C.c_double(), C.c_double()
+        _ck(load().atpm_energy_balance(self.h, C.byref(a), C.byref(e), C.byref(m)))
+        return a.value, e.value, m.value
+
+    def last_run_stats(self):
+        ms, la, fs = C.c_double(), C.c_int64(), C.c_int64()
+        _ck(load().atpm_last_run_stats(self.h, C.byref(ms), C.byref(la), C.byref(fs)))
+        return ms.value, la.value, fs.value
+
+
+def batch_run(solves):
+    """Advance several solves together until each converges (atpm_batch_run)."""
+    n = len(solves)
+    arr = (C.c_void_p * n)(*[s.h.value for s in solves])
+    cap = max(s.revcap for s in solves)
+    nrev = np.zeros(n, np.int32)
+    counts = np.zeros((n, cap), np.int32)
+    _ck(load().atpm_batch_run(arr, n, _p(nrev), _p(counts)))
+    return [counts[i, : nrev[i]].copy() for i in range(n)]
+
+
+def footprint(problem, precision: int, revcap: int = 301) -> int:
+    v = np.ascontiguousarray(problem.vertices, np.float64)
+    f = np.ascontiguousarray(problem.facets, np.int32)
+    dp = np.ascontiguousarray(problem.dep_ptr, np.int32)
+    di = np.ascontiguousarray(problem.dep_idx, np.int32)
+    dv = np.ascontiguousarray(problem.dep_vf, np.float32)
+    sh = Shape(len(v), len(f), v.ctypes.data, f.ctypes.data, dp.ctypes.data,
+               di.ctypes.data if len(di) else None, dv.ctypes.data if len(dv) else None)
+    p = make_params(problem, precision, revcap)
+    out = C.c_uint64()
+    _ck(load().atpm_solve_footprint(C.byref(sh), C.byref(p), C.byref(out)))
+    return out.value

@@ -1,0 +1,159 @@
+/*
+ * atpm.h -- C ABI of the GB300-native BinaryTPM thermophysical hot path.
+ *
+ * The reference (SamuelLeeJackson/BinaryTPM) implements its hot path as C++
+ * functions over an `Asteroid&` inside one compile-time-configured program.
+ * This ABI exposes the same stages as calls on an opaque solve handle, with
+ * runtime sizes, caller-owned host buffers and device state owned by the
+ * handle.  Each entry point names the reference function it replaces.
+ *
+ * Conventions
+ *  - Every call returns atpm_status; nothing aborts.  atpm_last_error()
+ *    returns a thread-local message for the last failure.
+ *  - Host arrays are facet-major [nf][ntau], the reference's AoS order
+ *    (AstFacet::_stemp[2][NTAU], 3905/Thermal/NominalPole/main.cpp:200-206).
+ *  - Precision ATPM_REFERENCE evaluates every float expression of the
+ *    reference CPU path in its operand order (no contraction, glibc-exact
+ *    powf), so temperatures and per-revolution convergence counts are
+ *    bit-identical to the reference run.  ATPM_FP64 carries the state in
+ *    double.  ATPM_FAST is the batched FP32 path (contracted, BF16 view
+ *    factors on the tensor cores, FP32 body-centred shadowing).
+ *  - A solve handle is not thread-safe; distinct handles may be used from
+ *    distinct threads.  Each handle owns one CUDA stream.
+ */
+#ifndef ATPM_H
+#define ATPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ATPM_API __attribute__((visibility("default")))
+#else
+#define ATPM_API
+#endif
+
+typedef enum atpm_status {
+    ATPM_OK = 0,
+    ATPM_E_INVALID = 1,      /* bad argument or shape */
+    ATPM_E_CUDA = 2,         /* a CUDA runtime call failed */
+    ATPM_E_NOMEM = 3,        /* device or host allocation failed */
+    ATPM_E_UNSUPPORTED = 4,  /* size or mode outside what this build handles */
+    ATPM_E_STATE = 5,        /* call out of order (e.g. no forcing yet) */
+    ATPM_E_NONFINITE = 6,    /* a temperature became NaN/Inf */
+    ATPM_E_ITERATION = 7,    /* a device loop hit its iteration cap */
+    ATPM_E_BUDGET = 8,       /* serving: request larger than the HBM budget */
+    ATPM_E_CANCELLED = 9     /* serving: request cancelled */
+} atpm_status;
+
+typedef enum atpm_precision {
+    ATPM_REFERENCE = 0,  /* FP32, reference operand order, bit-exact */
+    ATPM_FP64 = 1,       /* plain FP64 state and arithmetic */
+    ATPM_FAST = 2        /* batched FP32 + BF16 view factors */
+} atpm_precision;
+
+/* Shape model + its view-factor lists (the reference's text mesh and
+ * <shape>_selfheating_list.txt, main.cpp:400-434).  dep_* is CSR:
+ * row f lists the facets f sees (dep_idx) and their view factors (dep_vf),
+ * in file order. */
+typedef struct atpm_shape {
+    int32_t nv, nf;
+    const double* vertices;   /* [nv][3] km, body frame */
+    const int32_t* facets;    /* [nf][3] 0-based */
+    const int32_t* dep_ptr;   /* [nf+1] */
+    const int32_t* dep_idx;   /* [nnz] */
+    const float* dep_vf;      /* [nnz] */
+} atpm_shape;
+
+/* The reference's compile-time constants (main.cpp:17-64), at run time. */
+typedef struct atpm_params {
+    int32_t ntau;              /* NTAU: steps per rotation */
+    int32_t nx;                /* NX: depth intervals to 8 skin depths */
+    double polar[3];           /* polar0 (AU), polar1, polar2 (rad) */
+    double pole[2];            /* rot0, rot1 (rad) */
+    float rotation_period_s;   /* rotation_period */
+    float albedo;              /* bond_albedo */
+    float emissivity;          /* EPS */
+    float tacc;                /* TACC (K) */
+    float scattering_accuracy; /* scattering_accuracy (W/m^2) */
+    int32_t shadowing;         /* 0 off, 1 view-factor list (Thermal), 2 all pairs (Visibility) */
+    int32_t multiple_scattering; /* 0/1 */
+    int32_t revcap;            /* revolution cap (reference: 301) */
+    int32_t precision;         /* atpm_precision */
+} atpm_params;
+
+typedef struct atpm_context atpm_context;
+typedef struct atpm_solve atpm_solve;
+
+ATPM_API const char* atpm_status_string(atpm_status s);
+ATPM_API const char* atpm_last_error(void);
+ATPM_API int32_t atpm_version(void);
+
+/* Device selection + shared tables (set_cuda_device, GPU_code.cu:600-605). */
+ATPM_API atpm_status atpm_context_create(int32_t device, atpm_context** out);
+ATPM_API atpm_status atpm_context_destroy(atpm_context* ctx);
+
+/* Upload a shape and allocate the solve's resident state
+ * (Asteroid::Asteroid + readmodel + readselfheating, main.cpp:372-434). */
+ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* shape,
+                                       const atpm_params* params, atpm_solve** out);
+ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s);
+/* Device bytes held by a solve with this shape and params (HBM admission). */
+ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* shape, const atpm_params* params,
+                                          uint64_t* bytes);
+
+/* asteroidgeometry (main.cpp:894-1048) + astshadow (main.cpp:1286-1315, or
+ * the all-pairs form of Visibility/main.cpp:674-704 when shadowing == 2). */
+ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s);
+/* singlescattering + multiplescattering (main.cpp:1321-1433). */
+ATPM_API atpm_status atpm_scattering(atpm_solve* s);
+/* Replace the forcing with caller data ([nf][ntau] shadow 0/1 and total
+ * illumination W/m^2), e.g. from a reference Thermal run. */
+ATPM_API atpm_status atpm_set_forcing(atpm_solve* s, const int32_t* shadow, const float* illumination);
+/* Thermal inertia for the next revolutions; resets the convergence status
+ * (reset_asteroid_status + the TI assignment, main.cpp:2484-2493). */
+ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti);
+/* initialisetemperatures (main.cpp:1439-1467). */
+ATPM_API atpm_status atpm_initialise_temperatures(atpm_solve* s);
+/* One revolution: inertiadifference (main.cpp:1473-1557) or, for TI == 0,
+ * instequilibrium (main.cpp:1563-1612); then shape_converged
+ * (main.cpp:1876-1909) when rev > 5.  Outputs may be NULL. */
+ATPM_API atpm_status atpm_revolution(atpm_solve* s, int32_t rev, int32_t* numconverged,
+                                     int32_t* converged);
+/* The revolution loop of single_model (main.cpp:2521-2539): revolutions
+ * until converged or revcap; counts[rev] = facets converged after rev. */
+ATPM_API atpm_status atpm_run(atpm_solve* s, int32_t* nrev, int32_t* counts);
+/* Whole single_model flow for a TI sweep with warm start (main.cpp:2417-2590,
+ * roughness off): geometry, scattering, then per TI atpm_run.
+ * nrev[nti], counts[nti][revcap]; stemp1_out (may be NULL) gets the last TI. */
+ATPM_API atpm_status atpm_single_model(atpm_solve* s, const float* ti, int32_t nti, int32_t* nrev,
+                                       int32_t* counts, float* stemp1_out);
+
+/* Batched revolution loop: every solve runs atpm_run semantics, all solves
+ * advance together in shared launches until each converges or hits revcap.
+ * Solves must share precision and nx.  nrev[n], counts[n][revcap]. */
+ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_t* nrev,
+                                    int32_t* counts);
+
+/* Host copies of the solve's state ([nf][ntau] facet-major). */
+ATPM_API atpm_status atpm_get_shadow(atpm_solve* s, int32_t* out);
+ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out);
+ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0);
+ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp1);
+ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp /* [nf][nx+1] */);
+/* FP64 diagnostics of the last revolution: sum over facets and steps of the
+ * absorbed flux, emitted flux and the mean surface temperature. */
+ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,
+                                         double* mean_temperature);
+/* Device time (ms, CUDA events on the solve's stream) of the last atpm_run /
+ * atpm_batch_run revolution loop, and launches issued inside it. */
+ATPM_API atpm_status atpm_last_run_stats(atpm_solve* s, double* device_ms, int64_t* launches,
+                                         int64_t* facet_steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATPM_H */

@@ -1,0 +1,298 @@
+"""Build recipe for the reference's own CPU code (test infrastructure only).
+
+The reference configures every program by editing compile-time constants at
+the top of its source (``3905/Thermal/NominalPole/main.cpp:17-76``,
+``3905/Shape_Selfheating/main.cpp:10-17``).  This recipe
+
+  1. reads the unmodified sources from the reference checkout (``REF_ROOT``),
+  2. rewrites the constant definitions for one configuration, inserts a few
+     instrumentation hooks (per-revolution timer and convergence count, binary
+     dumps of the forcing and temperatures at full float precision), and
+  3. writes the scratch copy to ``oracle/_ref/<tag>/`` (git-ignored) and
+     compiles it there with ``g++ -O3 -fopenmp -ffp-contract=off``.
+
+``-ffp-contract=off`` pins the x86-64 reference semantics (no fused
+multiply-add) on every host, so an aarch64 build gives the same floats.
+
+The Thermal driver links against the 20 ``extern "C"`` symbols of its GPU
+module (``3905/Thermal/NominalPole/GPU_code.cu:600-1026``); for GPU-free runs
+they come from ``oracle/ref_gpu_cpu.cpp``, a CPU restatement of that module.
+
+Where the reference checkout is absent (the GPU host), a scratch copy that was
+generated earlier is compiled as it is; without one the build fails loudly.
+Nothing here is part of the product: only tests, ``__graft_entry__.smoke`` and
+``bench.py``'s CPU baseline call it.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import re
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("ATPM_REFERENCE_ROOT", "/root/reference"))
+OUT_ROOT = HERE / "_ref"
+
+THERMAL_SRC = "3905/Thermal/NominalPole/main.cpp"
+SELFHEAT_SRC = "3905/Shape_Selfheating/main.cpp"
+VISIB_SRC = "3905/Visibility/NominalPole/main.cpp"
+CRATER_FILES = ["new_crater2.txt", "new_crater2_selfheating_list.txt",
+                "new_crater2_photovectors.txt"]
+CRATER_DIR = "3905/Thermal/NominalPole"
+
+CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-std=c++14", "-w"]
+
+
+def _sub_const(src: str, name: str, value: str) -> str:
+    pat = re.compile(r"^([ \t]*(?:const[ \t]+)?(?:int|float|double|string)[ \t]+"
+                     + re.escape(name) + r"[ \t]*=[ \t]*)[^;]*;", re.M)
+    out, n = pat.subn(lambda m: m.group(1) + value + ";", src, count=1)
+    if n != 1:
+        raise RuntimeError(f"constant {name} not found in reference source")
+    return out
+
+
+def _insert_after(src: str, start: int, anchor: str, text: str) -> str:
+    i = src.find(anchor, start)
+    if i < 0:
+        raise RuntimeError(f"anchor not found: {anchor!r}")
+    j = i + len(anchor)
+    return src[:j] + text + src[j:]
+
+
+def _replace_from(src: str, start: int, anchor: str, text: str) -> str:
+    i = src.find(anchor, start)
+    if i < 0:
+        raise RuntimeError(f"anchor not found: {anchor!r}")
+    return src[:i] + text + src[i + len(anchor):]
+
+
+def _f(x: float) -> str:
+    s = "%.9g" % x
+    if not any(ch in s for ch in ".en"):
+        s += ".0"
+    return s + "f"
+
+
+def _d(x: float) -> str:
+    return "%.17g" % x
+
+
+# Instrumentation compiled into the scratch copy of the Thermal driver.  It
+# only reads the driver's objects through their public accessors.
+_THERMAL_HOOKS = r'''
+#include <chrono>
+#include <cstdio>
+static std::chrono::steady_clock::time_point __oracle_t0;
+static double __oracle_loop_s = 0.0;
+static void __oracle_dump_forcing(Asteroid& A) {
+	FILE* fp = fopen("oracle_forcing.bin", "wb");
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { int v = C->rtnshadow(s); fwrite(&v, 4, 1, fp); }
+	}
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = C->rtntotalillumination(s); fwrite(&v, 4, 1, fp); }
+	}
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = (float)cos(C->rtnillumangle(s)); fwrite(&v, 4, 1, fp); }
+	}
+	fclose(fp);
+}
+static void __oracle_rev_begin() { __oracle_t0 = std::chrono::steady_clock::now(); }
+static void __oracle_rev_end(Asteroid& A, int rev, float ti) {
+	auto t1 = std::chrono::steady_clock::now();
+	double s = std::chrono::duration<double>(t1 - __oracle_t0).count();
+	__oracle_loop_s += s;
+	FILE* fp = fopen("oracle_revs.txt", "a");
+	fprintf(fp, "%.9g %d %d %.9g\n", ti, rev, A.rtnnumconverged(), s);
+	fclose(fp);
+	__oracle_t0 = std::chrono::steady_clock::now();
+}
+static void __oracle_dump_temps(Asteroid& A, float ti) {
+	char name[64];
+	snprintf(name, sizeof(name), "oracle_temps_%.9g.bin", ti);
+	FILE* fp = fopen(name, "wb");
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = C->rtnstemp(1, s); fwrite(&v, 4, 1, fp); }
+	}
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = C->rtnstemp(0, s); fwrite(&v, 4, 1, fp); }
+	}
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int i = 0; i != NX + 1; ++i) { float v = C->rtntemp(i); fwrite(&v, 4, 1, fp); }
+	}
+	fclose(fp);
+}
+'''
+
+
+def thermal_defaults() -> dict:
+    return dict(
+        nv=642, nf=1280, shape="shape", ntau=720, nx=56,
+        polar=(1.0, 0.0, 0.0), rot=(3.14159265358979 / 2, 0.0),
+        shadowing=1, roughness=0, multiple_scattering=1,
+        tacc=0.005, scattering_accuracy=1e-4, eps=0.9,
+        rotation_period_s=2.26 * 3600.0, albedo=0.02,
+        ti_min=200.0, ti_max=200.0, ti_step=10.0,
+        threads=1, revcap=301,
+    )
+
+
+def _tag(prefix: str, cfg: dict) -> str:
+    h = hashlib.sha1(json.dumps(cfg, sort_keys=True).encode()).hexdigest()[:12]
+    return f"{prefix}_{h}"
+
+
+def patch_thermal(cfg: dict) -> str:
+    src = (REF_ROOT / THERMAL_SRC).read_text(errors="replace")
+    c = cfg
+    src = _sub_const(src, "ASTNUMVTX", str(c["nv"]))
+    src = _sub_const(src, "ASTNUMFACE", str(c["nf"]))
+    src = _sub_const(src, "shape_filename", '"%s"' % c["shape"])
+    src = _sub_const(src, "polar0", _d(c["polar"][0]))
+    src = _sub_const(src, "polar1", _d(c["polar"][1]))
+    src = _sub_const(src, "polar2", _d(c["polar"][2]))
+    src = _sub_const(src, "rot0", _d(c["rot"][0]))
+    src = _sub_const(src, "rot1", _d(c["rot"][1]))
+    src = _sub_const(src, "NTAU", str(c["ntau"]))
+    src = _sub_const(src, "NX", str(c["nx"]))
+    src = _sub_const(src, "shape_shadowing", str(c["shadowing"]))
+    src = _sub_const(src, "roughness_thermal_model", str(c["roughness"]))
+    src = _sub_const(src, "multiple_scattering", str(c["multiple_scattering"]))
+    src = _sub_const(src, "TACC", _f(c["tacc"]))
+    src = _sub_const(src, "scattering_accuracy", _f(c["scattering_accuracy"]))
+    src = _sub_const(src, "EPS", _f(c["eps"]))
+    src = _sub_const(src, "rotation_period", _f(c["rotation_period_s"]))
+    src = _sub_const(src, "bond_albedo", _f(c["albedo"]))
+    src = _sub_const(src, "minimum_thermal_inertia", _f(c["ti_min"]))
+    src = _sub_const(src, "maximum_thermal_inertia", _f(c["ti_max"]))
+    src = _sub_const(src, "thermal_inertia_step", _f(c["ti_step"]))
+    src = _sub_const(src, "num_threads", str(c["threads"]))
+    for w in ("write_shape_shadow", "write_shape_illumination",
+              "write_shape_temperature", "write_roughness_temperature"):
+        src = _sub_const(src, w, str(c.get(w, 0)))
+    # hooks
+    i = src.find("void single_model(Asteroid& A, Surface& S) {")
+    if i < 0:
+        raise RuntimeError("single_model not found")
+    src = src[:i] + _THERMAL_HOOKS + "\n" + src[i:]
+    i = src.find("void single_model(Asteroid& A, Surface& S) {")
+    src = _insert_after(src, i, "if (multiple_scattering == 1) { multiplescattering(A); }",
+                        "\n\t__oracle_dump_forcing(A);")
+    src = _replace_from(src, i, "while (A.rtnconverged() == 0 && rev < 301) {",
+                        "__oracle_rev_begin();\n\t\twhile (A.rtnconverged() == 0 && rev < %d) {"
+                        % int(c["revcap"]))
+    j = src.find("__oracle_rev_begin();", i)
+    src = _replace_from(src, j, "rev = rev + 1;",
+                        "__oracle_rev_end(A, rev, t_inertia);\n\t\t\trev = rev + 1;")
+    j = src.find("__oracle_rev_end(A, rev, t_inertia);", i)
+    src = _insert_after(src, j, "if (roughness_thermal_model == 1) { retrieve_GPU_roughness_temperatures(A); }",
+                        "\n\t\t__oracle_dump_temps(A, t_inertia);")
+    return src
+
+
+def _gpu_module_defines(cfg: dict) -> list[str]:
+    return [f"-DREF_ASTNUMFACE={cfg['nf']}", f"-DREF_NTAU={cfg['ntau']}",
+            f"-DREF_NX={cfg['nx']}"]
+
+
+def build_thermal(cfg: dict) -> Path:
+    """Return the path of a compiled reference Thermal driver for ``cfg``."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    tag = _tag("thermal", full)
+    d = OUT_ROOT / tag
+    exe = d / "thermal"
+    src_path = d / "main.cpp"
+    if exe.exists():
+        return exe
+    d.mkdir(parents=True, exist_ok=True)
+    if not src_path.exists():
+        if not (REF_ROOT / THERMAL_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        src_path.write_text(patch_thermal(full))
+        (d / "config.json").write_text(json.dumps(full, indent=1))
+    cmd = ["g++", *CXXFLAGS, *_gpu_module_defines(full), str(src_path),
+           str(HERE / "ref_gpu_cpu.cpp"), "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def patch_selfheating(nv: int, nf: int, shape: str, threads: int) -> str:
+    src = (REF_ROOT / SELFHEAT_SRC).read_text(errors="replace")
+    src = _sub_const(src, "ASTNUMVTX", str(nv))
+    src = _sub_const(src, "ASTNUMFACE", str(nf))
+    src = _sub_const(src, "filename", '"%s"' % shape)
+    src = _sub_const(src, "num_threads", str(threads))
+    return src
+
+
+def build_selfheating(nv: int, nf: int, shape: str, threads: int = 8) -> Path:
+    cfg = dict(nv=nv, nf=nf, shape=shape, threads=threads)
+    d = OUT_ROOT / _tag("selfheating", cfg)
+    exe = d / "selfheating"
+    src_path = d / "main.cpp"
+    if exe.exists():
+        return exe
+    d.mkdir(parents=True, exist_ok=True)
+    if not src_path.exists():
+        if not (REF_ROOT / SELFHEAT_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        src_path.write_text(patch_selfheating(nv, nf, shape, threads))
+    subprocess.run(["g++", *CXXFLAGS, str(src_path), "-o", str(exe)], check=True)
+    return exe
+
+
+def patch_visibility(cfg: dict) -> str:
+    src = (REF_ROOT / VISIB_SRC).read_text(errors="replace")
+    c = cfg
+    src = _sub_const(src, "ASTNUMVTX", str(c["nv"]))
+    src = _sub_const(src, "ASTNUMFACE", str(c["nf"]))
+    src = _sub_const(src, "shape_filename", '"%s"' % c["shape"])
+    src = _sub_const(src, "rot0", _d(c["rot"][0]))
+    src = _sub_const(src, "rot1", _d(c["rot"][1]))
+    src = _sub_const(src, "ob0", _d(c["observer"][0]))
+    src = _sub_const(src, "ob1", _d(c["observer"][1]))
+    src = _sub_const(src, "ob2", _d(c["observer"][2]))
+    src = _sub_const(src, "NTAU", str(c["ntau"]))
+    src = _sub_const(src, "num_threads", str(c["threads"]))
+    src = _sub_const(src, "roughness_visibility_test", "0")
+    src = _sub_const(src, "write_roughness_visibility", "0")
+    src = _sub_const(src, "shape_visibility_test", "1")
+    src = _sub_const(src, "write_shape_visibility", "1")
+    return src
+
+
+def build_visibility(cfg: dict) -> Path:
+    """Reference Visibility driver (all-pairs occultation toward an observer)."""
+    full = dict(nv=642, nf=1280, shape="shape", ntau=720, rot=(3.14159265358979 / 2, 0.0),
+                observer=(1.0, 0.0, 0.0), threads=1)
+    full.update(cfg)
+    d = OUT_ROOT / _tag("visibility", full)
+    exe = d / "visibility"
+    src_path = d / "main.cpp"
+    if exe.exists():
+        return exe
+    d.mkdir(parents=True, exist_ok=True)
+    if not src_path.exists():
+        if not (REF_ROOT / VISIB_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        src_path.write_text(patch_visibility(full))
+    subprocess.run(["g++", *CXXFLAGS, str(src_path), str(HERE / "ref_vis_stub.cpp"), "-o", str(exe)], check=True)
+    return exe
+
+
+def crater_files() -> dict[str, str]:
+    """Text of the reference's crater (roughness) model files."""
+    return {n: (REF_ROOT / CRATER_DIR / n).read_text() for n in CRATER_FILES}
+
+
+def run(exe: Path, workdir: Path, env_threads: int | None = None, quiet: bool = True):
+    env = dict(os.environ)
+    if env_threads:
+        env["OMP_NUM_THREADS"] = str(env_threads)
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run([str(exe)], cwd=str(workdir), check=True, stdout=out, env=env)

@@ -1,0 +1,104 @@
+"""Generate the golden fixtures under tests/golden/ by running the reference's
+own programs (compiled from scratch copies by oracle/refbuild.py).
+
+For every case: seeded synthetic mesh -> reference Shape_Selfheating (view-
+factor lists) -> reference Thermal (shadows, scattered illumination, final
+temperatures, per-revolution convergence counts) or reference Visibility
+(all-pairs occultation flags).  Arrays are stored at full float precision
+through the scratch copy's binary dumps.
+
+Run here (needs the reference checkout):  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import math
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from binarytpm_gb300 import formats, mesh  # noqa: E402
+from binarytpm_gb300.problem import BINARY_POLE, binary_mesh  # noqa: E402
+from oracle import refbuild  # noqa: E402
+
+HERE = Path(__file__).resolve().parent
+
+CASES = {
+    "single_s2": dict(kind="thermal", mesh=("single", 2, 1), ntau=72, nx=8, ti=[200.0],
+                      pole=(math.pi / 2, 0.0), polar=(1.0, 0.0, 0.0), period_h=2.26,
+                      albedo=0.02, tacc=0.005),
+    "binary_s3s1": dict(kind="thermal", mesh=("binary", 3, 1), ntau=48, nx=8, ti=[50.0, 200.0],
+                        pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9,
+                        albedo=0.02, tacc=0.005),
+    "vis_s3s1": dict(kind="visibility", mesh=("binary", 3, 1), ntau=48,
+                     pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
+}
+
+
+def case_mesh(spec):
+    kind, sub, seed = spec
+    if kind == "single":
+        return mesh.perturbed_body(sub, 0.39, 0.05, seed)
+    return binary_mesh(p_subdiv=sub, s_subdiv=seed)
+
+
+def run_case(name: str, c: dict, threads: int = 8) -> dict:
+    v, f = case_mesh(c["mesh"])
+    nv, nf = len(v), len(f)
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        mesh.write_shape(wd / "shape.txt", v, f)
+        sh = refbuild.build_selfheating(nv, nf, "shape", threads)
+        refbuild.run(sh, wd)
+        ptr, idx, vf = formats.read_selfheating_list(wd / "shape_selfheating_list.txt", nf)
+        out = dict(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf)
+        if c["kind"] == "thermal":
+            cfg = dict(nv=nv, nf=nf, ntau=c["ntau"], nx=c["nx"], polar=c["polar"], rot=c["pole"],
+                       rotation_period_s=c["period_h"] * 3600.0, albedo=c["albedo"], tacc=c["tacc"],
+                       ti_min=c["ti"][0], ti_max=c["ti"][-1],
+                       ti_step=(c["ti"][1] - c["ti"][0]) if len(c["ti"]) > 1 else 10.0,
+                       threads=1)
+            exe = refbuild.build_thermal(cfg)
+            refbuild.run(exe, wd)
+            ntau = c["ntau"]
+            F = np.fromfile(wd / "oracle_forcing.bin", dtype=np.int32).reshape(3, nf, ntau)
+            out["shadow"] = np.packbits(F[0].astype(np.uint8))
+            out["illumination"] = F[1].view(np.float32).copy()
+            out["cosillum"] = F[2].view(np.float32).copy()
+            T = np.fromfile(wd / ("oracle_temps_%g.bin" % c["ti"][-1]), dtype=np.float32)
+            n = nf * ntau
+            out["stemp1"] = T[:n].reshape(nf, ntau)
+            out["stemp0"] = T[n:2 * n].reshape(nf, ntau)
+            out["temp"] = T[2 * n:].reshape(nf, c["nx"] + 1)
+            revs = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)
+            counts = []
+            for ti in c["ti"]:
+                counts.append(revs[np.isclose(revs[:, 0], ti), 2].astype(np.int32))
+            out["counts"] = np.concatenate(counts)
+            out["counts_split"] = np.array([len(x) for x in counts], np.int32)
+        else:
+            cfg = dict(nv=nv, nf=nf, ntau=c["ntau"], rot=c["pole"], observer=c["observer"], threads=threads)
+            exe = refbuild.build_visibility(cfg)
+            refbuild.run(exe, wd)
+            flags = formats.read_values_after_header(wd / "shape_visibility.txt", nv, nf, np.int32)
+            out["visibility"] = np.packbits(flags.reshape(nf, c["ntau"]).astype(np.uint8))
+    out["case"] = np.array(json.dumps(c))
+    return out
+
+
+def main(names=None):
+    for name, c in CASES.items():
+        if names and name not in names:
+            continue
+        out = run_case(name, c)
+        np.savez_compressed(HERE / f"{name}.npz", **out)
+        print(name, {k: getattr(v, "shape", None) for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,76 @@
+"""CUDA path (libatpm via its C ABI) against the reference outputs and the oracle.
+
+REFERENCE precision must be bit-identical to the reference program's floats
+(shadows, scattered illumination, temperatures) and convergence counts.
+FP64 must match the FP64 oracle to 1e-9 K and FAST must stay within 0.01 K of
+the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(ctx, prob, precision, revcap=301):
+    from binarytpm_gb300 import lib
+
+    return lib.Solve(ctx, prob, precision=precision, revcap=revcap)
+
+
+@pytest.mark.parametrize("name", ["single_s2", "binary_s3s1"])
+def test_reference_mode_bit_exact(gpu_ctx, name):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden(name)
+    s = _solve(gpu_ctx, prob, lib.REFERENCE)
+    counts = s.single_model(prob.thermal_inertia)
+    assert np.array_equal(s.shadow(), ref["shadow"])
+    assert np.array_equal(s.illumination().view(np.uint32), ref["illumination"].view(np.uint32))
+    s1, s0 = s.surface_temperature()
+    bad = np.flatnonzero(s1.view(np.uint32) != ref["stemp1"].view(np.uint32))
+    assert bad.size == 0, f"{bad.size} temperatures differ, max {np.abs(s1 - ref['stemp1']).max()} K"
+    assert np.array_equal(s0.view(np.uint32), ref["stemp0"].view(np.uint32))
+    assert np.array_equal(s.depth_temperature().view(np.uint32), ref["temp"].view(np.uint32))
+    for got, want in zip(counts, ref["counts_list"]):
+        assert np.array_equal(got, want)
+
+
+def test_visibility_all_pairs_bit_exact(gpu_ctx):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden("vis_s3s1")
+    s = _solve(gpu_ctx, prob, lib.REFERENCE)
+    s.geometry_shadow()
+    assert np.array_equal(s.shadow(), ref["visibility"])
+
+
+@pytest.mark.parametrize("name", ["single_s2", "binary_s3s1"])
+def test_fp64_matches_fp64_oracle(gpu_ctx, name):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden(name)
+    o = oracle.single_model(prob, precision=1)
+    s = _solve(gpu_ctx, prob, lib.FP64)
+    counts = s.single_model(prob.thermal_inertia)
+    t = s.surface_temperature64()
+    assert np.max(np.abs(t - o["stemp1_64"])) < 1e-9
+    for got, want in zip(counts, o["counts"]):
+        assert np.array_equal(got, want)
+    # and the plain FP64 path stays within 0.01 K of the reference FP32 run
+    assert np.max(np.abs(t - ref["stemp1"])) < 0.01
+
+
+@pytest.mark.parametrize("name", ["single_s2", "binary_s3s1"])
+def test_fast_within_tolerance(gpu_ctx, name):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden(name)
+    o = oracle.single_model(prob, precision=1)
+    s = _solve(gpu_ctx, prob, lib.FAST)
+    s.single_model(prob.thermal_inertia)
+    t = s.surface_temperature64()
+    err = np.max(np.abs(t - o["stemp1_64"]))
+    assert err <= 0.01, err
