@@ -1,0 +1,412 @@
+#!/usr/bin/env python
+"""Benchmark: facet-steps/s of the batched FP32 thermal solve vs the plain
+FP64 GPU path on the binary-asteroid workload, with the reference's own
+OpenMP CPU code timed on this host beside it.
+
+Workload (one "step"): the synchronous binary (20,480 + 1,280 = 21,760
+facets, NX = 56, NTAU = 720, shadowing + self-heating on, TACC = 0.005 K)
+solved to convergence for a batch of 8 thermal inertias at once, starting
+from the reference's initial temperatures.  facet-steps = active facets x
+NTAU summed over the revolutions actually executed.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+Under torchrun (N > 1) every rank runs an independent replica (the solves do
+not shard); value = facet-steps of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "facet-steps/s, batched FP32 vs plain FP64 GPU at <=0.01 K; p50/p99 solve latency"
+UNIT = "facet-steps/s"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+
+
+def _peaks():
+    if PEAKS.exists():
+        d = json.loads(PEAKS.read_text())
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl" if _cuda() else "gloo")
+        dist = dist_mod
+    return world, rank, local, dist
+
+
+def _cuda():
+    import torch
+
+    return torch.cuda.is_available()
+
+
+def _max_over_ranks(x: float, dist, device) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(x: float, dist, device) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ----------------------------------------------------------------------------------------
+def reference_cpu(problem, ti: float, revs: int, threads: int):
+    """Time the reference's own Thermal program (compiled from a scratch copy by
+    oracle/refbuild.py) on this host: per-revolution wall time of its
+    revolution loop.  Returns (facet-steps/s, seconds, revolutions, threads)."""
+    from binarytpm_gb300 import formats, mesh
+    from oracle import refbuild
+
+    cfg = _ref_cfg(problem, ti, threads, revs)
+    exe = refbuild.build_thermal(cfg)
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        mesh.write_shape(wd / "shape.txt", problem.vertices, problem.facets)
+        formats.write_selfheating_list(wd / "shape_selfheating_list.txt", problem.dep_ptr, problem.dep_idx,
+                                       problem.dep_vf)
+        (wd / "shape_selfheating_vector_list.txt").write_text("")
+        (wd / "shape_photovectors.txt").write_text("0 0 0\n" * problem.nf)
+        refbuild.run(exe, wd, env_threads=threads)
+        revs_tab = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)
+    secs = float(revs_tab[:, 3].sum())
+    fs = 0
+    for r in range(len(revs_tab)):
+        active = problem.nf if r - 1 <= 5 else problem.nf - int(revs_tab[r - 1, 2])
+        fs += active * problem.ntau
+    return fs / secs, secs, len(revs_tab), threads
+
+
+def _ref_cfg(problem, ti, threads, revs):
+    return dict(nv=problem.nv, nf=problem.nf, ntau=problem.ntau, nx=problem.nx, polar=list(problem.polar),
+                rot=list(problem.pole), rotation_period_s=problem.rotation_period_s, albedo=problem.albedo,
+                tacc=problem.tacc, ti_min=ti, ti_max=ti, threads=threads, revcap=revs)
+
+
+def prepare():
+    """Write the reference scratch copy for this workload (needs the reference
+    checkout; the GPU host then compiles the copy it receives)."""
+    from binarytpm_gb300 import problem as P
+    from oracle import refbuild
+
+    v, f = P.binary_mesh(5, 3, 2)
+    prob = P.Problem(vertices=v, facets=f, dep_ptr=None, dep_idx=None, dep_vf=None, ntau=720, nx=56,
+                     polar=(1.0, 0.0, 0.0), pole=P.BINARY_POLE, rotation_period_s=11.9 * 3600.0,
+                     albedo=0.02, tacc=0.005)
+    return refbuild.thermal_source(_ref_cfg(prob, 200.0, 1, 3))
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    from binarytpm_gb300 import lib, workloads
+
+    ctx = lib.Context(0)
+    prob = workloads.binary_problem(ctx)
+    ctx.close()
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.steps):
+        v, secs, nrev, _ = reference_cpu(prob, 200.0, 3, threads)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "binary 20480+1280 facets, NX=56, NTAU=720, TI=200, reference OpenMP CPU",
+                       "sample": "3 revolutions per step (all facets active)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference",
+                             "sample": "reference Thermal revolution loop, 3 revolutions of the binary at TI=200"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU reference timing")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
+    args = ap.parse_args()
+    if args.prepare:
+        print(prepare())
+        return
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import torch
+
+    from binarytpm_gb300 import lib, workloads
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = lib.Context(local)
+    t_setup = time.perf_counter()
+    prob = workloads.binary_problem(ctx)
+    tis = workloads.BATCH_TI
+    s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    s0.geometry_shadow()
+    s0.scattering()
+    shadow, illum = s0.shadow(), s0.illumination()
+    solves = [s0] + [lib.Solve(ctx, prob, precision=lib.FAST) for _ in tis[1:]]
+    for s in solves[1:]:
+        s.set_forcing(shadow, illum)
+    setup_s = time.perf_counter() - t_setup
+
+    def step():
+        for s, ti in zip(solves, tis):
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+        counts = lib.batch_run(solves)
+        ms, launches, fs = s0.last_run_stats()
+        return ms, launches + 2 * len(solves), fs, counts
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _barrier(dist)
+    clk = Clocks(local)
+    clk.start()
+    t0 = time.perf_counter()
+    dev_ms, launches, fsteps, nrevs = 0.0, 0, 0, []
+    for _ in range(args.steps):
+        ms, la, fs, counts = step()
+        dev_ms += ms
+        launches += la
+        fsteps += fs
+        nrevs.append([len(c) for c in counts])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.stop()
+    _barrier(dist)
+    dev_ms_max = _max_over_ranks(dev_ms, dist, dev)
+    fsteps_all = _sum_over_ranks(float(fsteps), dist, dev)
+    value = fsteps_all / (dev_ms_max / 1e3)
+    wall_value = fsteps_all / _max_over_ranks(wall, dist, dev)
+
+    # per-kernel durations of one instrumented revolution of the same batch
+    kern = lib.profile_revolution(solves)
+    fast_T = [s.surface_temperature64() for s in solves]
+
+    # plain FP64 GPU path: one solve at a time, same thermal inertias
+    fp64 = None
+    err = None
+    if not args.no_fp64:
+        p = lib.Solve(ctx, prob, precision=lib.FP64)
+        p.set_forcing(shadow, illum)
+        f64_ms, f64_fs, errs, ferrs = 0.0, 0, [], []
+        cos = None
+        for ti, tf in zip(tis, fast_T):
+            p.set_thermal_inertia(ti)
+            p.initialise_temperatures()
+            p.run()
+            ms, _, fs = p.last_run_stats()
+            f64_ms += ms
+            f64_fs += fs
+            t64 = p.surface_temperature64()
+            errs.append(float(np.max(np.abs(tf - t64))))
+            if cos is None:
+                cos = s0.cosillum()
+            F64 = workloads.disk_flux(prob, t64, cos, shadow)
+            F32 = workloads.disk_flux(prob, tf, cos, shadow)
+            ferrs.append(float(np.max(np.abs(F32 - F64) / np.abs(F64))))
+        p.close()
+        fp64 = {"value": f64_fs / (f64_ms / 1e3), "unit": UNIT, "device_ms": f64_ms, "facet_steps": f64_fs,
+                "mode": "plain FP64, one solve at a time"}
+        err = {"max_temperature_error_K": max(errs), "max_rel_flux_error_12um": max(ferrs),
+               "per_ti_max_K": dict(zip([str(t) for t in tis], errs))}
+
+    # end to end through the C ABI from host buffers
+    e2e = e2e_run(ctx, prob, tis, max(1, min(args.steps, 2)))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, secs, nrev, th = reference_cpu(prob, 200.0, 3, os.cpu_count() or 1)
+            cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "reference",
+                   "sample": f"reference Thermal revolution loop, {nrev} revolutions of the binary at TI=200 "
+                             f"({secs:.1f} s)"}
+        except Exception as ex:  # the checker must not hide the GPU result
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": f"failed: {ex}"}
+
+    hbm, bf16, kind = _peaks()
+    roof = _roofline(kern, solves, hbm, kind)
+    lat = [n * (dev_ms / args.steps) / max(max(x) for x in nrevs) for x in nrevs for n in x]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "binary asteroid 20480+1280 facets, NX=56, NTAU=720, batch of 8 thermal inertias "
+                               "solved to convergence (TACC=0.005 K)",
+                   "thermal_inertia": tis, "precision": "FAST (batched FP32)", "parallelism": "replicas",
+                   "l2": "state per step 8 x 250 MB > L2 (inputs larger than L2)",
+                   "revolutions_per_solve": nrevs[-1], "nnz_viewfactors": int(prob.nnz)},
+        "wall_clock_value": wall_value, "setup_s": setup_s,
+        "fp64_plain": fp64,
+        "speedup_vs_fp64_plain": (value / fp64["value"]) if fp64 else None,
+        "errors_vs_fp64": err,
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "what": "batch start to solve convergence, device time"},
+        "roofline": roof,
+        "kernels_ms": kern,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    for s in solves:
+        s.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _roofline(kern, solves, hbm, kind):
+    """Dominant kernel: the conduction sweep.  Algorithmic bytes per active
+    facet-step: read E, Q, stemp1 (12 B) + write stemp0, stemp1 (8 B); plus
+    the depth column read and written once per revolution."""
+    k = kern.get("conduction")
+    if not k or not k["ms"]:
+        return None
+    nx = solves[0].nx
+    active_fs = k["facet_steps"]
+    cols = k["active_facets"]
+    bytes_ = active_fs * 20 + cols * 2 * (nx + 1) * 4
+    gbs = bytes_ / (k["ms"] / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "conduction_fast_nx56_traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text())
+        traffic = t["dram_bytes_per_facet_step"] * active_fs
+    flops = active_fs * (5 * (nx - 1) + 20 * 2)
+    return {"kernel": "k_conduction<FAST,56>", "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+            "frac": gbs / hbm, "peak_kind": kind, "traffic": traffic, "algorithmic_bytes": bytes_,
+            "fp32_gflops": flops / (k["ms"] / 1e3) / 1e9,
+            "note": "the sweep is FP32-issue bound; fp32_gflops against 152 SMs x 128 lanes x 2 x clock is "
+                    "the binding roofline"}
+
+
+def e2e_run(ctx, prob, tis, steps):
+    """Whole job from host buffers through the C ABI: upload shape + lists,
+    geometry/shadowing/scattering once, forcing to the other solves, batched
+    revolution loop, temperatures back to the host."""
+    from binarytpm_gb300 import lib
+
+    import torch
+
+    vals, h2d, d2h = [], 0, 0
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+        s0.geometry_shadow()
+        s0.scattering()
+        sh, il = s0.shadow(), s0.illumination()
+        solves = [s0] + [lib.Solve(ctx, prob, precision=lib.FAST) for _ in tis[1:]]
+        for s in solves[1:]:
+            s.set_forcing(sh, il)
+        for s, ti in zip(solves, tis):
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+        lib.batch_run(solves)
+        fs = solves[0].last_run_stats()[2]
+        temps = [s.surface_temperature() for s in solves]
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        vals.append(fs / dt)
+        shape_bytes = prob.vertices.nbytes + prob.facets.nbytes + prob.dep_ptr.nbytes + prob.dep_idx.nbytes + prob.dep_vf.nbytes
+        h2d = len(solves) * shape_bytes + (len(solves) - 1) * (sh.nbytes + il.nbytes)
+        d2h = sh.nbytes + il.nbytes + sum(t[0].nbytes + t[1].nbytes for t in temps)
+        for s in solves:
+            s.close()
+    return {"value": statistics.median(vals), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h),
+            "what": "C-ABI job from host arrays: solve create (H2D), geometry+shadowing+scattering, "
+                    "batched revolution loop, temperatures D2H"}
+
+
+if __name__ == "__main__":
+    main()

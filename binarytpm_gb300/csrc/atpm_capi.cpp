@@ -244,6 +244,36 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     return b;
 }
 
+
+// device table + tile maps for a set of solves (single solves reuse theirs)
+atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** tmp) {
+    atpm_solve* s0 = solves[0];
+    *tmp = nullptr;
+    if (n == 1) {
+        *out = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
+        return ATPM_OK;
+    }
+    std::vector<DevSolve> tab(n);
+    std::vector<int4> wm;
+    std::vector<int2> fm;
+    for (int i = 0; i < n; ++i) {
+        tab[i] = solves[i]->ds;
+        std::vector<int4> w1;
+        build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, fm);
+        if (solves[i]->nnz > 0) wm.insert(wm.end(), w1.begin(), w1.end());
+    }
+    const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
+    const size_t bf = align256(fm.size() * sizeof(int2));
+    CK(cudaMalloc(tmp, bt + bw + bf));
+    char* t = static_cast<char*>(*tmp);
+    CK(cudaMemcpy(t, tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice));
+    if (!wm.empty()) CK(cudaMemcpy(t + bt, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(t + bt + bw, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    *out = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + bt), (int)wm.size(),
+                      reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
+    return ATPM_OK;
+}
+
 atpm_status capture_graph(atpm_solve* s, const Batch& b, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
@@ -295,6 +325,10 @@ atpm_status get_transposed(atpm_solve* s, const void* dev, size_t rows, size_t c
     return ATPM_OK;
 }
 }  // namespace
+
+namespace atpm {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace atpm
 
 // =================================================================== C ABI
 extern "C" {
@@ -382,7 +416,7 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     char* a = static_cast<char*>(s->arena);
     DevSolve& d = s->ds;
     d.nf = s->nf; d.nv = s->nv; d.ntau = P->ntau; d.nx = P->nx; d.revcap = P->revcap;
-    d.mode = P->precision; d.nnz = s->nnz;
+    d.mode = P->precision; d.nnz = s->nnz; d.freeze = P->freeze ? 1 : 0;
     d.vert = reinterpret_cast<double*>(a + L.off[B_VERT]);
     d.fac = reinterpret_cast<int*>(a + L.off[B_FAC]);
     d.dep_ptr = reinterpret_cast<int*>(a + L.off[B_DPTR]);
@@ -658,28 +692,8 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     for (int i = 1; i < n; ++i) CK(cudaStreamSynchronize(solves[i]->st));
     Batch b;
     void* tmp = nullptr;
-    if (n == 1) {
-        b = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
-    } else {
-        std::vector<DevSolve> tab(n);
-        std::vector<int4> wm;
-        std::vector<int2> fm;
-        for (int i = 0; i < n; ++i) {
-            tab[i] = solves[i]->ds;
-            std::vector<int4> w1;
-            build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, fm);
-            if (solves[i]->nnz > 0) wm.insert(wm.end(), w1.begin(), w1.end());
-        }
-        const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
-        const size_t bf = align256(fm.size() * sizeof(int2));
-        CK(cudaMalloc(&tmp, bt + bw + bf));
-        char* t = static_cast<char*>(tmp);
-        CK(cudaMemcpy(t, tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice));
-        if (!wm.empty()) CK(cudaMemcpy(t + bt, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(t + bt + bw, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice));
-        b = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + bt), (int)wm.size(),
-                       reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
-    }
+    atpm_status rb = make_batch_for(solves, n, &b, &tmp);
+    if (rb) return rb;
     cudaGraphExec_t gx = nullptr;
     atpm_status r = capture_graph(s0, b, &gx);
     if (r) { if (tmp) cudaFree(tmp); return r; }
@@ -721,7 +735,7 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
         const int nr = ctl[i].rev;
         if (nrev) nrev[i] = nr;
         if (counts) std::memcpy(counts + (size_t)i * maxcap, cnt.data(), (size_t)s->P.revcap * 4);
-        const int64_t fs = facet_steps_from_counts(cnt.data(), nr, s->nf, s->P.ntau, s->ti == 0.0f);
+        const int64_t fs = facet_steps_from_counts(cnt.data(), nr, s->nf, s->P.ntau, s->ti == 0.0f || !s->P.freeze);
         s->last_nrev = nr;
         s->last_facet_steps = fs;
         fsteps_total += fs;
@@ -827,6 +841,66 @@ ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double
     if (absorbed) *absorbed = d[0];
     if (emitted) *emitted = d[1];
     if (mean_t) *mean_t = d[2] / n;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_get_cosillum(atpm_solve* s, float* out) {
+    if (!s || !out) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    if (s->rs == 8) {
+        std::vector<double> h(nt);
+        CK(cudaMemcpyAsync(h.data(), s->ds.cosil, nt * 8, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        for (size_t i = 0; i < nt; ++i) out[i] = (float)h[i];
+    } else {
+        CK(cudaMemcpyAsync(out, s->ds.cosil, nt * 4, cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+    }
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t n, double* kernel_ms,
+                                             int64_t* facet_steps, int64_t* active_facets) {
+    if (!solves || n < 1 || !kernel_ms) return fail(ATPM_E_INVALID, "bad arguments");
+    atpm_solve* s0 = solves[0];
+    CK(cudaSetDevice(s0->ctx->device));
+    int64_t fs = 0, act = 0;
+    for (int i = 0; i < n; ++i) {
+        atpm_solve* s = solves[i];
+        CK(cudaStreamSynchronize(s->st));
+        std::vector<uint8_t> conv(s->nf);
+        Ctl c;
+        CK(cudaMemcpy(conv.data(), s->ds.conv, s->nf, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&c, s->ds.ctl, sizeof c, cudaMemcpyDeviceToHost));
+        if (!c.active) return fail(ATPM_E_STATE, "solve %d is not active (set the thermal inertia first)", i);
+        int a = 0;
+        for (uint8_t v : conv) a += (v && s->P.freeze) ? 0 : 1;
+        act += a;
+        fs += (int64_t)a * s->P.ntau;
+    }
+    Batch b;
+    void* tmp = nullptr;
+    atpm_status rb = make_batch_for(solves, n, &b, &tmp);
+    if (rb) return rb;
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 6; ++k) CK(cudaEventCreate(&ev[k]));
+    cudaError_t e = cudaEventRecord(ev[0], s0->st);
+    for (int part = 0; part < 5 && e == cudaSuccess; ++part) {
+        if (launch_revolution_part(b, part, s0->st)) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(ev[part + 1], s0->st);
+    }
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[5]);
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        kernel_ms[k] = ms;
+    }
+    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
+    if (tmp) cudaFree(tmp);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "profile: %s", cudaGetErrorString(e));
+    if (facet_steps) *facet_steps = fs;
+    if (active_facets) *active_facets = act;
     return ATPM_OK;
 }
 

@@ -48,6 +48,7 @@ struct Ctl {
 struct DevSolve {
     int nf, nv, ntau, nx, revcap, mode;
     int nnz;
+    int freeze;             // 1: converged facets are frozen (reference)
     // shape
     const double* vert;      // [nv][3]
     const int* fac;          // [nf][3]
@@ -115,6 +116,8 @@ struct Batch {
     PowTab p4, p3;
 };
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
+// part 0 W, 1 Q, 2 conduction, 3 convergence, 4 advance
+int launch_revolution_part(const Batch& b, int part, stream_t st);
 int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);
 int launch_fill_initial(const DevSolve& s, const void* t_init, stream_t st);
 int launch_energy_balance(const DevSolve& s, stream_t st);

@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(1024) k_selfheat_q(Batch b) {
     const int f = t.y + threadIdx.y, s = t.z + threadIdx.x;
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
     R q = R(0);
-    if (f < nf && s < ntau && (inst || !sv.conv[f])) {
+    if (f < nf && s < ntau && (inst || !sv.freeze || !sv.conv[f])) {
         const R* W = static_cast<const R*>(sv.W);
         const int k1 = sv.dep_ptr[f + 1];
         for (int k = sv.dep_ptr[f]; k < k1; ++k) {
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(128) k_conduction(Batch b) {
     if (f >= sv.nf) return;
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
     if (inst) { column_equilibrium<MODE>(sv, f); return; }
-    if (sv.conv[f]) return;
+    if (sv.freeze && sv.conv[f]) return;
     column_revolution<MODE, NX>(sv, b, f);
 }
 
@@ -380,30 +380,41 @@ bool conduction_nx_supported(int nx) {
 }
 
 template <int MODE>
-static int launch_rev_mode(const Batch& b, cudaStream_t st) {
-    if (b.nw > 0) {
-        k_selfheat_w<MODE><<<b.nw, dim3(32, 8), 0, st>>>(b);
-        k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b);
-    }
-    switch (b.nx) {
+static int launch_rev_part(const Batch& b, int part, cudaStream_t st) {
+    switch (part) {
+        case 0: if (b.nw > 0) k_selfheat_w<MODE><<<b.nw, dim3(32, 8), 0, st>>>(b); break;
+        case 1: if (b.nw > 0) k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b); break;
+        case 2:
+            switch (b.nx) {
 #define NX_CASE(n) case n: k_conduction<MODE, n><<<b.nfb, 128, 0, st>>>(b); break;
-        NX_LIST(NX_CASE)
+                NX_LIST(NX_CASE)
 #undef NX_CASE
+                default: return 1;
+            }
+            break;
+        case 3: k_converge<<<b.nfb, 128, 0, st>>>(b); break;
+        case 4: k_advance<<<(b.n + 127) / 128, 128, 0, st>>>(b); break;
         default: return 1;
     }
-    k_converge<<<b.nfb, 128, 0, st>>>(b);
-    k_advance<<<(b.n + 127) / 128, 128, 0, st>>>(b);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
 }
 
-int launch_revolution(const Batch& b, stream_t stv) {
+int launch_revolution_part(const Batch& b, int part, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     switch (b.mode) {
-        case MODE_REF: return launch_rev_mode<MODE_REF>(b, st);
-        case MODE_FP64: return launch_rev_mode<MODE_FP64>(b, st);
-        case MODE_FAST: return launch_rev_mode<MODE_FAST>(b, st);
+        case MODE_REF: return launch_rev_part<MODE_REF>(b, part, st);
+        case MODE_FP64: return launch_rev_part<MODE_FP64>(b, part, st);
+        case MODE_FAST: return launch_rev_part<MODE_FAST>(b, part, st);
     }
     return 1;
+}
+
+int launch_revolution(const Batch& b, stream_t st) {
+    for (int part = 0; part < 5; ++part) {
+        const int rc = launch_revolution_part(b, part, st);
+        if (rc) return rc;
+    }
+    return 0;
 }
 
 int launch_initial_mean(const DevSolve& s, void* out, stream_t stv) {

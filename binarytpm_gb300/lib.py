@@ -36,7 +36,7 @@ class Params(C.Structure):
                 ("rotation_period_s", C.c_float), ("albedo", C.c_float), ("emissivity", C.c_float),
                 ("tacc", C.c_float), ("scattering_accuracy", C.c_float),
                 ("shadowing", C.c_int32), ("multiple_scattering", C.c_int32),
-                ("revcap", C.c_int32), ("precision", C.c_int32)]
+                ("revcap", C.c_int32), ("precision", C.c_int32), ("freeze", C.c_int32)]
 
 
 _lib = None
@@ -66,6 +66,12 @@ _SIGS = {
     "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_viewfactors_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                           C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+    "atpm_viewfactors_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_viewfactors_free": (C.c_int, [C.c_void_p]),
 }
 
 
@@ -119,7 +125,7 @@ class Context:
             pass
 
 
-def make_params(problem, precision: int, revcap: int = 301) -> Params:
+def make_params(problem, precision: int, revcap: int = 301, freeze: bool = True) -> Params:
     p = Params()
     p.ntau, p.nx = problem.ntau, problem.nx
     for i in range(3):
@@ -134,13 +140,14 @@ def make_params(problem, precision: int, revcap: int = 301) -> Params:
     p.multiple_scattering = problem.multiple_scattering
     p.revcap = revcap
     p.precision = precision
+    p.freeze = 1 if freeze else 0
     return p
 
 
 class Solve:
     """One resident solve (shape + state on the device)."""
 
-    def __init__(self, ctx: Context, problem, precision: int = REFERENCE, revcap: int = 301):
+    def __init__(self, ctx: Context, problem, precision: int = REFERENCE, revcap: int = 301, freeze: bool = True):
         lib = load()
         self.ctx, self.problem, self.precision, self.revcap = ctx, problem, precision, revcap
         self._keep = [np.ascontiguousarray(problem.vertices, np.float64),
@@ -152,7 +159,7 @@ class Solve:
         sh = Shape(len(v), len(f), v.ctypes.data, f.ctypes.data, dp.ctypes.data,
                    di.ctypes.data if len(di) else None, dv.ctypes.data if len(dv) else None)
         self.shape = sh
-        self.params = make_params(problem, precision, revcap)
+        self.params = make_params(problem, precision, revcap, freeze)
         h = C.c_void_p()
         _ck(lib.atpm_solve_create(ctx.h, C.byref(sh), C.byref(self.params), C.byref(h)))
         self.h = h
@@ -183,6 +190,7 @@ class Solve:
 
     def set_thermal_inertia(self, ti: float):
         _ck(load().atpm_set_thermal_inertia(self.h, float(ti)))
+        self._ti = float(ti)
 
     def initialise_temperatures(self):
         _ck(load().atpm_initialise_temperatures(self.h))
@@ -214,6 +222,11 @@ class Solve:
     def illumination(self):
         out = np.zeros((self.nf, self.ntau), np.float32)
         _ck(load().atpm_get_illumination(self.h, _p(out)))
+        return out
+
+    def cosillum(self):
+        out = np.zeros((self.nf, self.ntau), np.float32)
+        _ck(load().atpm_get_cosillum(self.h, _p(out)))
         return out
 
     def surface_temperature(self):
@@ -266,3 +279,45 @@ def footprint(problem, precision: int, revcap: int = 301) -> int:
     out = C.c_uint64()
     _ck(load().atpm_solve_footprint(C.byref(sh), C.byref(p), C.byref(out)))
     return out.value
+
+
+def viewfactors(ctx: Context, vertices, facets, refine: bool = True):
+    """Shape_Selfheating on the GPU: returns (dep_ptr, dep_idx, dep_vf, dep_vec, photovectors)."""
+    lib = load()
+    v = np.ascontiguousarray(vertices, np.float32)
+    f = np.ascontiguousarray(facets, np.int32)
+    h = C.c_void_p()
+    nnz = C.c_int64()
+    _ck(lib.atpm_viewfactors_compute(ctx.h, len(v), len(f), _p(v), _p(f), 1 if refine else 0,
+                                     C.byref(h), C.byref(nnz)))
+    try:
+        n = nnz.value
+        ptr = np.zeros(len(f) + 1, np.int32)
+        idx = np.zeros(n, np.int32)
+        vf = np.zeros(n, np.float32)
+        vec = np.zeros((n, 3), np.float32)
+        photo = np.zeros((len(f), 3), np.float32)
+        _ck(lib.atpm_viewfactors_get(h, _p(ptr), _p(idx), _p(vf), _p(vec), _p(photo)))
+    finally:
+        lib.atpm_viewfactors_free(h)
+    return ptr, idx, vf, vec, photo
+
+
+KERNEL_NAMES = ["selfheat_w", "selfheat_q", "conduction", "converge", "advance"]
+
+
+def profile_revolution(solves):
+    """Per-kernel device ms of one revolution of the batch (CUDA events).
+
+    The convergence flags are reset first (same thermal inertia), so every
+    facet is active, as in the early revolutions of a solve."""
+    for s in solves:
+        _ck(load().atpm_set_thermal_inertia(s.h, float(s._ti)))
+    n = len(solves)
+    arr = (C.c_void_p * n)(*[s.h.value for s in solves])
+    ms = np.zeros(5, np.float64)
+    fs, act = C.c_int64(), C.c_int64()
+    _ck(load().atpm_profile_revolution(arr, n, _p(ms), C.byref(fs), C.byref(act)))
+    out = {k: {"ms": float(v)} for k, v in zip(KERNEL_NAMES, ms)}
+    out["conduction"].update(facet_steps=fs.value, active_facets=act.value)
+    return out

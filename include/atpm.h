@@ -83,6 +83,9 @@ typedef struct atpm_params {
     int32_t multiple_scattering; /* 0/1 */
     int32_t revcap;            /* revolution cap (reference: 301) */
     int32_t precision;         /* atpm_precision */
+    int32_t freeze;            /* 1: converged facets stop updating (reference,
+                                  main.cpp:1503); 0: every facet advances every
+                                  revolution (schedule-independent comparisons) */
 } atpm_params;
 
 typedef struct atpm_context atpm_context;
@@ -144,6 +147,13 @@ ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out);
 ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0);
 ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp1);
 ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp /* [nf][nx+1] */);
+/* (float)cos of the Sun angle of every facet and step ([nf][ntau]). */
+ATPM_API atpm_status atpm_get_cosillum(atpm_solve* s, float* out);
+/* One revolution of the given (active) solves with a CUDA event between
+ * kernels: kernel_ms[5] = self-heating W, self-heating Q, conduction,
+ * convergence, advance.  Advances the solves by one revolution. */
+ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t n, double* kernel_ms,
+                                             int64_t* facet_steps, int64_t* active_facets);
 /* FP64 diagnostics of the last revolution: sum over facets and steps of the
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,
@@ -152,6 +162,23 @@ ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double
  * atpm_batch_run revolution loop, and launches issued inside it. */
 ATPM_API atpm_status atpm_last_run_stats(atpm_solve* s, double* device_ms, int64_t* launches,
                                          int64_t* facet_steps);
+
+/* ---- view factors: the Shape_Selfheating stage (3905/Shape_Selfheating/main.cpp:817-889) ----
+ * Facing screen + view factor of every facet pair (selfheating, main.cpp:628-744),
+ * occlusion culling over each facet's candidate list (hidden, main.cpp:187-368)
+ * and, when refine != 0, 10x10 sub-facet refinement of pairs with vf >= 0.05
+ * (betterviewfactors, main.cpp:374-622).  Vertices are float like the
+ * reference's reader.  The result is held until atpm_viewfactors_free. */
+typedef struct atpm_vf_result atpm_vf_result;
+ATPM_API atpm_status atpm_viewfactors_compute(atpm_context* ctx, int32_t nv, int32_t nf, const float* vertices,
+                                              const int32_t* facets, int32_t refine, atpm_vf_result** out,
+                                              int64_t* nnz);
+/* dep_ptr[nf+1], dep_idx[nnz], dep_vf[nnz], dep_vec[nnz][3] (area-weighted
+ * direction sums, main.cpp:730-732 and 592-602), photovectors[nf][3]
+ * (main.cpp:824-835); any output may be NULL. */
+ATPM_API atpm_status atpm_viewfactors_get(const atpm_vf_result* r, int32_t* dep_ptr, int32_t* dep_idx, float* dep_vf,
+                                          float* dep_vec, float* photovectors);
+ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
 
 #ifdef __cplusplus
 }

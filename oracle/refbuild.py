@@ -170,7 +170,9 @@ def patch_thermal(cfg: dict) -> str:
     src = _sub_const(src, "minimum_thermal_inertia", _f(c["ti_min"]))
     src = _sub_const(src, "maximum_thermal_inertia", _f(c["ti_max"]))
     src = _sub_const(src, "thermal_inertia_step", _f(c["ti_step"]))
-    src = _sub_const(src, "num_threads", str(c["threads"]))
+    # thread count and revolution cap are compile-time macros so one scratch
+    # copy serves every host
+    src = _sub_const(src, "num_threads", "ORACLE_THREADS")
     for w in ("write_shape_shadow", "write_shape_illumination",
               "write_shape_temperature", "write_roughness_temperature"):
         src = _sub_const(src, w, str(c.get(w, 0)))
@@ -183,8 +185,7 @@ def patch_thermal(cfg: dict) -> str:
     src = _insert_after(src, i, "if (multiple_scattering == 1) { multiplescattering(A); }",
                         "\n\t__oracle_dump_forcing(A);")
     src = _replace_from(src, i, "while (A.rtnconverged() == 0 && rev < 301) {",
-                        "__oracle_rev_begin();\n\t\twhile (A.rtnconverged() == 0 && rev < %d) {"
-                        % int(c["revcap"]))
+                        "__oracle_rev_begin();\n\t\twhile (A.rtnconverged() == 0 && rev < ORACLE_REVCAP) {")
     j = src.find("__oracle_rev_begin();", i)
     src = _replace_from(src, j, "rev = rev + 1;",
                         "__oracle_rev_end(A, rev, t_inertia);\n\t\t\trev = rev + 1;")
@@ -199,24 +200,32 @@ def _gpu_module_defines(cfg: dict) -> list[str]:
             f"-DREF_NX={cfg['nx']}"]
 
 
+def thermal_source(cfg: dict) -> Path:
+    """Write (once) the scratch copy of the Thermal driver for ``cfg``."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    threads, revcap = full.pop("threads"), full.pop("revcap")
+    d = OUT_ROOT / _tag("thermal", full)
+    src_path = d / "main.cpp"
+    if not src_path.exists():
+        if not (REF_ROOT / THERMAL_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        d.mkdir(parents=True, exist_ok=True)
+        src_path.write_text(patch_thermal(full))
+        (d / "config.json").write_text(json.dumps(full, indent=1))
+    return src_path
+
+
 def build_thermal(cfg: dict) -> Path:
     """Return the path of a compiled reference Thermal driver for ``cfg``."""
     full = dict(thermal_defaults())
     full.update(cfg)
-    tag = _tag("thermal", full)
-    d = OUT_ROOT / tag
-    exe = d / "thermal"
-    src_path = d / "main.cpp"
+    src_path = thermal_source(full)
+    exe = src_path.parent / ("thermal_t%d_r%d" % (full["threads"], full["revcap"]))
     if exe.exists():
         return exe
-    d.mkdir(parents=True, exist_ok=True)
-    if not src_path.exists():
-        if not (REF_ROOT / THERMAL_SRC).exists():
-            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
-        src_path.write_text(patch_thermal(full))
-        (d / "config.json").write_text(json.dumps(full, indent=1))
-    cmd = ["g++", *CXXFLAGS, *_gpu_module_defines(full), str(src_path),
-           str(HERE / "ref_gpu_cpu.cpp"), "-o", str(exe)]
+    cmd = ["g++", *CXXFLAGS, *_gpu_module_defines(full), "-DORACLE_THREADS=%d" % full["threads"],
+           "-DORACLE_REVCAP=%d" % full["revcap"], str(src_path), str(HERE / "ref_gpu_cpu.cpp"), "-o", str(exe)]
     subprocess.run(cmd, check=True)
     return exe
 

@@ -1,0 +1,51 @@
+"""The C-ABI library: builds, loads, exports every symbol include/atpm.h declares."""
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        names |= set(re.findall(r"ATPM_API\s+[^;(]*?\b(atpm_\w+)\s*\(", h.read_text()))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert {"atpm_solve_create", "atpm_run", "atpm_batch_run", "atpm_viewfactors_compute"} <= names
+
+
+def test_library_exports_every_declared_symbol():
+    from binarytpm_gb300 import build
+
+    lib = build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\b(atpm_\w+)\b", out))
+    missing = _declared() - exported
+    assert not missing, missing
+
+
+def test_library_loads_and_binds():
+    from binarytpm_gb300 import build, lib
+
+    build.build()
+    L = lib.load()
+    assert L.atpm_version() >= 100
+    assert L.atpm_status_string(0) == b"ok"
+    # every Python binding names a declared symbol
+    assert set(lib.exported_symbols()) <= _declared()
+
+
+def test_no_gpu_is_an_error_not_a_fallback():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from binarytpm_gb300 import lib
+
+    with pytest.raises(lib.AtpmError):
+        lib.Context(0)
