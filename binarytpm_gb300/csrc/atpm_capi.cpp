@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -77,6 +78,9 @@ struct atpm_solve {
     int4* wmap = nullptr;
     int2* fmap = nullptr;
     int nw = 0, nfb = 0;
+    void* tc_mem = nullptr;   // tensor-core tiles + W tiles (FAST)
+    int4* qmap = nullptr;
+    int nq = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<double> vert_h;
@@ -228,6 +232,136 @@ void build_maps(int nf, int ntau, int solve, std::vector<int4>& w, std::vector<i
     for (int f0 = 0; f0 < nf; f0 += 128) fm.push_back(make_int2(solve, f0));
 }
 
+// FAST conduction variant: ATPM_COND_VARIANT in {1,2,3} (minimum resident
+// blocks per SM given to the register allocator), default 3 (fastest on
+// GB300 for NX = 56: 2.09 -> 1.52 ms per batched revolution)
+int cond_variant() {
+    const char* e = std::getenv("ATPM_COND_VARIANT");
+    if (e && e[0] >= '1' && e[0] <= '3' && e[1] == 0) return e[0] - '0';
+    return 3;
+}
+
+bool tc_enabled() {
+    const char* e = std::getenv("ATPM_TC");
+    return !(e && e[0] == '0');
+}
+
+uint16_t f2bf(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+// step chunking of the tensor-core product: equal chunks of N <= tc_max_chunk()
+// steps, N a multiple of 16 (720 steps -> 5 chunks of 144)
+void tc_chunks(int ntau, int* n, int* nch) {
+    const int cap = tc_max_chunk();
+    const int c = (ntau + cap - 1) / cap;
+    int nn = (ntau + c - 1) / c;
+    nn = (nn + 15) / 16 * 16;
+    *n = nn;
+    *nch = c;
+}
+
+void build_tc_maps(int nf, int ntau, int solve, std::vector<int4>& q) {
+    int n, nch;
+    tc_chunks(ntau, &n, &nch);
+    const int nmb = (nf + 127) / 128;
+    for (int mb = 0; mb < nmb; ++mb)
+        for (int c = 0; c < nch; ++c) q.push_back(make_int4(solve, mb, c, 0));
+}
+
+// block-sparse BF16 tiles of the view-factor matrix (128 x 64, swizzled)
+atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
+    const int nf = s->nf, ntau = s->P.ntau;
+    const int nmb = (nf + 127) / 128, nkb = (nf + 63) / 64;
+    int N, nch;
+    tc_chunks(ntau, &N, &nch);
+    std::vector<std::vector<int>> cols(nmb);
+    for (int f = 0; f < nf; ++f)
+        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) cols[f / 128].push_back(sh->dep_idx[k] / 64);
+    std::vector<int> tptr(nmb + 1, 0), tcol;
+    std::vector<std::vector<int>> slot(nmb);
+    for (int mb = 0; mb < nmb; ++mb) {
+        auto& c = cols[mb];
+        std::sort(c.begin(), c.end());
+        c.erase(std::unique(c.begin(), c.end()), c.end());
+        tptr[mb + 1] = tptr[mb] + (int)c.size();
+        tcol.insert(tcol.end(), c.begin(), c.end());
+    }
+    const size_t ntiles = tcol.size();
+    const size_t tile_el = 128 * 64;
+    std::vector<uint16_t> tiles(std::max<size_t>(ntiles, 1) * tile_el, 0);
+    std::vector<float> vmax(std::max<size_t>(ntiles, 1), 0.0f);
+    for (int mb = 0; mb < nmb; ++mb) {
+        const int t0 = tptr[mb];
+        const auto& c = cols[mb];
+        for (int f = mb * 128; f < std::min(nf, (mb + 1) * 128); ++f)
+            for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
+                const int g = sh->dep_idx[k];
+                const int t = t0 + (int)(std::lower_bound(c.begin(), c.end(), g / 64) - c.begin());
+                uint16_t& e = tiles[(size_t)t * tile_el + tc_swizzle_offset((uint32_t)(f % 128), (uint32_t)(g % 64))];
+                e = f2bf(sh->dep_vf[k]);
+                vmax[t] = std::max(vmax[t], std::fabs(sh->dep_vf[k]));
+            }
+    }
+    // residual tiles V - bf16(V) where a tile holds a view factor >= 1e-4
+    std::vector<int> lo_of(std::max<size_t>(ntiles, 1), -1);
+    int nlo = 0;
+    for (size_t t = 0; t < ntiles; ++t)
+        if (vmax[t] >= 1e-4f) lo_of[t] = nlo++;
+    std::vector<uint16_t> lo_tiles(std::max(nlo, 1) * tile_el, 0);
+    for (int mb = 0; mb < nmb; ++mb) {
+        const int t0 = tptr[mb];
+        const auto& c = cols[mb];
+        for (int f = mb * 128; f < std::min(nf, (mb + 1) * 128); ++f)
+            for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
+                const int g = sh->dep_idx[k];
+                const int t = t0 + (int)(std::lower_bound(c.begin(), c.end(), g / 64) - c.begin());
+                if (lo_of[t] < 0) continue;
+                const uint16_t hb = f2bf(sh->dep_vf[k]);
+                uint32_t hu = (uint32_t)hb << 16;
+                float hf;
+                std::memcpy(&hf, &hu, 4);
+                lo_tiles[(size_t)lo_of[t] * tile_el + tc_swizzle_offset((uint32_t)(f % 128), (uint32_t)(g % 64))] =
+                    f2bf(sh->dep_vf[k] - hf);
+            }
+    }
+    const size_t b_tiles = align256(tiles.size() * 2);
+    const size_t b_ptr = align256((nmb + 1) * 4), b_col = align256(std::max<size_t>(ntiles, 1) * 4);
+    const size_t b_w = align256((size_t)nkb * nch * N * 64 * 2 * 2);
+    const size_t b_lo = align256(lo_tiles.size() * 2), b_loi = align256(lo_of.size() * 4);
+    char* m = nullptr;
+    CK(cudaMalloc((void**)&m, b_tiles + b_ptr + b_col + b_w + b_lo + b_loi));
+    s->tc_mem = m;
+    char* p_lo = m + b_tiles + b_ptr + b_col + b_w;
+    CK(cudaMemcpy(m, tiles.data(), tiles.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m + b_tiles, tptr.data(), (nmb + 1) * 4, cudaMemcpyHostToDevice));
+    if (ntiles) CK(cudaMemcpy(m + b_tiles + b_ptr, tcol.data(), ntiles * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemset(m + b_tiles + b_ptr + b_col, 0, b_w));
+    CK(cudaMemcpy(p_lo, lo_tiles.data(), lo_tiles.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice));
+    DevSolve& d = s->ds;
+    d.tc_tiles = m;
+    d.tc_ptr = reinterpret_cast<const int*>(m + b_tiles);
+    d.tc_col = reinterpret_cast<const int*>(m + b_tiles + b_ptr);
+    d.Wb = m + b_tiles + b_ptr + b_col;
+    d.tc_lo_tiles = p_lo;
+    d.tc_lo = reinterpret_cast<const int*>(p_lo + b_lo);
+    d.tc_n = N;
+    d.tc_nchunks = nch;
+    d.tc_nmb = nmb;
+    d.tc_nkb = nkb;
+    std::vector<int4> q;
+    build_tc_maps(nf, ntau, 0, q);
+    CK(cudaMalloc(&s->qmap, q.size() * sizeof(int4)));
+    CK(cudaMemcpy(s->qmap, q.data(), q.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    s->nq = (int)q.size();
+    return ATPM_OK;
+}
+
 Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, int nw, const int2* fm,
                  int nfb, int mode, int nx) {
     Batch b;
@@ -241,6 +375,10 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.nx = nx;
     b.p4 = view(ctx->p4);
     b.p3 = view(ctx->p3);
+    b.qmap = nullptr;
+    b.nq = 0;
+    b.tc_nmax = 0;
+    b.cond_variant = cond_variant();
     return b;
 }
 
@@ -251,26 +389,39 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
     *tmp = nullptr;
     if (n == 1) {
         *out = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
+        out->qmap = s0->qmap;
+        out->nq = s0->nq;
+        out->tc_nmax = s0->ds.tc_n;
         return ATPM_OK;
     }
     std::vector<DevSolve> tab(n);
-    std::vector<int4> wm;
+    std::vector<int4> wm, qm;
     std::vector<int2> fm;
+    int nmax = 0;
     for (int i = 0; i < n; ++i) {
         tab[i] = solves[i]->ds;
         std::vector<int4> w1;
         build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, fm);
         if (solves[i]->nnz > 0) wm.insert(wm.end(), w1.begin(), w1.end());
+        if (solves[i]->nq > 0) {
+            build_tc_maps(solves[i]->nf, solves[i]->P.ntau, i, qm);
+            nmax = std::max(nmax, solves[i]->ds.tc_n);
+        }
     }
     const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
     const size_t bf = align256(fm.size() * sizeof(int2));
-    CK(cudaMalloc(tmp, bt + bw + bf));
+    const size_t bq = align256(std::max<size_t>(qm.size(), 1) * sizeof(int4));
+    CK(cudaMalloc(tmp, bt + bw + bf + bq));
     char* t = static_cast<char*>(*tmp);
     CK(cudaMemcpy(t, tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice));
     if (!wm.empty()) CK(cudaMemcpy(t + bt, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(t + bt + bw, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (!qm.empty()) CK(cudaMemcpy(t + bt + bw + bf, qm.data(), qm.size() * sizeof(int4), cudaMemcpyHostToDevice));
     *out = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + bt), (int)wm.size(),
                       reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
+    out->qmap = reinterpret_cast<int4*>(t + bt + bw + bf);
+    out->nq = (int)qm.size();
+    out->tc_nmax = nmax;
     return ATPM_OK;
 }
 
@@ -304,6 +455,7 @@ atpm_status check_status(atpm_solve* s, int st) {
     if (st & ST_NONFINITE) return fail(ATPM_E_NONFINITE, "a surface temperature became non-finite");
     if (st & ST_NEWTON_CAP) return fail(ATPM_E_ITERATION, "Newton iteration cap reached");
     if (st & ST_SCATTER_CAP) return fail(ATPM_E_ITERATION, "scattering iteration cap reached");
+    if (st & ST_TC_TIMEOUT) return fail(ATPM_E_ITERATION, "tensor-core pipeline wait timed out");
     (void)s;
     return ATPM_OK;
 }
@@ -470,6 +622,9 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
         e = cudaStreamSynchronize(s->st);
         if (e != cudaSuccess) goto cuda_fail;
     }
+    if (P->precision == ATPM_FAST && s->nnz > 0 && tc_enabled()) {
+        if ((r = build_tc(s, sh)) != ATPM_OK) { atpm_solve_destroy(s); return r; }
+    }
     if ((r = upload_table(s)) != ATPM_OK) { atpm_solve_destroy(s); return r; }
     e = cudaEventCreate(&s->ev0);
     if (e != cudaSuccess) goto cuda_fail;
@@ -492,6 +647,8 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->wmap) cudaFree(s->wmap);
     if (s->fmap) cudaFree(s->fmap);
     if (s->ds_dev) cudaFree(s->ds_dev);
+    if (s->tc_mem) cudaFree(s->tc_mem);
+    if (s->qmap) cudaFree(s->qmap);
     if (s->arena) cudaFree(s->arena);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
@@ -642,6 +799,7 @@ ATPM_API atpm_status atpm_initialise_temperatures(atpm_solve* s) {
         for (int f = 0; f < nf; ++f) m[f] = std::pow((1.0f - P.albedo) * m[f] / es, 0.25f);
         CK(cudaMemcpyAsync(mean, m.data(), nf * 4, cudaMemcpyHostToDevice, s->st));
         if (launch_fill_initial(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "fill launch");
+        if (launch_w_bf16_one(s->ds, s->st)) return fail(ATPM_E_CUDA, "W launch");
         CK(cudaStreamSynchronize(s->st));
     }
     s->have_temps = true;
@@ -901,6 +1059,37 @@ ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t 
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "profile: %s", cudaGetErrorString(e));
     if (facet_steps) *facet_steps = fs;
     if (active_facets) *active_facets = act;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q) {
+    if (!s || !q) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    Ctl c, on{0, 1, 0, 0};
+    CK(cudaMemcpy(&c, s->ds.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(s->ds.ctl, &on, sizeof on, cudaMemcpyHostToDevice));
+    Batch b;
+    void* tmp = nullptr;
+    atpm_solve* one[1] = {s};
+    atpm_status r = make_batch_for(one, 1, &b, &tmp);
+    if (r) return r;
+    int rc = launch_revolution_part(b, 0, s->st);
+    if (!rc) rc = launch_w_bf16_one(s->ds, s->st);
+    if (!rc) rc = launch_revolution_part(b, 1, s->st);
+    CK(cudaStreamSynchronize(s->st));
+    CK(cudaMemcpy(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice));
+    if (rc) return fail(ATPM_E_CUDA, "self-heating launch");
+    int st = 0;
+    CK(cudaMemcpy(&st, s->ds.status, 4, cudaMemcpyDeviceToHost));
+    if (st & ST_TC_TIMEOUT) return fail(ATPM_E_ITERATION, "tensor-core pipeline wait timed out");
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    if (s->rs == 8) {
+        std::vector<double> h(nt);
+        CK(cudaMemcpy(h.data(), s->ds.Q, nt * 8, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nt; ++i) q[i] = (float)h[i];
+    } else {
+        CK(cudaMemcpy(q, s->ds.Q, nt * 4, cudaMemcpyDeviceToHost));
+    }
     return ATPM_OK;
 }
 

@@ -193,7 +193,7 @@ int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t stv) {
     k_geom_vertices<<<(unsigned)((nvt + 255) / 256), 256, 0, st>>>(a);
     if (s.mode == MODE_FP64) k_geom_facets<MODE_FP64><<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a);
     else k_geom_facets<MODE_REF><<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t stv) {
@@ -201,7 +201,7 @@ int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t stv) {
     GeomArgs a{s, g};
     dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
     k_shadow_dep<<<grd, blk, 0, st>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_shadow_allpairs(const DevSolve& s, const GeomWork& g, stream_t stv) {
@@ -209,7 +209,7 @@ int launch_shadow_allpairs(const DevSolve& s, const GeomWork& g, stream_t stv) {
     GeomArgs a{s, g};
     dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
     k_shadow_all<<<grd, blk, 0, st>>>(a);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 }  // namespace atpm

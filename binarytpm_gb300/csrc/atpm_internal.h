@@ -26,6 +26,7 @@ enum : int {
     ST_NEWTON_CAP = 2,    // Newton iteration cap reached
     ST_POW_RANGE = 4,     // REFERENCE mode: pow argument outside the exact table range
     ST_SCATTER_CAP = 8,   // scattering iteration cap reached
+    ST_TC_TIMEOUT = 16,   // a tensor-core pipeline wait gave up
 };
 
 // exception table: glibc powf(x, e) where it differs from the device's
@@ -77,7 +78,21 @@ struct DevSolve {
     float ti, oma, es, es4, m1, r, tacc, tacc10, alb, solar, sacc;
     double ti_d, oma_d, es_d, es4_d, m1_d, r_d, tacc_d, tacc10_d, alb_d, solar_d, sacc_d;
     int newton_cap;
+    // FAST precision, tensor-core self-heating (atpm_spmm_tc.cu); null when off
+    const int* tc_ptr;       // [nmb+1] tile range of each 128-facet row block
+    const int* tc_col;       // [ntiles] 64-facet column block of each tile
+    const void* tc_tiles;    // [ntiles][128*64] BF16, swizzled K-major
+    const int* tc_lo;        // [ntiles] index into tc_lo_tiles, or -1
+    const void* tc_lo_tiles; // [nlo][128*64] BF16 residual V - bf16(V) of tiles with large entries
+    void* Wb;                // [nkb][nchunks][2][tc_n*64] BF16 eps*sigma*T^4 (hi, lo), swizzled
+    int tc_n, tc_nchunks, tc_nmb, tc_nkb;
 };
+
+// element offset of (row, k) inside a 128-byte-swizzled K-major tile with 64
+// BF16 per row: 16-byte chunk c of row r is stored at chunk c ^ (r % 8)
+__host__ __device__ __forceinline__ uint32_t swz(uint32_t row, uint32_t k) {
+    return row * 64u + ((((k >> 3) ^ (row & 7u)) << 3) | (k & 7u));
+}
 
 // ---------------------------------------------------------------- launchers
 // (definitions in the .cu files; `stream` is a cudaStream_t)
@@ -114,6 +129,10 @@ struct Batch {
     int nfb;
     int mode, nx;
     PowTab p4, p3;
+    const int4* qmap;        // tensor-core work items {solve, row block, step chunk, 0}
+    int nq;
+    int tc_nmax;             // largest step chunk in the batch
+    int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
 };
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
 // part 0 W, 1 Q, 2 conduction, 3 convergence, 4 advance
@@ -121,6 +140,13 @@ int launch_revolution_part(const Batch& b, int part, stream_t st);
 int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);
 int launch_fill_initial(const DevSolve& s, const void* t_init, stream_t st);
 int launch_energy_balance(const DevSolve& s, stream_t st);
+// tensor-core self-heating (atpm_spmm_tc.cu)
+int launch_w_bf16(const Batch& b, stream_t st);
+int launch_w_bf16_one(const DevSolve& s, stream_t st);
+int launch_spmm_tc(const Batch& b, stream_t st);
+size_t spmm_tc_smem_bytes(int N);
+uint32_t tc_swizzle_offset(uint32_t row, uint32_t k);
+int tc_max_chunk();  // largest step chunk N of the tensor-core product
 bool conduction_nx_supported(int nx);
 
 // pow exception tables (atpm_powtab.cpp)

@@ -171,7 +171,7 @@ int launch_single_scattering(const DevSolve& s, stream_t stv) {
         case MODE_FP64: k_single_scatter<MODE_FP64><<<grd, blk, 0, st>>>(s); break;
         default: k_single_scatter<MODE_FAST><<<grd, blk, 0, st>>>(s); break;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 size_t multiple_scattering_work_bytes(const DevSolve& s) {
@@ -187,7 +187,7 @@ int launch_multiple_scattering(const DevSolve& s, void* work, stream_t stv) {
         case MODE_FP64: k_multi_gs<MODE_FP64><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
         default: k_multi_gs<MODE_FAST><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_forcing_transpose(const DevSolve& s, stream_t stv) {
@@ -197,7 +197,7 @@ int launch_forcing_transpose(const DevSolve& s, stream_t stv) {
         k_forcing_t<double><<<grd, blk, 0, st>>>(static_cast<const double*>(s.Efm), static_cast<double*>(s.E), s.nf, s.ntau);
     else
         k_forcing_t<float><<<grd, blk, 0, st>>>(static_cast<const float*>(s.Efm), static_cast<float*>(s.E), s.nf, s.ntau);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* illum_d, stream_t stv) {
@@ -206,7 +206,7 @@ int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* 
     const int g = (int)((n + 255) / 256);
     if (s.mode == MODE_FP64) k_set_forcing<double><<<g, 256, 0, st>>>(s, shadow_d, illum_d);
     else k_set_forcing<float><<<g, 256, 0, st>>>(s, shadow_d, illum_d);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 }  // namespace atpm

@@ -1,0 +1,347 @@
+// Block-sparse self-heating flux on the 5th-generation tensor cores (FAST
+// precision).  The reference sums Q_f = sum_g eps sigma T_g^4 V_fg over each
+// facet's view-factor list (3905/Thermal/NominalPole/main.cpp:1519-1529); with
+// previous-revolution temperatures the whole revolution is one product
+//
+//     Q[s][f] = sum_g V[f][g] * (W_hi[s][g] + W_lo[s][g])
+//
+// with W = eps sigma T^4 split into two BF16 parts (W_hi = bf16(W),
+// W_lo = bf16(W - W_hi): a 16-bit significand, so the flux does not jitter
+// from one revolution to the next by more than ~1e-5 relative) and V in BF16.
+// Tiles holding a view factor >= 1e-4 (neighbours in concavities, where one
+// entry can carry a third of a facet's flux) also keep V_lo = bf16(V - V_hi)
+// and get a third product V_lo * W_hi.  Accumulation is FP32 in TMEM.
+// Row blocks whose 128 facets are all frozen (reference freeze protocol)
+// are skipped: their flux is not read.
+//
+// V is stored as 128 x 64 BF16 tiles (block-sparse rows: every 128-facet row
+// block keeps the 64-facet column blocks it touches) and W as 64-facet x N-step
+// tiles.  Both are laid out in HBM already in the 128-byte-swizzled K-major
+// form the tensor core reads, so each tile moves with one bulk copy
+// (cp.async.bulk) into a 4-stage shared-memory ring.  One elected thread
+// issues tcgen05.mma (M = 128, N = step chunk, K = 16) into a TMEM
+// accumulator; the four warps then drain TMEM with tcgen05.ld and write Q
+// coalesced along facets.
+//
+// Every mbarrier wait is bounded (about one second of clock cycles); a
+// timeout sets ST_TC_TIMEOUT in the solve's status word and the block drains
+// and frees its TMEM instead of spinning.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "atpm_internal.h"
+
+namespace atpm {
+
+namespace {
+
+constexpr int TC_M = 128;        // facets per row block (TMEM lanes)
+constexpr int TC_K = 64;         // facets per column block (one 128-byte swizzle row of BF16)
+constexpr int TC_STAGES = 4;   // upper bound; the ring depth follows the stage size
+constexpr long long WAIT_CYCLES = 2000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false after ~1 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > WAIT_CYCLES) return false;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (tcgen05 descriptor version 1)
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;       // stride byte offset
+    d |= (uint64_t)1 << 46;                  // descriptor version
+    d |= (uint64_t)2 << 61;                  // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: D f32, A/B bf16, both K-major, M = 128, N = n
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
+
+// ring depth: as many stages (<= 4) as fit in 220 KB of shared memory;
+// a stage holds A_hi, A_lo (16 KB each) and B_hi, B_lo (N x 128 B each)
+__host__ __device__ inline int tc_stages(int N) {
+    const int stage = (TC_M * TC_K * 4 + N * TC_K * 4 + 1023) & ~1023;
+    const int s = (220 * 1024) / stage;
+    return s < TC_STAGES ? s : TC_STAGES;
+}
+
+}  // namespace
+
+uint32_t tc_swizzle_offset(uint32_t row, uint32_t k) { return swz(row, k); }
+int tc_max_chunk() { return 160; }
+
+// W = eps sigma T^4 in BF16, written as (column block, step chunk) tiles
+__global__ void __launch_bounds__(256) k_w_bf16(Batch b) {
+    const int4 t = b.wmap[blockIdx.x];
+    const DevSolve& sv = b.tab[t.x];
+    if (!sv.ctl->active || !sv.tc_tiles) return;
+    const int nf = sv.nf, ntau = sv.ntau, N = sv.tc_n, nch = sv.tc_nchunks;
+    const float* T = static_cast<const float*>(sv.stemp1);
+    __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
+    const float es = sv.es;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int s = t.z + j, f = t.y + threadIdx.x;
+        if (s >= ntau || f >= nf) continue;
+        const float x = T[(size_t)s * nf + f];
+        const float x2 = x * x;
+        const float w = es * (x2 * x2);
+        const int kb = f / TC_K, k = f % TC_K, nc = s / N, n = s % N;
+        const size_t base = ((size_t)kb * nch + nc) * (size_t)2 * N * TC_K;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+        W[base + swz(n, k)] = hi;
+        W[base + (size_t)N * TC_K + swz(n, k)] = __float2bfloat16_rn(w - __bfloat162float(hi));
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
+    extern __shared__ __align__(1024) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
+    __shared__ uint32_t tmem_base;
+    const int4 item = b.qmap[blockIdx.x];
+    const DevSolve& sv = b.tab[item.x];
+    if (!sv.ctl->active || !sv.tc_tiles) return;
+    const int mb = item.y, nc = item.z;
+    const int N = sv.tc_n, nch = sv.tc_nchunks;
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int t0 = sv.tc_ptr[mb], T = sv.tc_ptr[mb + 1] - t0;
+    float* Q = static_cast<float*>(sv.Q);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int f = mb * TC_M + warp * 32 + lane;
+    const bool everyone = !sv.freeze || sv.ti == 0.0f;
+    if (!__syncthreads_or(f < nf && (everyone || !sv.conv[f]))) return;  // all frozen
+    if (T == 0) {
+        if (f < nf)
+            for (int n = 0; n < N; ++n) {
+                const int s = nc * N + n;
+                if (s < ntau) Q[(size_t)s * nf + f] = 0.0f;
+            }
+        return;
+    }
+    // 1024-byte aligned stage ring (alignment of the shared-window address)
+    unsigned char* base = dyn + ((1024u - (smem_u32(dyn) & 1023u)) & 1023u);
+    const uint32_t a_bytes = TC_M * TC_K * 2;
+    const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;  // hi + lo
+    const uint32_t stage_bytes = (2 * a_bytes + b_bytes + 1023) & ~1023u;
+    const int S = tc_stages(N);
+    const uint32_t ncols = (N <= 32) ? 32 : (N <= 64) ? 64 : (N <= 128) ? 128 : 256;
+    if (warp == 0) {
+        tc_alloc(&tmem_base, ncols);
+        tc_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < TC_STAGES; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    const __nv_bfloat16* tiles = static_cast<const __nv_bfloat16*>(sv.tc_tiles);
+    const __nv_bfloat16* lo_tiles = static_cast<const __nv_bfloat16*>(sv.tc_lo_tiles);
+    const __nv_bfloat16* Wb = static_cast<const __nv_bfloat16*>(sv.Wb);
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = idesc_bf16(N);
+        auto load = [&](int i, int st) {
+            unsigned char* sa = base + (size_t)st * stage_bytes;
+            const int kb = sv.tc_col[t0 + i];
+            const int lo = sv.tc_lo[t0 + i];
+            mbar_expect_tx(&full[st], a_bytes + (lo >= 0 ? a_bytes : 0u) + b_bytes);
+            bulk_g2s(sa, tiles + (size_t)(t0 + i) * (TC_M * TC_K), a_bytes, &full[st]);
+            if (lo >= 0) bulk_g2s(sa + a_bytes, lo_tiles + (size_t)lo * (TC_M * TC_K), a_bytes, &full[st]);
+            bulk_g2s(sa + 2 * a_bytes, Wb + ((size_t)kb * nch + nc) * (size_t)2 * N * TC_K, b_bytes, &full[st]);
+        };
+        const int pro = T < S ? T : S;
+        for (int i = 0; i < pro; ++i) load(i, i);
+        for (int i = 0; i < T && ok; ++i) {
+            const int st = i % S;
+            const uint32_t ph = (uint32_t)(i / S) & 1u;
+            if (!mbar_wait(&full[st], ph)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t sa = smem_u32(base + (size_t)st * stage_bytes);
+            const uint64_t ad = sw128_desc(sa), al = sw128_desc(sa + a_bytes);
+            const uint64_t bh = sw128_desc(sa + 2 * a_bytes), bl = sw128_desc(sa + 2 * a_bytes + b_bytes / 2);
+            const bool has_lo = sv.tc_lo[t0 + i] >= 0;
+#pragma unroll
+            for (int k = 0; k < TC_K / 16; ++k) {
+                tc_mma(tmem, ad + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, (i | k) != 0);
+                tc_mma(tmem, ad + (uint64_t)(2 * k), bl + (uint64_t)(2 * k), idesc, 1u);
+                if (has_lo) tc_mma(tmem, al + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, 1u);
+            }
+            tc_commit(&empty[st]);
+            const int j = i + S;
+            if (j < T) {
+                if (!mbar_wait(&empty[st], ph)) { ok = false; break; }
+                load(j, st);
+            }
+        }
+        tc_commit(&done);
+        if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);
+    }
+    __syncwarp();
+    const bool fin = __all_sync(0xffffffffu, mbar_wait(&done, 0));
+    tc_fence_after();
+    if (fin) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc_ld16(tmem + lane_base + (uint32_t)c0, v);
+            if (f < nf) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int s = nc * N + c0 + j;
+                    if (c0 + j < N && s < ntau) Q[(size_t)s * nf + f] = v[j];
+                }
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        atomicOr(sv.status, ST_TC_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, ncols);
+}
+
+size_t spmm_tc_smem_bytes(int N) {
+    const size_t a = TC_M * TC_K * 2 * 2, bb = (size_t)N * TC_K * 2 * 2;
+    return (size_t)tc_stages(N) * ((a + bb + 1023) & ~(size_t)1023) + 1024;
+}
+
+int launch_spmm_tc(const Batch& b, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    if (b.nq == 0) return 0;
+    const size_t smem = spmm_tc_smem_bytes(b.tc_nmax);
+    static int attr_dev = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (attr_dev != dev) {
+        size_t most = 0;  // largest ring over every admissible chunk size
+        for (int n = 16; n <= tc_max_chunk(); n += 16) most = spmm_tc_smem_bytes(n) > most ? spmm_tc_smem_bytes(n) : most;
+        if (cudaFuncSetAttribute(k_spmm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) != cudaSuccess)
+            return 2;
+        attr_dev = dev;
+    }
+    k_spmm_tc<<<b.nq, 128, smem, st>>>(b);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+__global__ void __launch_bounds__(256) k_w_bf16_one(DevSolve sv) {
+    const int nf = sv.nf, ntau = sv.ntau, N = sv.tc_n, nch = sv.tc_nchunks;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)nf * ntau) return;
+    const int s = (int)(i / nf), f = (int)(i % nf);
+    const float x = static_cast<const float*>(sv.stemp1)[i];
+    const float x2 = x * x;
+    const float w = sv.es * (x2 * x2);
+    __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
+    const size_t base = ((size_t)(f / TC_K) * nch + s / N) * (size_t)2 * N * TC_K;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+    W[base + swz(s % N, f % TC_K)] = hi;
+    W[base + (size_t)N * TC_K + swz(s % N, f % TC_K)] = __float2bfloat16_rn(w - __bfloat162float(hi));
+}
+
+int launch_w_bf16_one(const DevSolve& s, stream_t stv) {
+    if (!s.tc_tiles) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t n = (size_t)s.nf * s.ntau;
+    k_w_bf16_one<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_w_bf16(const Batch& b, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    if (b.nw == 0) return 0;
+    k_w_bf16<<<b.nw, dim3(32, 8), 0, st>>>(b);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+}  // namespace atpm

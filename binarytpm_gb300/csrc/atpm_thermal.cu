@@ -16,6 +16,7 @@
 // that have stopped, so the same launch sequence (or a captured graph of it)
 // can be replayed until every solve in the batch is done.
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 
 #include "atpm_internal.h"
 
@@ -236,6 +237,102 @@ __device__ __forceinline__ void column_revolution(const DevSolve& sv, const Batc
     if (flags) atomicOr(sv.status, flags);
 }
 
+// FAST + tensor-core self-heating: eps*sigma*T^4 of the new surface
+// temperature goes straight into the hi/lo BF16 tiles the next revolution's
+// product reads (atpm_spmm_tc.cu), so no separate pass re-reads stemp1.
+__device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float t) {
+    const int N = sv.tc_n;
+    const float t2 = t * t;
+    const float w = sv.es * (t2 * t2);
+    __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
+    const size_t base = ((size_t)(f >> 6) * sv.tc_nchunks + s / N) * (size_t)2 * N * 64;
+    const uint32_t o = swz((uint32_t)(s % N), (uint32_t)(f & 63));
+    const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+    W[base + o] = hi;
+    W[base + (size_t)N * 64 + o] = __float2bfloat16_rn(w - __bfloat162float(hi));
+}
+
+// FAST precision: the same update, scheduled for the FP32 pipes.  Node 1 is
+// advanced first (the boundary solve needs it); the Newton boundary of step s
+// runs two unconditional iterations (a third and more only while the change
+// is still >= TACC/10), and the FTCS update of nodes 2..NX-1 -- which does not
+// depend on the boundary result -- sits in the same basic block so the
+// scheduler overlaps it with the Newton dependency chain.
+template <int NX>
+__device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f) {
+    const int nf = sv.nf, ntau = sv.ntau;
+    const float r = sv.r, oma = sv.oma, es = sv.es, es4 = sv.es4, m1 = sv.m1, tacc = sv.tacc, tacc10 = sv.tacc10;
+    float* temp = static_cast<float*>(sv.temp);
+    const float* __restrict__ E = static_cast<const float*>(sv.E);
+    const float* __restrict__ Q = static_cast<const float*>(sv.Q);
+    float* __restrict__ S0 = static_cast<float*>(sv.stemp0);
+    float* __restrict__ S1 = static_cast<float*>(sv.stemp1);
+    float T[NX + 1];
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) T[i] = temp[(size_t)i * nf + f];
+    bool hot = false;
+    int flags = 0;
+    const int cap = sv.newton_cap;
+    size_t o = (size_t)f;
+    float e_n = E[o], q_n = Q[o], old_n = S1[o];
+    for (int s = 0; s < ntau; ++s, o += nf) {
+        const float e = e_n, q = q_n, old = old_n;
+        if (s + 1 < ntau) {
+            e_n = E[o + nf];
+            q_n = Q[o + nf];
+            old_n = S1[o + nf];
+        }
+        S0[o] = old;
+        const float t1 = T[1];
+        T[1] = fmaf(r, (T[2] + T[0]) - 2.0f * t1, t1);
+        const float a = fmaf(oma, e, q);
+        // Newton iterations 1 and 2
+        float TR0 = T[0];
+        float t2 = TR0 * TR0;
+        float sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
+        float sbcd = fmaf(es4, t2 * TR0, m1);
+        float TR1 = TR0 + __fdividef(sbc, sbcd);
+        float DT = fabsf(TR1 - TR0);
+        if (DT >= tacc10) {
+            TR0 = TR1;
+            t2 = TR0 * TR0;
+            sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
+            sbcd = fmaf(es4, t2 * TR0, m1);
+            TR1 = TR0 + __fdividef(sbc, sbcd);
+            DT = fabsf(TR1 - TR0);
+        }
+        // remaining nodes (independent of the boundary result)
+        float tm = t1;
+#pragma unroll
+        for (int i = 2; i < NX; ++i) {
+            const float ti = T[i];
+            T[i] = fmaf(r, (T[i + 1] + tm) - 2.0f * ti, ti);
+            tm = ti;
+        }
+        int it = 2;
+        while (DT >= tacc10) {
+            if (it >= cap) { flags |= ST_NEWTON_CAP; break; }
+            TR0 = TR1;
+            t2 = TR0 * TR0;
+            sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
+            sbcd = fmaf(es4, t2 * TR0, m1);
+            TR1 = TR0 + __fdividef(sbc, sbcd);
+            DT = fabsf(TR1 - TR0);
+            ++it;
+        }
+        T[0] = TR1;
+        S1[o] = TR1;
+        if (sv.Wb) store_w(sv, f, s, TR1);
+        T[NX] = T[NX - 1];
+        hot = hot || (fabsf(TR1 - old) >= tacc);
+        if (!isfinite(TR1)) flags |= ST_NONFINITE;
+    }
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = T[i];
+    sv.hot[f] = hot ? 1 : 0;
+    if (flags) atomicOr(sv.status, flags);
+}
+
 // instequilibrium (main.cpp:1563-1612): every facet, every step, no depth
 template <int MODE>
 __device__ __forceinline__ void column_equilibrium(const DevSolve& sv, int f) {
@@ -258,13 +355,18 @@ __device__ __forceinline__ void column_equilibrium(const DevSolve& sv, int f) {
         if constexpr (MODE == MODE_FP64) tn = sqrt(sqrt(x));
         else tn = (float)sqrt(sqrt((double)x));
         S1[o] = tn;
+        if constexpr (MODE == MODE_FAST) {
+            if (sv.Wb) store_w(sv, f, s, tn);
+        }
         hot = hot || (A::fabs_(A::sub(tn, old)) >= c.tacc);
     }
     sv.hot[f] = hot ? 1 : 0;
 }
 
-template <int MODE, int NX>
-__global__ void __launch_bounds__(128) k_conduction(Batch b) {
+// MINB: minimum resident blocks per SM requested from the register allocator
+// (FAST only; the variants trade registers for occupancy, picked at run time)
+template <int MODE, int NX, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     const int2 fb = b.fmap[blockIdx.x];
     const DevSolve& sv = b.tab[fb.x];
     if (!sv.ctl->active) return;
@@ -273,7 +375,8 @@ __global__ void __launch_bounds__(128) k_conduction(Batch b) {
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
     if (inst) { column_equilibrium<MODE>(sv, f); return; }
     if (sv.freeze && sv.conv[f]) return;
-    column_revolution<MODE, NX>(sv, b, f);
+    if constexpr (MODE == MODE_FAST) column_revolution_fast<NX>(sv, f);
+    else column_revolution<MODE, NX>(sv, b, f);
 }
 
 // -------------------------------------------------------------- convergence
@@ -381,22 +484,41 @@ bool conduction_nx_supported(int nx) {
 
 template <int MODE>
 static int launch_rev_part(const Batch& b, int part, cudaStream_t st) {
+    // FAST + tensor cores: the conduction sweep keeps W current (store_w), so
+    // part 0 has nothing to do
+    if (MODE == MODE_FAST && b.nq > 0 && part < 2) return part == 0 ? 0 : launch_spmm_tc(b, st);
     switch (part) {
         case 0: if (b.nw > 0) k_selfheat_w<MODE><<<b.nw, dim3(32, 8), 0, st>>>(b); break;
         case 1: if (b.nw > 0) k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b); break;
         case 2:
-            switch (b.nx) {
-#define NX_CASE(n) case n: k_conduction<MODE, n><<<b.nfb, 128, 0, st>>>(b); break;
-                NX_LIST(NX_CASE)
+            if (MODE == MODE_FAST && b.cond_variant == 3) {
+                switch (b.nx) {
+#define NX_CASE(n) case n: k_conduction<MODE, n, 3><<<b.nfb, 128, 0, st>>>(b); break;
+                    NX_LIST(NX_CASE)
 #undef NX_CASE
-                default: return 1;
+                    default: return 1;
+                }
+            } else if (MODE == MODE_FAST && b.cond_variant == 2) {
+                switch (b.nx) {
+#define NX_CASE(n) case n: k_conduction<MODE, n, 2><<<b.nfb, 128, 0, st>>>(b); break;
+                    NX_LIST(NX_CASE)
+#undef NX_CASE
+                    default: return 1;
+                }
+            } else {
+                switch (b.nx) {
+#define NX_CASE(n) case n: k_conduction<MODE, n><<<b.nfb, 128, 0, st>>>(b); break;
+                    NX_LIST(NX_CASE)
+#undef NX_CASE
+                    default: return 1;
+                }
             }
             break;
         case 3: k_converge<<<b.nfb, 128, 0, st>>>(b); break;
         case 4: k_advance<<<(b.n + 127) / 128, 128, 0, st>>>(b); break;
         default: return 1;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_revolution_part(const Batch& b, int part, stream_t stv) {
@@ -425,7 +547,7 @@ int launch_initial_mean(const DevSolve& s, void* out, stream_t stv) {
         case MODE_FP64: k_initial_mean<MODE_FP64><<<g, 128, 0, st>>>(s, out); break;
         default: k_initial_mean<MODE_FAST><<<g, 128, 0, st>>>(s, out); break;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_fill_initial(const DevSolve& s, const void* t0, stream_t stv) {
@@ -433,7 +555,7 @@ int launch_fill_initial(const DevSolve& s, const void* t0, stream_t stv) {
     const int g = (s.nf + 127) / 128;
     if (s.mode == MODE_FP64) k_fill_initial<double><<<g, 128, 0, st>>>(s, static_cast<const double*>(t0));
     else k_fill_initial<float><<<g, 128, 0, st>>>(s, static_cast<const float*>(t0));
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_energy_balance(const DevSolve& s, stream_t stv) {
@@ -441,7 +563,7 @@ int launch_energy_balance(const DevSolve& s, stream_t stv) {
     const int g = (s.nf + 127) / 128;
     if (s.mode == MODE_FP64) k_energy<MODE_FP64><<<g, 128, 0, st>>>(s);
     else k_energy<MODE_REF><<<g, 128, 0, st>>>(s);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 }  // namespace atpm

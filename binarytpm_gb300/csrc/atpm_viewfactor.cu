@@ -342,23 +342,23 @@ struct VfBuffers {
 
 int vf_init(const VfGeom& g, cudaStream_t st) {
     k_vf_init<<<(g.nf + 127) / 128, 128, 0, st>>>(g);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 int vf_count(const VfGeom& g, int* count, cudaStream_t st) {
     k_vf_count<<<g.nf, 256, 0, st>>>(g, count);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 int vf_fill(const VfGeom& g, const long long* ptr, int* idx, float* vf, float* dir, cudaStream_t st) {
     k_vf_fill<<<g.nf, 256, 0, st>>>(g, ptr, idx, vf, dir);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 int vf_hidden(const VfGeom& g, const long long* ptr, const int* idx, uint8_t* keep, cudaStream_t st) {
     k_vf_hidden<<<g.nf, 256, 0, st>>>(g, ptr, idx, keep);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 int vf_refine(const VfGeom& g, const long long* ptr, const int* idx, float* vf, float* dir, cudaStream_t st) {
     k_vf_refine<<<g.nf, 128, 0, st>>>(g, ptr, idx, vf, dir);
-    return cudaPeekAtLastError() == cudaSuccess ? 0 : 2;
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 }  // namespace atpm

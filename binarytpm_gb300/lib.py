@@ -67,6 +67,7 @@ _SIGS = {
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_viewfactors_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
@@ -227,6 +228,12 @@ class Solve:
     def cosillum(self):
         out = np.zeros((self.nf, self.ntau), np.float32)
         _ck(load().atpm_get_cosillum(self.h, _p(out)))
+        return out
+
+    def selfheating_flux(self):
+        """Q [ntau][nf] for the current temperatures."""
+        out = np.zeros((self.ntau, self.nf), np.float32)
+        _ck(load().atpm_selfheating_flux(self.h, _p(out)))
         return out
 
     def surface_temperature(self):

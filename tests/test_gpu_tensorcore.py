@@ -1,0 +1,84 @@
+"""The FAST self-heating product on the tensor cores (tcgen05, BF16 view
+factors times a hi+lo BF16 split of eps*sigma*T^4, FP32 accumulation in TMEM)
+against a host evaluation of the same sum."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+SIGMA = np.float32(5.67e-8)
+
+
+def _bf16(x):
+    """Round float32 to the nearest BF16 (ties to even), returned as float64."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16
+    return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+
+
+def _host_q(prob, T, rounded):
+    """Q[s][f] = sum_g vf * eps sigma T[g][s]^4 (float64 accumulation)."""
+    es = np.float32(prob.emissivity) * SIGMA
+    T2 = (T * T).astype(np.float32)
+    W = (es * (T2 * T2)).astype(np.float32)          # [nf][ntau]
+    vf = prob.dep_vf
+    rows = np.repeat(np.arange(prob.nf), np.diff(prob.dep_ptr))
+    if rounded:
+        hi = _bf16(W)
+        lo = _bf16((W - hi.astype(np.float32)).astype(np.float32))
+        W = hi + lo
+        # V_hi everywhere; V_lo added in 128x64 tiles holding a value >= 1e-4
+        key = (rows // 128) * ((prob.nf + 63) // 64) + prob.dep_idx // 64
+        u, inv = np.unique(key, return_inverse=True)
+        vmax = np.zeros(len(u), np.float32)
+        np.maximum.at(vmax, inv, np.abs(vf))
+        vhi = _bf16(vf)
+        vlo = _bf16((vf - vhi.astype(np.float32)).astype(np.float32))
+        vf = vhi + np.where(vmax[inv] >= np.float32(1e-4), vlo, 0.0)
+    Q = np.zeros((prob.nf, T.shape[1]))
+    np.add.at(Q, rows, vf[:, None] * W[prob.dep_idx].astype(np.float64))
+    return Q.T
+
+
+@pytest.mark.parametrize("ntau", [48, 300, 720])
+def test_tensorcore_selfheating_matches_host(gpu_ctx, ntau):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden("binary_s3s1")
+    prob = prob.with_(ntau=ntau)
+    rng = np.random.default_rng(ntau)
+    s = lib.Solve(gpu_ctx, prob, precision=lib.FAST)
+    shadow = (rng.random((prob.nf, ntau)) < 0.5).astype(np.int32)
+    illum = (rng.random((prob.nf, ntau)) * 600).astype(np.float32)
+    s.set_forcing(shadow, illum)
+    s.set_thermal_inertia(200.0)
+    s.initialise_temperatures()
+    s.run()  # evolve so temperatures vary with facet and step
+    T, _ = s.surface_temperature()
+    q = s.selfheating_flux().astype(np.float64)
+    q_bf = _host_q(prob, T, rounded=True)
+    q_ex = _host_q(prob, T, rounded=False)
+    scale = np.abs(q_bf).max()
+    assert scale > 1.0
+    assert np.max(np.abs(q - q_bf)) <= 1e-5 * scale, np.max(np.abs(q - q_bf)) / scale
+    # compensated BF16 operands: close to the exact FP32 sum
+    assert np.max(np.abs(q - q_ex)) <= 1e-3 * scale
+
+
+def test_tensorcore_off_uses_gather(gpu_ctx, monkeypatch):
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden("binary_s3s1")
+    monkeypatch.setenv("ATPM_TC", "0")
+    s = lib.Solve(gpu_ctx, prob, precision=lib.FAST)
+    s.set_forcing(ref["shadow"], ref["illumination"])
+    s.set_thermal_inertia(200.0)
+    s.initialise_temperatures()
+    T, _ = s.surface_temperature()
+    q = s.selfheating_flux().astype(np.float64)
+    q_ex = _host_q(prob, T, rounded=False)
+    assert np.max(np.abs(q - q_ex)) <= 1e-5 * np.abs(q_ex).max()
