@@ -170,6 +170,28 @@ def prepare():
     return refbuild.thermal_source(_ref_cfg(prob, 200.0, 1, 3))
 
 
+def profile_case():
+    """A small, fast case of the same kernels for ncu --set full captures:
+    the binary with a subdivision-4 primary (5,120 + 1,280 facets, NX = 56,
+    NTAU = 720), two FAST solves, three instrumented revolutions."""
+    from binarytpm_gb300 import lib, workloads
+
+    ctx = lib.Context(0)
+    prob = workloads.binary_problem(ctx, p_subdiv=4)
+    s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    s0.geometry_shadow()
+    s0.scattering()
+    sh, il = s0.shadow(), s0.illumination()
+    s1 = lib.Solve(ctx, prob, precision=lib.FAST)
+    s1.set_forcing(sh, il)
+    for s, ti in ((s0, 200.0), (s1, 800.0)):
+        s.set_thermal_inertia(ti)
+        s.initialise_temperatures()
+    for _ in range(3):
+        k = lib.profile_revolution([s0, s1])
+    print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz}))
+
+
 def run_reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -205,9 +227,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU reference timing")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu captures: binary 5120+1280 facets, 2 solves, 3 instrumented revolutions")
     args = ap.parse_args()
     if args.prepare:
         print(prepare())
+        return
+    if args.profile_case:
+        profile_case()
         return
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":

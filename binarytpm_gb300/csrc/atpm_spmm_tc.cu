@@ -228,10 +228,15 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
     const __nv_bfloat16* tiles = static_cast<const __nv_bfloat16*>(sv.tc_tiles);
     const __nv_bfloat16* lo_tiles = static_cast<const __nv_bfloat16*>(sv.tc_lo_tiles);
     const __nv_bfloat16* Wb = static_cast<const __nv_bfloat16*>(sv.Wb);
-    bool ok = true;
+    // warp 0 lane 0: producer (bulk copies into the stage ring);
+    // warp 1 lane 0: MMA issuer.  Stage st is refilled as soon as the MMAs
+    // that read it complete (tcgen05.commit -> empty[st]), while the issuer
+    // keeps feeding the tensor pipe from the stages already full.
     if (threadIdx.x == 0) {
-        const uint32_t idesc = idesc_bf16(N);
-        auto load = [&](int i, int st) {
+        bool ok = true;
+        for (int i = 0; i < T; ++i) {
+            const int st = i % S;
+            if (i >= S && !mbar_wait(&empty[st], (uint32_t)((i / S) - 1) & 1u)) { ok = false; break; }
             unsigned char* sa = base + (size_t)st * stage_bytes;
             const int kb = sv.tc_col[t0 + i];
             const int lo = sv.tc_lo[t0 + i];
@@ -239,13 +244,14 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
             bulk_g2s(sa, tiles + (size_t)(t0 + i) * (TC_M * TC_K), a_bytes, &full[st]);
             if (lo >= 0) bulk_g2s(sa + a_bytes, lo_tiles + (size_t)lo * (TC_M * TC_K), a_bytes, &full[st]);
             bulk_g2s(sa + 2 * a_bytes, Wb + ((size_t)kb * nch + nc) * (size_t)2 * N * TC_K, b_bytes, &full[st]);
-        };
-        const int pro = T < S ? T : S;
-        for (int i = 0; i < pro; ++i) load(i, i);
-        for (int i = 0; i < T && ok; ++i) {
+        }
+        if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);
+    } else if (threadIdx.x == 32) {
+        const uint32_t idesc = idesc_bf16(N);
+        bool ok = true;
+        for (int i = 0; i < T; ++i) {
             const int st = i % S;
-            const uint32_t ph = (uint32_t)(i / S) & 1u;
-            if (!mbar_wait(&full[st], ph)) { ok = false; break; }
+            if (!mbar_wait(&full[st], (uint32_t)(i / S) & 1u)) { ok = false; break; }
             tc_fence_after();
             const uint32_t sa = smem_u32(base + (size_t)st * stage_bytes);
             const uint64_t ad = sw128_desc(sa), al = sw128_desc(sa + a_bytes);
@@ -258,11 +264,6 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
                 if (has_lo) tc_mma(tmem, al + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, 1u);
             }
             tc_commit(&empty[st]);
-            const int j = i + S;
-            if (j < T) {
-                if (!mbar_wait(&empty[st], ph)) { ok = false; break; }
-                load(j, st);
-            }
         }
         tc_commit(&done);
         if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);

@@ -252,12 +252,18 @@ __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float 
     W[base + (size_t)N * 64 + o] = __float2bfloat16_rn(w - __bfloat162float(hi));
 }
 
-// FAST precision: the same update, scheduled for the FP32 pipes.  Node 1 is
-// advanced first (the boundary solve needs it); the Newton boundary of step s
-// runs two unconditional iterations (a third and more only while the change
-// is still >= TACC/10), and the FTCS update of nodes 2..NX-1 -- which does not
-// depend on the boundary result -- sits in the same basic block so the
-// scheduler overlaps it with the Newton dependency chain.
+// FAST precision: the same update, scheduled for the FP32 pipes.
+//  * The column is advanced as offsets theta_i = T_i - T_ref from a per-facet
+//    reference (the bottom node at the start of the revolution).  The FTCS
+//    Laplacian is translation-invariant, so each step rounds to the ulp of
+//    theta (a few K) instead of the ulp of T (~300 K): 10-100x less roundoff
+//    than the reference's absolute FP32 update, which is what keeps the FAST
+//    path within 0.01 K of FP64 over hundreds of revolutions.
+//  * Node 1 is advanced first (the boundary solve needs it); the Newton
+//    boundary runs two iterations unconditionally (more only while the change
+//    is still >= TACC/10), and the update of nodes 2..NX-1 -- independent of
+//    the boundary result -- sits in the same basic block, so the scheduler
+//    overlaps it with the Newton dependency chain.
 template <int NX>
 __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f) {
     const int nf = sv.nf, ntau = sv.ntau;
@@ -268,8 +274,16 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     float* __restrict__ S0 = static_cast<float*>(sv.stemp0);
     float* __restrict__ S1 = static_cast<float*>(sv.stemp1);
     float T[NX + 1];
+    const float Tref = temp[(size_t)NX * nf + f];
+    // W tile addressing, advanced incrementally (no per-step division)
+    __nv_bfloat16* Wb = static_cast<__nv_bfloat16*>(sv.Wb);
+    const int N = sv.tc_n;
+    const size_t chunk = (size_t)2 * N * 64;
+    size_t wrow = Wb ? (size_t)(f >> 6) * sv.tc_nchunks * chunk : 0;
+    const uint32_t kc = (uint32_t)(f & 63) >> 3, k7 = (uint32_t)f & 7u;
+    int wn = 0;
 #pragma unroll
-    for (int i = 0; i <= NX; ++i) T[i] = temp[(size_t)i * nf + f];
+    for (int i = 0; i <= NX; ++i) T[i] = temp[(size_t)i * nf + f] - Tref;
     bool hot = false;
     int flags = 0;
     const int cap = sv.newton_cap;
@@ -286,20 +300,22 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         const float t1 = T[1];
         T[1] = fmaf(r, (T[2] + T[0]) - 2.0f * t1, t1);
         const float a = fmaf(oma, e, q);
-        // Newton iterations 1 and 2
-        float TR0 = T[0];
-        float t2 = TR0 * TR0;
-        float sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
-        float sbcd = fmaf(es4, t2 * TR0, m1);
-        float TR1 = TR0 + __fdividef(sbc, sbcd);
-        float DT = fabsf(TR1 - TR0);
+        // Newton iterations 1 and 2 on theta_0 (T_0 = Tref + theta_0)
+        float th = T[0];
+        float TR = Tref + th;
+        float t2 = TR * TR;
+        float sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
+        float sbcd = fmaf(es4, t2 * TR, m1);
+        float th1 = th + __fdividef(sbc, sbcd);
+        float DT = fabsf(th1 - th);
         if (DT >= tacc10) {
-            TR0 = TR1;
-            t2 = TR0 * TR0;
-            sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
-            sbcd = fmaf(es4, t2 * TR0, m1);
-            TR1 = TR0 + __fdividef(sbc, sbcd);
-            DT = fabsf(TR1 - TR0);
+            th = th1;
+            TR = Tref + th;
+            t2 = TR * TR;
+            sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
+            sbcd = fmaf(es4, t2 * TR, m1);
+            th1 = th + __fdividef(sbc, sbcd);
+            DT = fabsf(th1 - th);
         }
         // remaining nodes (independent of the boundary result)
         float tm = t1;
@@ -312,23 +328,33 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         int it = 2;
         while (DT >= tacc10) {
             if (it >= cap) { flags |= ST_NEWTON_CAP; break; }
-            TR0 = TR1;
-            t2 = TR0 * TR0;
-            sbc = fmaf(m1, T[1] - TR0, a) - es * (t2 * t2);
-            sbcd = fmaf(es4, t2 * TR0, m1);
-            TR1 = TR0 + __fdividef(sbc, sbcd);
-            DT = fabsf(TR1 - TR0);
+            th = th1;
+            TR = Tref + th;
+            t2 = TR * TR;
+            sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
+            sbcd = fmaf(es4, t2 * TR, m1);
+            th1 = th + __fdividef(sbc, sbcd);
+            DT = fabsf(th1 - th);
             ++it;
         }
-        T[0] = TR1;
-        S1[o] = TR1;
-        if (sv.Wb) store_w(sv, f, s, TR1);
+        T[0] = th1;
+        const float Tsurf = Tref + th1;
+        S1[o] = Tsurf;
+        if (Wb) {
+            const float t2s = Tsurf * Tsurf;
+            const float w = es * (t2s * t2s);
+            const uint32_t off = (uint32_t)wn * 64u + ((kc ^ ((uint32_t)wn & 7u)) << 3) + k7;
+            const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+            Wb[wrow + off] = hi;
+            Wb[wrow + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
+            if (++wn == N) { wn = 0; wrow += chunk; }
+        }
         T[NX] = T[NX - 1];
-        hot = hot || (fabsf(TR1 - old) >= tacc);
-        if (!isfinite(TR1)) flags |= ST_NONFINITE;
+        hot = hot || (fabsf(Tsurf - old) >= tacc);
     }
+    if (!isfinite(T[0] + Tref)) flags |= ST_NONFINITE;
 #pragma unroll
-    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = T[i];
+    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = Tref + T[i];
     sv.hot[f] = hot ? 1 : 0;
     if (flags) atomicOr(sv.status, flags);
 }
