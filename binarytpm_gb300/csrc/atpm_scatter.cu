@@ -12,6 +12,10 @@
 //   k_forcing_t       [nf][ntau] -> [ntau][nf] for the conduction sweep
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/atpm.h"
 #include "atpm_internal.h"
 
 namespace atpm {
@@ -209,4 +213,122 @@ int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* 
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+
+// --------------------------------------------------------- no-allocation variant
+// Scattered sunlight over caller-owned device buffers for callers that cannot
+// allocate device memory themselves or through this library: code running
+// where cudaMalloc is unavailable or forbidden (inside a framework that owns
+// every device allocation through its own pool, or a host loop that must not
+// trigger allocator synchronisation).  The Gauss-Seidel work arrays live in a
+// fixed file-scope device array instead of a per-call allocation.
+//
+//  * Limit: nf * ntau <= ATPM_NOALLOC_MAX_CELLS (2^20 cells, 12 MiB of
+//    scratch); larger problems are rejected with ATPM_E_UNSUPPORTED.  Every
+//    GPU that loads the library reserves this array until the process exits.
+//  * The first call on a device looks up the array's device address with
+//    cudaGetSymbolAddress, with that device current; make that first call
+//    before any stream capture on the device.
+//  * All calls share the one array: calls whose work overlaps on the GPU
+//    (different streams, or different host threads) race and corrupt each
+//    other's results.  Serialise them.
+//  * The array keeps the previous call's contents; every cell a call reads is
+//    written by that call first (the status word is cleared by each call).
+namespace {
+constexpr size_t kNoAllocMaxCells = size_t(1) << 20;
+constexpr size_t kNoAllocStatusSlot = 3 * kNoAllocMaxCells;  // one int after the three arrays
+static __device__ __align__(256) float g_noalloc_scratch[3 * kNoAllocMaxCells + 64];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};  // per-device address of g_noalloc_scratch
+
+int noalloc_scratch(void** out, int* device, char* err, size_t errlen) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        std::snprintf(err, errlen, "cudaGetDevice: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    if (dev < 0 || dev >= 256) {
+        std::snprintf(err, errlen, "device ordinal %d out of range", dev);
+        return 1;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            std::snprintf(err, errlen, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+            return 1;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    *device = dev;
+    return 0;
+}
+}  // namespace
+
+void set_last_error(const char* msg);
+
 }  // namespace atpm
+
+extern "C" ATPM_API atpm_status atpm_scattering_noalloc(
+    int32_t nf, int32_t ntau, const int32_t* dep_ptr, const int32_t* dep_idx, const float* dep_vf,
+    const float* cosillum, const uint8_t* shadow, float solar, float albedo, float scattering_accuracy,
+    int32_t multiple, float* illumination, int32_t* status, void* stream) {
+    using namespace atpm;
+    char err[256];
+    if (nf < 1 || ntau < 1 || !dep_ptr || !cosillum || !shadow || !illumination) {
+        set_last_error("scattering_noalloc: bad arguments");
+        return ATPM_E_INVALID;
+    }
+    if ((size_t)nf * (size_t)ntau > kNoAllocMaxCells) {
+        std::snprintf(err, sizeof err,
+                      "scattering_noalloc: nf*ntau = %lld exceeds the fixed scratch of %lld cells; "
+                      "use atpm_scattering",
+                      (long long)nf * ntau, (long long)kNoAllocMaxCells);
+        set_last_error(err);
+        return ATPM_E_UNSUPPORTED;
+    }
+    void* scratch = nullptr;
+    int dev = 0;
+    if (noalloc_scratch(&scratch, &dev, err, sizeof err)) {
+        set_last_error(err);
+        return ATPM_E_CUDA;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int* st_word = status ? status : reinterpret_cast<int*>(static_cast<float*>(scratch) + kNoAllocStatusSlot);
+    if (!status) {
+        cudaError_t e = cudaMemsetAsync(st_word, 0, sizeof(int), st);
+        if (e != cudaSuccess) {
+            std::snprintf(err, sizeof err, "scattering_noalloc: %s", cudaGetErrorString(e));
+            set_last_error(err);
+            return ATPM_E_CUDA;
+        }
+    }
+    DevSolve sv{};
+    sv.nf = nf;
+    sv.ntau = ntau;
+    sv.mode = MODE_REF;
+    sv.dep_ptr = dep_ptr;
+    sv.dep_idx = dep_idx;
+    sv.dep_vf = dep_vf;
+    sv.nnz = 0;
+    sv.shadow = const_cast<uint8_t*>(shadow);
+    sv.cosil = const_cast<float*>(cosillum);
+    sv.Efm = illumination;
+    sv.status = st_word;
+    sv.solar = solar;
+    sv.alb = albedo;
+    sv.sacc = scattering_accuracy;
+    dim3 blk(32, 8), grd((ntau + 31) / 32, (nf + 7) / 8);
+    k_single_scatter<MODE_REF><<<grd, blk, 0, st>>>(sv);
+    if (multiple) k_multi_gs<MODE_REF><<<ntau, 32, 0, st>>>(sv, scratch, 1000);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        std::snprintf(err, sizeof err, "scattering_noalloc launch: %s", cudaGetErrorString(e));
+        set_last_error(err);
+        return ATPM_E_CUDA;
+    }
+    return ATPM_OK;
+}

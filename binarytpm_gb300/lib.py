@@ -69,6 +69,9 @@ _SIGS = {
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_scattering_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
     "atpm_viewfactors_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "atpm_viewfactors_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

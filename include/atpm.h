@@ -184,6 +184,29 @@ ATPM_API atpm_status atpm_viewfactors_get(const atpm_vf_result* r, int32_t* dep_
                                           float* dep_vec, float* photovectors);
 ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
 
+/* ---- no device allocation ----
+ * Single + multiple scattering (the computation of atpm_scattering) over
+ * caller-owned DEVICE buffers, allocating nothing: for callers that cannot
+ * allocate device memory (a framework that owns every allocation through its
+ * own pool, or code that must not trigger allocator synchronisation).  The
+ * Gauss-Seidel work arrays live in one fixed file-scope device array of
+ * 2^20 cells x 3 floats (12 MiB), reserved on every GPU that loads the
+ * library until exit.  No counterpart in the reference.
+ *   nf * ntau must be <= 2^20, otherwise ATPM_E_UNSUPPORTED.
+ *   dep_ptr/idx/vf: CSR lists; cosillum [nf][ntau] float; shadow [nf][ntau]
+ *   bytes 0/1; illumination [nf][ntau] float output.  status: optional
+ *   device int the kernels OR ST_* bits into (8 = scattering cap reached);
+ *   the caller zeroes it.  Work is enqueued on `stream` (a cudaStream_t,
+ *   NULL = default stream); the call returns without waiting for it.
+ *   The first call on a device looks up the array's address
+ *   (cudaGetSymbolAddress) with that device current: make it before any
+ *   stream capture on that device.  Calls share the array: calls that
+ *   overlap on the GPU race and must be serialised by the caller. */
+ATPM_API atpm_status atpm_scattering_noalloc(int32_t nf, int32_t ntau, const int32_t* dep_ptr, const int32_t* dep_idx,
+                                             const float* dep_vf, const float* cosillum, const uint8_t* shadow,
+                                             float solar, float albedo, float scattering_accuracy, int32_t multiple,
+                                             float* illumination, int32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
