@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/atpm.h"
+#include "atpm_host.h"
 #include "atpm_internal.h"
 
 using namespace atpm;
@@ -57,40 +58,6 @@ const float kSIGMA = 5.67e-8f;             // main.cpp:15
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
-
-struct atpm_context {
-    int device = 0;
-    std::mutex mu;
-    bool tables = false;
-    HostPowTab p4, p3;
-};
-
-struct atpm_solve {
-    atpm_context* ctx = nullptr;
-    atpm_params P{};
-    int nf = 0, nv = 0, nnz = 0;
-    size_t rs = 4;  // bytes per state scalar
-    cudaStream_t st = nullptr;
-    void* arena = nullptr;
-    size_t arena_bytes = 0;
-    DevSolve ds{};
-    DevSolve* ds_dev = nullptr;
-    int4* wmap = nullptr;
-    int2* fmap = nullptr;
-    int nw = 0, nfb = 0;
-    void* tc_mem = nullptr;   // tensor-core tiles + W tiles (FAST)
-    int4* qmap = nullptr;
-    int nq = 0;
-    cudaGraphExec_t graph = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::vector<double> vert_h;
-    std::vector<int32_t> fac_h;
-    bool have_forcing = false, have_temps = false;
-    float ti = 0.0f;
-    double last_ms = 0.0;
-    int64_t last_launches = 0, last_facet_steps = 0;
-    int last_nrev = 0;
-};
 
 namespace {
 
@@ -480,6 +447,76 @@ atpm_status get_transposed(atpm_solve* s, const void* dev, size_t rows, size_t c
 
 namespace atpm {
 void set_last_error(const char* msg) { g_err = msg; }
+atpm_status fail_status(atpm_status s, const char* msg) {
+    g_err = msg;
+    return s;
+}
+
+namespace {
+struct HostTable {
+    std::vector<DevSolve> tab;
+    std::vector<int4> wm, qm;
+    std::vector<int2> fm;
+    int nmax = 0;
+    size_t bt = 0, bw = 0, bf = 0, bq = 0;
+};
+void host_table(atpm_solve* const* solves, int n, HostTable& h) {
+    h.tab.resize(n);
+    for (int i = 0; i < n; ++i) {
+        h.tab[i] = solves[i]->ds;
+        std::vector<int4> w1;
+        build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, h.fm);
+        if (solves[i]->nnz > 0) h.wm.insert(h.wm.end(), w1.begin(), w1.end());
+        if (solves[i]->nq > 0) {
+            build_tc_maps(solves[i]->nf, solves[i]->P.ntau, i, h.qm);
+            h.nmax = std::max(h.nmax, solves[i]->ds.tc_n);
+        }
+    }
+    h.bt = align256(n * sizeof(DevSolve));
+    h.bw = align256(std::max<size_t>(h.wm.size(), 1) * sizeof(int4));
+    h.bf = align256(h.fm.size() * sizeof(int2));
+    h.bq = align256(std::max<size_t>(h.qm.size(), 1) * sizeof(int4));
+}
+}  // namespace
+
+size_t batch_table_bytes(atpm_solve* const* solves, int n) {
+    HostTable h;
+    host_table(solves, n, h);
+    return h.bt + h.bw + h.bf + h.bq;
+}
+
+atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st) {
+    HostTable h;
+    host_table(solves, n, h);
+    char* t = static_cast<char*>(table);
+    CK(cudaMemcpyAsync(t, h.tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice, st));
+    if (!h.wm.empty()) CK(cudaMemcpyAsync(t + h.bt, h.wm.data(), h.wm.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(t + h.bt + h.bw, h.fm.data(), h.fm.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    if (!h.qm.empty())
+        CK(cudaMemcpyAsync(t + h.bt + h.bw + h.bf, h.qm.data(), h.qm.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));  // host staging above is released on return
+    atpm_solve* s0 = solves[0];
+    Batch b = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + h.bt), (int)h.wm.size(),
+                         reinterpret_cast<int2*>(t + h.bt + h.bw), (int)h.fm.size(), s0->P.precision, s0->P.nx);
+    b.qmap = reinterpret_cast<int4*>(t + h.bt + h.bw + h.bf);
+    b.nq = (int)h.qm.size();
+    b.tc_nmax = h.nmax;
+    for (int r = 0; r < k; ++r)
+        if (launch_revolution(b, st)) return fail(ATPM_E_CUDA, "batched revolution launch");
+    return ATPM_OK;
+}
+
+atpm_status copy_forcing(atpm_solve* from, atpm_solve* to, cudaStream_t st) {
+    if (from->nf != to->nf || from->P.ntau != to->P.ntau || from->rs != to->rs)
+        return fail(ATPM_E_INVALID, "copy_forcing: solves differ in size or precision");
+    const size_t nt = (size_t)from->nf * from->P.ntau;
+    CK(cudaMemcpyAsync(to->ds.shadow, from->ds.shadow, nt, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(to->ds.cosil, from->ds.cosil, nt * from->rs, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(to->ds.Efm, from->ds.Efm, nt * from->rs, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(to->ds.E, from->ds.E, nt * from->rs, cudaMemcpyDeviceToDevice, st));
+    to->have_forcing = true;
+    return ATPM_OK;
+}
 }  // namespace atpm
 
 // =================================================================== C ABI

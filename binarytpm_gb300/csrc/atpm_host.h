@@ -1,0 +1,57 @@
+// Host-side objects of libatpm shared by the C ABI (atpm_capi.cpp) and the
+// serving scheduler (atpm_server.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/atpm.h"
+#include "atpm_internal.h"
+
+struct atpm_context {
+    int device = 0;
+    std::mutex mu;
+    bool tables = false;
+    atpm::HostPowTab p4, p3;
+};
+
+struct atpm_solve {
+    atpm_context* ctx = nullptr;
+    atpm_params P{};
+    int nf = 0, nv = 0, nnz = 0;
+    size_t rs = 4;  // bytes per state scalar
+    cudaStream_t st = nullptr;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    atpm::DevSolve ds{};
+    atpm::DevSolve* ds_dev = nullptr;
+    int4* wmap = nullptr;
+    int2* fmap = nullptr;
+    int nw = 0, nfb = 0;
+    void* tc_mem = nullptr;   // tensor-core tiles + W tiles (FAST)
+    int4* qmap = nullptr;
+    int nq = 0;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<double> vert_h;
+    std::vector<int32_t> fac_h;
+    bool have_forcing = false, have_temps = false;
+    float ti = 0.0f;
+    double last_ms = 0.0;
+    int64_t last_launches = 0, last_facet_steps = 0;
+    int last_nrev = 0;
+};
+
+
+namespace atpm {
+// one batched revolution chunk for solves that share precision and nx:
+// k revolutions launched directly (no graph); `table` is a caller-owned
+// device buffer of at least batch_table_bytes(solves, n) bytes
+size_t batch_table_bytes(atpm_solve* const* solves, int n);
+atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st);
+// copy the forcing (shadow, Sun angle, illumination) of `from` into `to`
+atpm_status copy_forcing(atpm_solve* from, atpm_solve* to, cudaStream_t st);
+atpm_status fail_status(atpm_status s, const char* msg);
+}  // namespace atpm

@@ -72,6 +72,14 @@ _SIGS = {
     "atpm_scattering_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p,
                                           C.c_void_p, C.c_void_p]),
+    "atpm_server_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_void_p)]),
+    "atpm_server_add_shape": (C.c_int, [C.c_void_p, C.POINTER(Shape), C.POINTER(Params), C.POINTER(C.c_int32)]),
+    "atpm_server_submit": (C.c_int, [C.c_void_p, C.c_int32, C.c_float, C.POINTER(C.c_int64)]),
+    "atpm_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
+    "atpm_server_wait": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_server_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_server_destroy": (C.c_int, [C.c_void_p]),
     "atpm_viewfactors_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                            C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "atpm_viewfactors_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -331,3 +339,61 @@ def profile_revolution(solves):
     out = {k: {"ms": float(v)} for k, v in zip(KERNEL_NAMES, ms)}
     out["conduction"].update(facet_steps=fs.value, active_facets=act.value)
     return out
+
+
+class Server:
+    """Continuous-batching solve server (atpm_server_*)."""
+
+    def __init__(self, ctx: Context, precision: int = FAST, nx: int = 56, budget_bytes: int = 64 << 30,
+                 max_active: int = 64, revs_per_tick: int = 2):
+        h = C.c_void_p()
+        _ck(load().atpm_server_create(ctx.h, precision, nx, budget_bytes, max_active, revs_per_tick, C.byref(h)))
+        self.h, self.precision, self._shapes = h, precision, {}
+
+    def add_shape(self, problem, revcap: int = 301, freeze: bool = True) -> int:
+        v = np.ascontiguousarray(problem.vertices, np.float64)
+        f = np.ascontiguousarray(problem.facets, np.int32)
+        dp = np.ascontiguousarray(problem.dep_ptr, np.int32)
+        di = np.ascontiguousarray(problem.dep_idx, np.int32)
+        dv = np.ascontiguousarray(problem.dep_vf, np.float32)
+        sh = Shape(len(v), len(f), v.ctypes.data, f.ctypes.data, dp.ctypes.data,
+                   di.ctypes.data if len(di) else None, dv.ctypes.data if len(dv) else None)
+        p = make_params(problem, self.precision, revcap, freeze)
+        sid = C.c_int32()
+        _ck(load().atpm_server_add_shape(self.h, C.byref(sh), C.byref(p), C.byref(sid)))
+        self._shapes[sid.value] = (len(f), problem.ntau)
+        return sid.value
+
+    def submit(self, shape_id: int, ti: float) -> int:
+        rid = C.c_int64()
+        _ck(load().atpm_server_submit(self.h, shape_id, float(ti), C.byref(rid)))
+        return rid.value
+
+    def cancel(self, rid: int):
+        _ck(load().atpm_server_cancel(self.h, rid))
+
+    def wait(self, rid: int, shape_id: int, timeout_s: float = 600.0):
+        nf, ntau = self._shapes[shape_id]
+        out = np.zeros((nf, ntau), np.float32)
+        nrev, lat = C.c_int32(), C.c_double()
+        _ck(load().atpm_server_wait(self.h, rid, timeout_s, _p(out), C.byref(nrev), C.byref(lat)))
+        return out, nrev.value, lat.value
+
+    def stats(self):
+        p50, p99, fs = C.c_double(), C.c_double(), C.c_double()
+        n, res = C.c_int64(), C.c_uint64()
+        _ck(load().atpm_server_stats(self.h, C.byref(p50), C.byref(p99), C.byref(fs), C.byref(n), C.byref(res)))
+        return {"p50_s": p50.value, "p99_s": p99.value, "facet_steps_per_s": fs.value, "completed": n.value,
+                "resident_bytes": res.value}
+
+    def close(self):
+        if self.h:
+            rc = load().atpm_server_destroy(self.h)
+            self.h = None
+            _ck(rc)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -184,6 +184,30 @@ ATPM_API atpm_status atpm_viewfactors_get(const atpm_vf_result* r, int32_t* dep_
                                           float* dep_vec, float* photovectors);
 ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
 
+/* ---- serving: continuous batching on one GPU ----
+ * A server keeps many solves resident and advances them together: shapes
+ * are registered once (geometry, shadowing and scattering computed and kept
+ * on the device), requests carry a thermal inertia, are admitted while a
+ * batch slot is free and their device footprint fits the HBM budget, and
+ * every scheduler tick advances all resident solves by revs_per_tick
+ * revolutions in shared launches.  Finished solves are retired (results
+ * copied out, memory returned) and waiting requests admitted in their place.
+ * A result does not depend on what else was in the batch. */
+typedef struct atpm_server atpm_server;
+ATPM_API atpm_status atpm_server_create(atpm_context* ctx, int32_t precision, int32_t nx, uint64_t budget_bytes,
+                                        int32_t max_active, int32_t revs_per_tick, atpm_server** out);
+ATPM_API atpm_status atpm_server_add_shape(atpm_server* s, const atpm_shape* shape, const atpm_params* params,
+                                           int32_t* shape_id);
+ATPM_API atpm_status atpm_server_submit(atpm_server* s, int32_t shape_id, float thermal_inertia, int64_t* request_id);
+ATPM_API atpm_status atpm_server_cancel(atpm_server* s, int64_t request_id);
+/* Wait up to timeout_s for a request; stemp1 [nf][ntau] (may be NULL). */
+ATPM_API atpm_status atpm_server_wait(atpm_server* s, int64_t request_id, double timeout_s, float* stemp1,
+                                      int32_t* nrev, double* latency_s);
+/* Latency percentiles (submit to result) and facet-steps/s of completed requests. */
+ATPM_API atpm_status atpm_server_stats(atpm_server* s, double* p50_s, double* p99_s, double* facet_steps_per_s,
+                                       int64_t* completed, uint64_t* resident_bytes);
+ATPM_API atpm_status atpm_server_destroy(atpm_server* s);
+
 /* ---- no device allocation ----
  * Single + multiple scattering (the computation of atpm_scattering) over
  * caller-owned DEVICE buffers, allocating nothing: for callers that cannot

@@ -230,6 +230,42 @@ def build_thermal(cfg: dict) -> Path:
     return exe
 
 
+_DROPIN_HOOKS = r'''
+#define ATPM_DROPIN_REVCAP ORACLE_REVCAP
+#define ATPM_DROPIN_AFTER_FORCING(A) __oracle_dump_forcing(A)
+#define ATPM_DROPIN_AFTER_TI(A, ti, nrev, counts) do { \
+    FILE* fp_ = fopen("oracle_revs.txt", "a"); \
+    for (int r_ = 0; r_ < (nrev); ++r_) fprintf(fp_, "%.9g %d %d %.9g\n", (ti), r_, (counts)[r_], 0.0); \
+    fclose(fp_); __oracle_dump_temps(A, ti); } while (0)
+#include "thermal_dropin.inc"
+'''
+
+
+def build_thermal_dropin(cfg: dict, lib_dir: Path, include_dir: Path, glue_dir: Path) -> Path:
+    """The reference Thermal driver with single_model replaced by the drop-in
+    glue (binarytpm_gb300/driver/thermal_dropin.inc) over libatpm."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    src_path = thermal_source(full)
+    d = src_path.parent
+    exe = d / ("thermal_dropin_t%d_r%d" % (full["threads"], full["revcap"]))
+    drop = d / "main_dropin.cpp"
+    src = src_path.read_text()
+    i = src.find("int main() {")
+    if i < 0:
+        raise RuntimeError("main() not found in the scratch copy")
+    src = src[:i] + _DROPIN_HOOKS + "\n" + src[i:]
+    src = _replace_from(src, 0, "if (single_run == 1) { single_model(A, S); }",
+                        "if (single_run == 1) { single_model_atpm(A, S); }")
+    drop.write_text(src)
+    cmd = ["g++", *CXXFLAGS, *_gpu_module_defines(full), "-DORACLE_THREADS=%d" % full["threads"],
+           "-DORACLE_REVCAP=%d" % full["revcap"], "-I", str(include_dir), "-I", str(glue_dir), str(drop),
+           str(HERE / "ref_gpu_cpu.cpp"), "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir),
+           "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
 def patch_selfheating(nv: int, nf: int, shape: str, threads: int) -> str:
     src = (REF_ROOT / SELFHEAT_SRC).read_text(errors="replace")
     src = _sub_const(src, "ASTNUMVTX", str(nv))

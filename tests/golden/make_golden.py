@@ -47,6 +47,33 @@ def case_mesh(spec):
     return binary_mesh(p_subdiv=sub, s_subdiv=seed)
 
 
+def thermal_cfg(name: str, threads: int = 1, revcap: int = 301) -> dict:
+    """The compile-time configuration of the reference Thermal run of a case."""
+    c = CASES[name]
+    v, f = case_mesh(c["mesh"])
+    return dict(nv=len(v), nf=len(f), ntau=c["ntau"], nx=c["nx"], polar=c["polar"], rot=c["pole"],
+                rotation_period_s=c["period_h"] * 3600.0, albedo=c["albedo"], tacc=c["tacc"],
+                ti_min=c["ti"][0], ti_max=c["ti"][-1],
+                ti_step=(c["ti"][1] - c["ti"][0]) if len(c["ti"]) > 1 else 10.0,
+                threads=threads, revcap=revcap)
+
+
+def write_thermal_inputs(wd: Path, vertices, facets, dep_ptr, dep_idx, dep_vf) -> None:
+    """Input files the reference Thermal driver reads (main.cpp:400-460)."""
+    mesh.write_shape(wd / "shape.txt", vertices, facets)
+    formats.write_selfheating_list(wd / "shape_selfheating_list.txt", dep_ptr, dep_idx, dep_vf)
+    (wd / "shape_selfheating_vector_list.txt").write_text("")
+    (wd / "shape_photovectors.txt").write_text("0 0 0\n" * len(facets))
+
+
+def prepare_sources() -> None:
+    """Write the scratch copies of the golden Thermal configurations (so a host
+    without the reference checkout can compile them)."""
+    for name, c in CASES.items():
+        if c["kind"] == "thermal":
+            refbuild.thermal_source(thermal_cfg(name))
+
+
 def run_case(name: str, c: dict, threads: int = 8) -> dict:
     v, f = case_mesh(c["mesh"])
     nv, nf = len(v), len(f)
@@ -58,12 +85,7 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
         ptr, idx, vf = formats.read_selfheating_list(wd / "shape_selfheating_list.txt", nf)
         out = dict(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf)
         if c["kind"] == "thermal":
-            cfg = dict(nv=nv, nf=nf, ntau=c["ntau"], nx=c["nx"], polar=c["polar"], rot=c["pole"],
-                       rotation_period_s=c["period_h"] * 3600.0, albedo=c["albedo"], tacc=c["tacc"],
-                       ti_min=c["ti"][0], ti_max=c["ti"][-1],
-                       ti_step=(c["ti"][1] - c["ti"][0]) if len(c["ti"]) > 1 else 10.0,
-                       threads=1)
-            exe = refbuild.build_thermal(cfg)
+            exe = refbuild.build_thermal(thermal_cfg(name))
             refbuild.run(exe, wd)
             ntau = c["ntau"]
             F = np.fromfile(wd / "oracle_forcing.bin", dtype=np.int32).reshape(3, nf, ntau)
