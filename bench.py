@@ -189,7 +189,8 @@ def profile_case():
         s.initialise_temperatures()
     for _ in range(3):
         k = lib.profile_revolution([s0, s1])
-    print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz}))
+    tiles, lo = _tile_stats(prob)
+    print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz, "tiles": tiles, "lo_tiles": lo}))
 
 
 def run_reference_arm(args, world, rank):
@@ -332,7 +333,7 @@ def main():
                    "sample": f"failed: {ex}"}
 
     hbm, bf16, kind = _peaks()
-    roof = _roofline(kern, solves, hbm, kind)
+    roof = _roofline(kern, solves, prob, hbm, bf16, kind)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -442,29 +443,57 @@ def accuracy(ctx, prob, tis, shadow, illum, cosillum):
             "schedule": f"{ACC_REVS} revolutions, every facet advancing (freeze off), same forcing"}
 
 
-def _roofline(kern, solves, hbm, kind):
-    """Dominant kernel: the conduction sweep.  Algorithmic bytes per active
-    facet-step: read E, Q, stemp1 (12 B) + write stemp0, stemp1 (8 B); plus
-    the depth column read and written once per revolution."""
-    k = kern.get("conduction")
-    if not k or not k["ms"]:
-        return None
-    nx = solves[0].nx
-    active_fs = k["facet_steps"]
-    cols = k["active_facets"]
-    bytes_ = active_fs * 20 + cols * 2 * (nx + 1) * 4
-    gbs = bytes_ / (k["ms"] / 1e3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "conduction_fast_nx56_traffic.json"
-    if tf.exists():
-        t = json.loads(tf.read_text())
-        traffic = t["dram_bytes_per_facet_step"] * active_fs
-    flops = active_fs * (5 * (nx - 1) + 20 * 2)
-    return {"kernel": "k_conduction<FAST,56>", "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-            "frac": gbs / hbm, "peak_kind": kind, "traffic": traffic, "algorithmic_bytes": bytes_,
-            "fp32_gflops": flops / (k["ms"] / 1e3) / 1e9,
-            "note": "the sweep is FP32-issue bound; fp32_gflops against 152 SMs x 128 lanes x 2 x clock is "
-                    "the binding roofline"}
+def _tile_stats(prob):
+    """Tile structure of the FAST tensor-core product: 128x64 tiles touched,
+    and how many of them carry the residual (a view factor >= 1e-4)."""
+    rows = np.repeat(np.arange(prob.nf), np.diff(prob.dep_ptr))
+    key = (rows // 128).astype(np.int64) * ((prob.nf + 63) // 64) + prob.dep_idx // 64
+    u, inv = np.unique(key, return_inverse=True)
+    vmax = np.zeros(len(u), np.float32)
+    np.maximum.at(vmax, inv, np.abs(prob.dep_vf))
+    return len(u), int((vmax >= 1e-4).sum())
+
+
+def _roofline(kern, solves, prob, hbm, bf16, kind):
+    """Dominant kernel of the revolution loop: the tensor-core self-heating
+    product (k_spmm_tc).  Algorithmic FLOP per solve-revolution =
+    2 * nnz * NTAU (the list sum); executed = every 128x64 tile x step chunk x
+    (2 or 3 BF16 products for the hi/lo compensation).  The conduction sweep
+    is reported beside it: 20 B algorithmic HBM per facet-step."""
+    out = {}
+    k = kern.get("selfheat_q")
+    n = len(solves)
+    if k and k["ms"]:
+        flops = 2.0 * prob.nnz * prob.ntau * n
+        tiles, lo = _tile_stats(prob)
+        ntau_pad = -(-prob.ntau // 144) * 144 if prob.ntau > 160 else -(-prob.ntau // 16) * 16
+        exe = (2 * tiles + lo) * 128.0 * 64 * ntau_pad * 2 * n
+        traffic = None
+        tf = ROOT / "profiles" / "spmm_tc_traffic.json"
+        if tf.exists():
+            t = json.loads(tf.read_text())
+            traffic = t["dram_bytes_per_tile_chunk"] * tiles * (ntau_pad // 144 if prob.ntau > 160 else 1) * n
+        ach = flops / (k["ms"] / 1e3) / 1e12
+        out = {"kernel": "k_spmm_tc", "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+               "frac": ach / bf16, "peak_kind": kind, "traffic": traffic, "algorithmic_flop": flops,
+               "executed_tflops": exe / (k["ms"] / 1e3) / 1e12, "executed_frac": exe / (k["ms"] / 1e3) / 1e12 / bf16,
+               "note": "algorithmic = 2 nnz NTAU; executed counts the zero padding of the 128x64 BF16 tiles "
+                       f"({tiles} tiles, {lo} with residual) and the hi/lo products"}
+    c = kern.get("conduction")
+    if c and c["ms"]:
+        nx = solves[0].nx
+        bytes_ = c["facet_steps"] * 20 + c["active_facets"] * 2 * (nx + 1) * 4
+        gbs = bytes_ / (c["ms"] / 1e3) / 1e9
+        traffic = None
+        tf = ROOT / "profiles" / "conduction_fast_nx56_traffic.json"
+        if tf.exists():
+            traffic = json.loads(tf.read_text())["dram_bytes_per_facet_step"] * c["facet_steps"]
+        flops = c["facet_steps"] * (5 * (nx - 1) + 20 * 2)
+        out["conduction"] = {"kernel": "k_conduction<FAST,56,3>", "bound": "hbm", "achieved": gbs, "peak": hbm,
+                             "unit": "GB/s", "frac": gbs / hbm, "traffic": traffic, "algorithmic_bytes": bytes_,
+                             "fp32_tflops": flops / (c["ms"] / 1e3) / 1e12,
+                             "note": "FP32-issue bound (about 230 instructions per facet-step at minimum)"}
+    return out
 
 
 def e2e_run(ctx, prob, tis, steps):
