@@ -72,6 +72,17 @@ atpm_status ensure_tables(atpm_context* c) {
     return ATPM_OK;
 }
 
+// x^0.25 exceptions (about 1 s of host powf calls): only REFERENCE solves
+// that initialise temperatures or run at TI 0 need them
+atpm_status ensure_qroot_table(atpm_context* c) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (c->pq.slots_dev) return ATPM_OK;
+    char err[256];
+    CK(cudaSetDevice(c->device));
+    if (build_pow_table(-4, &c->pq, err, sizeof err)) return fail(ATPM_E_CUDA, "%s", err);
+    return ATPM_OK;
+}
+
 PowTab view(const HostPowTab& h) {
     PowTab t;
     t.slots = h.slots_dev;
@@ -342,6 +353,7 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.nx = nx;
     b.p4 = view(ctx->p4);
     b.p3 = view(ctx->p3);
+    b.pq = view(ctx->pq);
     b.qmap = nullptr;
     b.nq = 0;
     b.tc_nmax = 0;
@@ -451,6 +463,8 @@ atpm_status fail_status(atpm_status s, const char* msg) {
     g_err = msg;
     return s;
 }
+atpm_status ensure_pow_tables(atpm_context* c) { return ensure_tables(c); }
+atpm_status ensure_pow_tables_qroot(atpm_context* c) { return ensure_qroot_table(c); }
 
 namespace {
 struct HostTable {
@@ -558,6 +572,7 @@ ATPM_API atpm_status atpm_context_destroy(atpm_context* c) {
     cudaSetDevice(c->device);
     if (c->p4.slots_dev) cudaFree(c->p4.slots_dev);
     if (c->p3.slots_dev) cudaFree(c->p3.slots_dev);
+    if (c->pq.slots_dev) cudaFree(c->pq.slots_dev);
     delete c;
     return ATPM_OK;
 }
@@ -796,6 +811,10 @@ ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
     if (!s) return fail(ATPM_E_INVALID, "null solve");
     if (!(ti >= 0.0f) || !std::isfinite(ti)) return fail(ATPM_E_INVALID, "thermal inertia %g", (double)ti);
     CK(cudaSetDevice(s->ctx->device));
+    if (ti == 0.0f && s->P.precision == ATPM_REFERENCE) {
+        atpm_status rq = ensure_qroot_table(s->ctx);
+        if (rq) return rq;
+    }
     s->ti = ti;
     set_scalars(s, ti);
     atpm_status r = upload_table(s);
@@ -818,27 +837,13 @@ ATPM_API atpm_status atpm_initialise_temperatures(atpm_solve* s) {
     void* mean = static_cast<char*>(s->arena) + layout(s->nv, s->nf, s->nnz, s->P).off[B_MEAN];
     if (launch_initial_mean(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "initial mean launch");
     const atpm_params& P = s->P;
-    if (P.precision == ATPM_FP64) {
-        std::vector<double> m(nf);
-        CK(cudaMemcpyAsync(m.data(), mean, nf * 8, cudaMemcpyDeviceToHost, s->st));
-        CK(cudaStreamSynchronize(s->st));
-        const double alb = P.albedo, es = (double)P.emissivity * (double)kSIGMA;
-        for (int f = 0; f < nf; ++f) m[f] = std::pow((1.0 - alb) * m[f] / es, 0.25);
-        CK(cudaMemcpyAsync(mean, m.data(), nf * 8, cudaMemcpyHostToDevice, s->st));
-        if (launch_fill_initial(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "fill launch");
-        CK(cudaStreamSynchronize(s->st));
-    } else {
-        std::vector<float> m(nf);
-        CK(cudaMemcpyAsync(m.data(), mean, nf * 4, cudaMemcpyDeviceToHost, s->st));
-        CK(cudaStreamSynchronize(s->st));
-        const float es = P.emissivity * kSIGMA;
-        // main.cpp:1458, with this host's libm powf
-        for (int f = 0; f < nf; ++f) m[f] = std::pow((1.0f - P.albedo) * m[f] / es, 0.25f);
-        CK(cudaMemcpyAsync(mean, m.data(), nf * 4, cudaMemcpyHostToDevice, s->st));
-        if (launch_fill_initial(s->ds, mean, s->st)) return fail(ATPM_E_CUDA, "fill launch");
-        if (launch_w_bf16_one(s->ds, s->st)) return fail(ATPM_E_CUDA, "W launch");
-        CK(cudaStreamSynchronize(s->st));
+    if (P.precision == ATPM_REFERENCE) {
+        atpm_status r = ensure_qroot_table(s->ctx);
+        if (r) return r;
     }
+    if (launch_fill_initial(s->ds, mean, view(s->ctx->pq), s->st)) return fail(ATPM_E_CUDA, "fill launch");
+    if (P.precision != ATPM_FP64 && launch_w_bf16_one(s->ds, s->st)) return fail(ATPM_E_CUDA, "W launch");
+    CK(cudaStreamSynchronize(s->st));
     s->have_temps = true;
     return ATPM_OK;
 }

@@ -1,0 +1,299 @@
+// Host side of the crater (roughness) module: runtime-sized C ABI over the
+// kernels of atpm_crater.cu.  One call per function of the reference's GPU
+// module (3905/Thermal/NominalPole/GPU_code.cu:600-1026); arrays are
+// [facet][step][sub-facet] like the module's structs.  Built with
+// -ffp-contract=off: the scalars below follow the module's float expressions.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "atpm_host.h"
+
+using namespace atpm;
+
+struct atpm_crater {
+    atpm_context* ctx = nullptr;
+    int nf = 0, ntau = 0, nx = 0, nsf = 0, precision = 0;
+    cudaStream_t st = nullptr;
+    void* mem = nullptr;
+    float* scratch = nullptr;  // 2 x nf x nsf (initialisation)
+    float PI = 0.0f, rot = 0.0f;
+    bool have_model = false;
+    CraterDev d{};
+};
+
+namespace {
+atpm_status cfail(atpm_status s, const char* what, cudaError_t e) {
+    char b[256];
+    std::snprintf(b, sizeof b, "crater %s: %s", what, cudaGetErrorString(e));
+    return atpm::fail_status(s, b);
+}
+#define CC(call, what)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cfail(ATPM_E_CUDA, what, e_); \
+    } while (0)
+
+size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+atpm_status launch(atpm_crater* c, int what, std::initializer_list<float> f, void* p0 = nullptr,
+                   void* p1 = nullptr) {
+    std::vector<float> fa(f);
+    fa.resize(8, 0.0f);
+    auto view = [](const HostPowTab& h) {
+        PowTab t{};
+        t.slots = h.slots_dev;
+        t.log2slots = h.log2slots;
+        t.lo_bits = h.lo_bits;
+        t.hi_bits = h.hi_bits;
+        return t;
+    };
+    if (crater_launch(what, c->d, view(c->ctx->p4), view(c->ctx->pq), fa.data(), p0, p1, c->st))
+        return cfail(ATPM_E_CUDA, "launch", cudaGetLastError());
+    CC(cudaStreamSynchronize(c->st), "kernel");
+    int stw = 0;
+    CC(cudaMemcpy(&stw, c->d.status, 4, cudaMemcpyDeviceToHost), "status");
+    if (stw & ST_NONFINITE) return atpm::fail_status(ATPM_E_NONFINITE, "crater: non-finite temperature");
+    if (stw & (ST_NEWTON_CAP | ST_SCATTER_CAP)) return atpm::fail_status(ATPM_E_ITERATION, "crater: iteration cap");
+    return ATPM_OK;
+}
+}  // namespace
+
+namespace atpm {
+atpm_status ensure_pow_tables(atpm_context* c);
+atpm_status ensure_pow_tables_qroot(atpm_context* c);
+}
+
+extern "C" {
+
+ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t ntau, int32_t nx, int32_t nsf,
+                                        int32_t precision, atpm_crater** out) {
+    if (!ctx || !out || nf < 1 || ntau < 1 || nsf < 1 || nsf > 128)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_create: bad arguments (nsf <= 128)");
+    if (precision != ATPM_REFERENCE && precision != ATPM_FAST)
+        return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: REFERENCE or FAST precision");
+    if (!crater_nx_supported(nx)) return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: nx not built");
+    if ((size_t)nsf * nsf * 4 + nsf * 8 > 200 * 1024)
+        return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: crater matrix too large for shared memory");
+    CC(cudaSetDevice(ctx->device), "device");
+    atpm_status r = atpm::ensure_pow_tables(ctx);
+    if (!r && precision == ATPM_REFERENCE) r = atpm::ensure_pow_tables_qroot(ctx);
+    if (r) return r;
+    auto* c = new atpm_crater();
+    c->ctx = ctx;
+    c->nf = nf;
+    c->ntau = ntau;
+    c->nx = nx;
+    c->nsf = nsf;
+    c->precision = precision;
+    const size_t fs = (size_t)nf * ntau, fss = fs * nsf;
+    const size_t sz[] = {(size_t)nsf * nsf * 4, 128 * 3 * 4, (size_t)nsf * 3 * 4, (size_t)nsf * 6 * 4, 100 * 2 * 4,
+                         (size_t)nf, (size_t)nf * 4, (size_t)nf * 4, (size_t)nf, fs * 4, fss * 4, fs * 12, fss * 4,
+                         fss * 4, fss * 4, fss * 4, fss * 4, fss * 4, (size_t)nf * (nx + 1) * nsf * 4, 16,
+                         (size_t)nf * nsf * 8};
+    const int n = sizeof(sz) / sizeof(sz[0]);
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) total += al(sz[i]);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->mem, total);
+    if (e != cudaSuccess) {
+        if (c->st) cudaStreamDestroy(c->st);
+        delete c;
+        return cfail(ATPM_E_NOMEM, "allocation", e);
+    }
+    cudaMemset(c->mem, 0, total);
+    char* p = static_cast<char*>(c->mem);
+    void* ptr[32];
+    for (int i = 0; i < n; ++i) {
+        ptr[i] = p;
+        p += al(sz[i]);
+    }
+    CraterDev& d = c->d;
+    d.nf = nf; d.ntau = ntau; d.nx = nx; d.nsf = nsf; d.mode = precision == ATPM_FAST ? MODE_FAST : MODE_REF;
+    d.V = (float*)ptr[0]; d.cverts = (float*)ptr[1]; d.cfac = (int*)ptr[2]; d.ctri = (float*)ptr[3];
+    d.cmult = (float*)ptr[4]; d.conv = (uint8_t*)ptr[5]; d.albedo = (float*)ptr[6]; d.ti = (float*)ptr[7];
+    d.hot = (uint8_t*)ptr[8]; d.shadow = (int*)ptr[9]; d.sfc_shadow = (float*)ptr[10]; d.illumvec = (float*)ptr[11];
+    d.illumangle = (float*)ptr[12]; d.RI = (float*)ptr[13]; d.RGI = (float*)ptr[14]; d.RGH = (float*)ptr[15];
+    d.stemp0 = (float*)ptr[16]; d.stemp1 = (float*)ptr[17]; d.temp = (float*)ptr[18]; d.status = (int*)ptr[19];
+    c->scratch = (float*)ptr[20];
+    // trivector multipliers of the 10x10 sub-points (GPU_code.cu:669-687)
+    float mult[100][2];
+    for (int k = 1; k != 11; ++k)
+        for (int l = 1; l != k + 1; ++l) {
+            const int q = ((k - 1) * (k - 1)) + (2 * (l - 1));
+            mult[q][0] = (float)k - (1.0f / 3.0f);
+            mult[q][1] = (float)l - (2.0f / 3.0f);
+        }
+    for (int k = 2; k != 11; ++k)
+        for (int l = 1; l != k; ++l) {
+            const int q = ((k - 1) * (k - 1)) + (2 * (l - 1)) + 1;
+            mult[q][0] = (float)k - (2.0f / 3.0f);
+            mult[q][1] = (float)l - (1.0f / 3.0f);
+        }
+    cudaMemcpy((void*)d.cmult, mult, sizeof mult, cudaMemcpyHostToDevice);
+    c->PI = 4.0f * std::atan(1.0f);
+    d.PI = c->PI;
+    *out = c;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c) {
+    if (!c) return ATPM_OK;
+    cudaSetDevice(c->ctx->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    if (c->mem) cudaFree(c->mem);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_set_model(atpm_crater* c, int32_t nsv, const float* vertices, const int32_t* facets,
+                                           const float* trivectors, const float* viewfactors, float rot_period) {
+    if (!c || nsv < 3 || nsv > 128 || !vertices || !facets || !trivectors || !viewfactors)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_set_model: bad arguments");
+    for (int i = 0; i < 3 * c->nsf; ++i)
+        if (facets[i] < 0 || facets[i] >= nsv) return atpm::fail_status(ATPM_E_INVALID, "crater_set_model: facet index");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    CC(cudaMemcpy((void*)c->d.V, viewfactors, (size_t)c->nsf * c->nsf * 4, cudaMemcpyHostToDevice), "model");
+    CC(cudaMemcpy((void*)c->d.cverts, vertices, (size_t)nsv * 12, cudaMemcpyHostToDevice), "model");
+    CC(cudaMemcpy((void*)c->d.cfac, facets, (size_t)c->nsf * 12, cudaMemcpyHostToDevice), "model");
+    CC(cudaMemcpy((void*)c->d.ctri, trivectors, (size_t)c->nsf * 24, cudaMemcpyHostToDevice), "model");
+    c->rot = rot_period;
+    c->d.rot_period = rot_period;
+    c->have_model = true;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_set_properties(atpm_crater* c, const uint8_t* converged, const float* albedo,
+                                                const float* ti) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    if (converged) CC(cudaMemcpy(c->d.conv, converged, c->nf, cudaMemcpyHostToDevice), "properties");
+    if (albedo) CC(cudaMemcpy((void*)c->d.albedo, albedo, (size_t)c->nf * 4, cudaMemcpyHostToDevice), "properties");
+    if (ti) CC(cudaMemcpy((void*)c->d.ti, ti, (size_t)c->nf * 4, cudaMemcpyHostToDevice), "properties");
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_get_properties(atpm_crater* c, uint8_t* converged, float* albedo, float* ti) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    if (converged) CC(cudaMemcpy(converged, c->d.conv, c->nf, cudaMemcpyDeviceToHost), "properties");
+    if (albedo) CC(cudaMemcpy(albedo, c->d.albedo, (size_t)c->nf * 4, cudaMemcpyDeviceToHost), "properties");
+    if (ti) CC(cudaMemcpy(ti, c->d.ti, (size_t)c->nf * 4, cudaMemcpyDeviceToHost), "properties");
+    return ATPM_OK;
+}
+
+// which: 0 shadow (int [nf][ntau]), 1 sub-facet shadow, 2 Sun vector ([nf][ntau][3]), 3 sub-facet Sun angle,
+// 4 illumination, 5 global illumination, 6 global heating (sub-facet arrays [nf][ntau][nsf])
+ATPM_API atpm_status atpm_crater_set_array(atpm_crater* c, int32_t which, const void* data) {
+    if (!c || !data || which < 0 || which > 6) return atpm::fail_status(ATPM_E_INVALID, "crater_set_array");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const size_t fs = (size_t)c->nf * c->ntau, fss = fs * c->nsf;
+    void* dst[] = {(void*)c->d.shadow, c->d.sfc_shadow, (void*)c->d.illumvec, (void*)c->d.illumangle, c->d.RI,
+                   (void*)c->d.RGI, (void*)c->d.RGH};
+    const size_t bytes[] = {fs * 4, fss * 4, fs * 12, fss * 4, fss * 4, fss * 4, fss * 4};
+    CC(cudaMemcpy(dst[which], data, bytes[which], cudaMemcpyHostToDevice), "set_array");
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* data) {
+    if (!c || !data || which < 0 || which > 6) return atpm::fail_status(ATPM_E_INVALID, "crater_get_array");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const size_t fs = (size_t)c->nf * c->ntau, fss = fs * c->nsf;
+    const void* src[] = {c->d.shadow, c->d.sfc_shadow, c->d.illumvec, c->d.illumangle, c->d.RI, c->d.RGI, c->d.RGH};
+    const size_t bytes[] = {fs * 4, fss * 4, fs * 12, fss * 4, fss * 4, fss * 4, fss * 4};
+    CC(cudaMemcpy(data, src[which], bytes[which], cudaMemcpyDeviceToHost), "get_array");
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c) {
+    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    return launch(c, 0, {});
+}
+
+ATPM_API atpm_status atpm_crater_scattering(atpm_crater* c, float solar, float accuracy, int32_t multiple) {
+    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    return launch(c, 1, {solar, accuracy, multiple ? 1.0f : 0.0f});
+}
+
+ATPM_API atpm_status atpm_crater_zero_temperatures(atpm_crater* c) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const size_t fss = (size_t)c->nf * c->ntau * c->nsf;
+    CC(cudaMemset(c->d.stemp0, 0, fss * 4), "zero");
+    CC(cudaMemset(c->d.stemp1, 0, fss * 4), "zero");
+    CC(cudaMemset(c->d.temp, 0, (size_t)c->nf * (c->nx + 1) * c->nsf * 4), "zero");
+    return ATPM_OK;
+}
+
+// roughness_initialise_temperatures (GPU_code.cu:328-371): mean absorbed
+// flux -> 4th root -> crater self-heating of that temperature -> second mean
+// -> 4th root -> every depth and step
+ATPM_API atpm_status atpm_crater_initialise_temperatures(atpm_crater* c, float eps, float sigma) {
+    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const float es = eps * sigma;
+    const size_t n = (size_t)c->nf * c->nsf;
+    float* mean = c->scratch;
+    float* selfh = c->scratch + n;
+    // a non-finite value is reported but does not stop the sequence (the
+    // module's kernels run on regardless); any other failure does
+    atpm_status r = ATPM_OK;
+    for (int k = 0; k < 6; ++k) {
+        atpm_status x = ATPM_OK;
+        switch (k) {
+            case 0: x = launch(c, 5, {}, mean, nullptr); break;
+            case 1: x = launch(c, 8, {es}, mean); break;
+            case 2: x = launch(c, 6, {es}, mean, selfh); break;
+            case 3: x = launch(c, 5, {}, mean, selfh); break;
+            case 4: x = launch(c, 8, {es}, mean); break;
+            default: x = launch(c, 7, {}, mean, nullptr); break;
+        }
+        if (x != ATPM_OK) {
+            if (x != ATPM_E_NONFINITE) return x;
+            r = x;
+        }
+    }
+    return r;
+}
+
+// GPU_inertia_difference (GPU_code.cu:982-998): one revolution
+ATPM_API atpm_status atpm_crater_inertia_difference(atpm_crater* c, float eps, float sigma, float tacc) {
+    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const float es = eps * sigma, es4 = 4.0f * es;
+    const float dz = 8.0f / c->nx;
+    const float dtau = (2.0f * c->PI) / c->ntau;
+    const float m0 = dtau / (dz * dz);
+    const float tacc2 = tacc / 10.0f;
+    return launch(c, 2, {es, es4, m0, dz, tacc, tacc2});
+}
+
+ATPM_API atpm_status atpm_crater_inst_equilibrium(atpm_crater* c, float eps, float sigma) {
+    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    return launch(c, 3, {eps * sigma});
+}
+
+ATPM_API atpm_status atpm_crater_converged(atpm_crater* c, float tacc) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    return launch(c, 4, {tacc});
+}
+
+ATPM_API atpm_status atpm_crater_get_temperatures(atpm_crater* c, float* stemp0, float* stemp1, float* temp) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    const size_t fss = (size_t)c->nf * c->ntau * c->nsf;
+    if (stemp0) CC(cudaMemcpy(stemp0, c->d.stemp0, fss * 4, cudaMemcpyDeviceToHost), "get");
+    if (stemp1) CC(cudaMemcpy(stemp1, c->d.stemp1, fss * 4, cudaMemcpyDeviceToHost), "get");
+    if (temp) CC(cudaMemcpy(temp, c->d.temp, (size_t)c->nf * (c->nx + 1) * c->nsf * 4, cudaMemcpyDeviceToHost), "get");
+    return ATPM_OK;
+}
+
+}  // extern "C"

@@ -15,6 +15,7 @@ struct atpm_context {
     std::mutex mu;
     bool tables = false;
     atpm::HostPowTab p4, p3;
+    atpm::HostPowTab pq;  // x^0.25, built on first need
 };
 
 struct atpm_solve {

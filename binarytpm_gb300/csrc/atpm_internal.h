@@ -38,6 +38,29 @@ struct PowTab {
     uint32_t hi_bits;     // one past the last float covered
 };
 
+#ifdef __CUDACC__
+// libm-exact result: table hit -> libm's value, miss -> the device value v;
+// an argument outside the table's range (or no table) flags ST_POW_RANGE
+__device__ __forceinline__ float pow_table_fix(const PowTab& t, float x, float v, int* status) {
+    const uint32_t b = __float_as_uint(x);
+    if (t.slots && b - t.lo_bits < t.hi_bits - t.lo_bits) {
+        const uint32_t mask = (1u << t.log2slots) - 1u;
+        uint32_t h = (b * 2654435761u) >> (32 - t.log2slots);
+        for (int probe = 0; probe < 1024; ++probe) {
+            const uint2 kv = __ldg(&t.slots[h]);
+            if (kv.x == b) return __uint_as_float(kv.y);
+            if (kv.x == 0xFFFFFFFFu) return v;
+            h = (h + 1u) & mask;
+        }
+        return v;
+    }
+    if (x != 0.0f) atomicOr(status, 4 /* ST_POW_RANGE */);
+    return v;
+}
+// x^0.25 through two correctly rounded double square roots (host: emu_qroot)
+__device__ __forceinline__ float dev_qroot(float x) { return (float)__dsqrt_rn(__dsqrt_rn((double)x)); }
+#endif
+
 // per-solve control words (device memory, updated by the advance kernel)
 struct Ctl {
     int rev;        // next revolution index
@@ -129,6 +152,7 @@ struct Batch {
     int nfb;
     int mode, nx;
     PowTab p4, p3;
+    PowTab pq;               // x^0.25 (built only when a REFERENCE solve has TI 0)
     const int4* qmap;        // tensor-core work items {solve, row block, step chunk, 0}
     int nq;
     int tc_nmax;             // largest step chunk in the batch
@@ -138,7 +162,8 @@ int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, conver
 // part 0 W, 1 Q, 2 conduction, 3 convergence, 4 advance
 int launch_revolution_part(const Batch& b, int part, stream_t st);
 int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);
-int launch_fill_initial(const DevSolve& s, const void* t_init, stream_t st);
+// T0 = ((1-A) mean / (eps sigma))^0.25 (x^0.25 exact to libm through pq in REFERENCE)
+int launch_fill_initial(const DevSolve& s, const void* mean, const PowTab& pq, stream_t st);
 int launch_energy_balance(const DevSolve& s, stream_t st);
 // tensor-core self-heating (atpm_spmm_tc.cu)
 int launch_w_bf16(const Batch& b, stream_t st);
@@ -149,16 +174,53 @@ uint32_t tc_swizzle_offset(uint32_t row, uint32_t k);
 int tc_max_chunk();  // largest step chunk N of the tensor-core product
 bool conduction_nx_supported(int nx);
 
+// crater (roughness) module (atpm_crater.cu); layouts [facet][step][sub-facet]
+struct CraterDev {
+    int nf, ntau, nx, nsf, mode;
+    // crater model
+    const float* V;          // [nsf][nsf] V[i][j]
+    const float* cverts;     // [nsv][3]
+    const int* cfac;         // [nsf][3]
+    const float* ctri;       // [nsf][2][3]
+    const float* cmult;      // [100][2] trivector multipliers
+    float PI, rot_period;
+    // per facet
+    uint8_t* conv;           // sfc_converged
+    const float* albedo;
+    const float* ti;
+    uint8_t* hot;            // some |stemp1-stemp0| >= TACC in the last revolution
+    // per facet, step (, sub-facet)
+    const int* shadow;       // [nf][ntau]
+    float* sfc_shadow;       // [nf][ntau][nsf]
+    const float* illumvec;   // [nf][ntau][3]
+    const float* illumangle; // [nf][ntau][nsf]
+    float* RI;               // illumination [nf][ntau][nsf]
+    const float* RGI;        // global illumination
+    const float* RGH;        // global heating
+    float* stemp0;           // [nf][ntau][nsf]
+    float* stemp1;
+    float* temp;             // [nf][nx+1][nsf]
+    int* status;
+};
+
+// what: 0 partial shadow, 1 scattering, 2 revolution, 3 equilibrium,
+// 4 converged, 5 initial mean, 6 initial self-heating, 7 fill, 8 fourth root
+int crater_launch(int what, const CraterDev& c, const PowTab& p4, const PowTab& pq, const float* fargs, void* p0,
+                  void* p1, stream_t st);
+bool crater_nx_supported(int nx);
+
 // pow exception tables (atpm_powtab.cpp)
 struct HostPowTab {
     uint2* slots_dev = nullptr;
     uint32_t log2slots = 0, lo_bits = 0, hi_bits = 0;
     int64_t exceptions = 0;
 };
-// builds the table for exponent e in {3, 4} over [2^-4, 2^12) and uploads it
+// builds the table for exponent e in {3, 4} over [2^-4, 2^12), or for the
+// quarter power (e = -4) over [2^-24, 2^44), and uploads it
 int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen);
 // host emulation of the device's double-float x^e (exact IEEE ops)
 float emu_pow3(float x);
 float emu_pow4(float x);
+float emu_qroot(float x);
 
 }  // namespace atpm

@@ -1,7 +1,8 @@
-// glibc-exact x^3 and x^4 for the REFERENCE precision mode.
+// glibc-exact x^3, x^4 and x^0.25 for the REFERENCE precision mode.
 //
 // The reference evaluates pow(T, 4.0f) and pow(T, 3.0f) with the host libm's
-// powf (3905/Thermal/NominalPole/main.cpp:1523-1538).  glibc's powf is not
+// powf (3905/Thermal/NominalPole/main.cpp:1523-1538), and the instantaneous
+// equilibrium temperature as pow(x, 0.25f) (main.cpp:1455, 1606).  glibc's powf is not
 // correctly rounded: over the floats in [0.5, 5000] about 0.07 % of the
 // results differ by one unit in the last place from the correctly rounded
 // power.  The device evaluates x^e with a double-float product (exact IEEE
@@ -10,6 +11,12 @@
 // The table is built here by calling powf itself on every float of that
 // range (multi-threaded), so it reproduces whatever libm the host links; no
 // libm code or constant is restated.
+//
+// x^0.25 (e = -4) is evaluated on the device as (float)sqrt(sqrt((double)x))
+// (two correctly rounded square roots); about 0.06 % of glibc's powf(x, 0.25f)
+// results differ from it.  Its table covers x in [2^-24, 2^44), temperatures
+// from 2^-6 K to 2048 K (about 3.6e5 exceptions, 1 s on 8 host threads), and
+// is only built when a REFERENCE solve needs it.
 //
 // Build with -ffp-contract=off: the emulation must round each operation.
 #include <cuda_runtime.h>
@@ -46,6 +53,8 @@ float emu_pow3(float x) {
     return p + c;
 }
 
+float emu_qroot(float x) { return (float)std::sqrt(std::sqrt((double)x)); }
+
 static inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 static inline float bitsf(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
@@ -54,9 +63,10 @@ static inline uint32_t slot_of(uint32_t key, uint32_t log2slots) {
 }
 
 int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen) {
-    const float lo = 0.0625f, hi = 4096.0f;
+    const bool q = (e == -4);
+    const float lo = q ? std::ldexp(1.0f, -24) : 0.0625f, hi = q ? std::ldexp(1.0f, 44) : 4096.0f;
     const uint32_t lo_bits = fbits(lo), hi_bits = fbits(hi);
-    const float ef = (float)e;
+    const float ef = q ? 0.25f : (float)e;
     unsigned nth = std::thread::hardware_concurrency();
     if (nth == 0) nth = 4;
     if (nth > 64) nth = 64;
@@ -71,7 +81,7 @@ int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen) {
                 float x = bitsf(u);
                 volatile float xv = x;
                 float ref = std::pow((float)xv, ef);  // libm powf, as the reference
-                float dev = (e == 4) ? emu_pow4(x) : emu_pow3(x);
+                float dev = q ? emu_qroot(x) : (e == 4) ? emu_pow4(x) : emu_pow3(x);
                 if (fbits(ref) != fbits(dev)) found[t].push_back(make_uint2(u, fbits(ref)));
             }
         });

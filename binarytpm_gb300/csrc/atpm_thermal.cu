@@ -67,22 +67,8 @@ __device__ __forceinline__ float dev_pow3(float x) {
     return __fadd_rn(p, c);
 }
 
-// libm-exact result: table hit -> libm's value, miss -> the double-float value
 __device__ __forceinline__ float pow_fix(const PowTab& t, float x, float v, int* status) {
-    uint32_t b = __float_as_uint(x);
-    if (b - t.lo_bits < t.hi_bits - t.lo_bits) {
-        const uint32_t mask = (1u << t.log2slots) - 1u;
-        uint32_t h = (b * 2654435761u) >> (32 - t.log2slots);
-        for (int probe = 0; probe < 1024; ++probe) {
-            uint2 kv = __ldg(&t.slots[h]);
-            if (kv.x == b) return __uint_as_float(kv.y);
-            if (kv.x == 0xFFFFFFFFu) return v;
-            h = (h + 1u) & mask;
-        }
-        return v;
-    }
-    if (x != 0.0f) atomicOr(status, ST_POW_RANGE);
-    return v;
+    return pow_table_fix(t, x, v, status);
 }
 
 template <int MODE> struct Pw;
@@ -361,7 +347,7 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
 
 // instequilibrium (main.cpp:1563-1612): every facet, every step, no depth
 template <int MODE>
-__device__ __forceinline__ void column_equilibrium(const DevSolve& sv, int f) {
+__device__ __forceinline__ void column_equilibrium(const DevSolve& sv, const Batch& b, int f) {
     using A = Ar<MODE>;
     using R = typename A::R;
     const int nf = sv.nf, ntau = sv.ntau;
@@ -379,7 +365,8 @@ __device__ __forceinline__ void column_equilibrium(const DevSolve& sv, int f) {
         const R x = A::div(A::add(A::mul(c.oma, E[o]), Q[o]), c.es);
         R tn;
         if constexpr (MODE == MODE_FP64) tn = sqrt(sqrt(x));
-        else tn = (float)sqrt(sqrt((double)x));
+        else if constexpr (MODE == MODE_REF) tn = pow_fix(b.pq, x, dev_qroot(x), sv.status);  // powf(x, 0.25f)
+        else tn = dev_qroot(x);
         S1[o] = tn;
         if constexpr (MODE == MODE_FAST) {
             if (sv.Wb) store_w(sv, f, s, tn);
@@ -399,7 +386,7 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     const int f = fb.y + threadIdx.x;
     if (f >= sv.nf) return;
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
-    if (inst) { column_equilibrium<MODE>(sv, f); return; }
+    if (inst) { column_equilibrium<MODE>(sv, b, f); return; }
     if (sv.freeze && sv.conv[f]) return;
     if constexpr (MODE == MODE_FAST) column_revolution_fast<NX>(sv, f);
     else column_revolution<MODE, NX>(sv, b, f);
@@ -454,11 +441,21 @@ __global__ void k_initial_mean(DevSolve sv, void* out) {
     static_cast<R*>(out)[f] = t;
 }
 
-template <class R>
-__global__ void k_fill_initial(DevSolve sv, const R* t0) {
+// initialisetemperatures (main.cpp:1455-1462): the facet's mean absorbed
+// flux -> T0 = ((1 - A) mean / (eps sigma))^0.25 everywhere in its column
+template <int MODE>
+__global__ void k_fill_initial(DevSolve sv, const void* mean, PowTab pq) {
+    using R = typename Ar<MODE>::R;
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= sv.nf) return;
-    const R v = t0[f];
+    const R m = static_cast<const R*>(mean)[f];
+    R v;
+    if constexpr (MODE == MODE_FP64) {
+        v = sqrt(sqrt(__ddiv_rn(__dmul_rn(sv.oma_d, m), sv.es_d)));
+    } else {
+        const float x = __fdiv_rn(__fmul_rn(sv.oma, m), sv.es);
+        v = (MODE == MODE_REF) ? pow_fix(pq, x, dev_qroot(x), sv.status) : dev_qroot(x);  // powf(x, 0.25f)
+    }
     R* temp = static_cast<R*>(sv.temp);
     R* S0 = static_cast<R*>(sv.stemp0);
     R* S1 = static_cast<R*>(sv.stemp1);
@@ -576,11 +573,14 @@ int launch_initial_mean(const DevSolve& s, void* out, stream_t stv) {
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-int launch_fill_initial(const DevSolve& s, const void* t0, stream_t stv) {
+int launch_fill_initial(const DevSolve& s, const void* mean, const PowTab& pq, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const int g = (s.nf + 127) / 128;
-    if (s.mode == MODE_FP64) k_fill_initial<double><<<g, 128, 0, st>>>(s, static_cast<const double*>(t0));
-    else k_fill_initial<float><<<g, 128, 0, st>>>(s, static_cast<const float*>(t0));
+    switch (s.mode) {
+        case MODE_REF: k_fill_initial<MODE_REF><<<g, 128, 0, st>>>(s, mean, pq); break;
+        case MODE_FP64: k_fill_initial<MODE_FP64><<<g, 128, 0, st>>>(s, mean, pq); break;
+        default: k_fill_initial<MODE_FAST><<<g, 128, 0, st>>>(s, mean, pq); break;
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

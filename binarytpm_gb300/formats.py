@@ -3,6 +3,12 @@
 * ``<shape>_selfheating_list.txt`` -- one line per facet: ``n idx_1 .. idx_n
   vf_1 .. vf_n`` (``3905/Shape_Selfheating/main.cpp:859-870``, read by
   ``3905/Thermal/NominalPole/main.cpp:418-434``).  Returned as CSR arrays.
+* ``<shape>_selfheating_vector_list.txt`` -- per facet with dependencies,
+  three floats per dependent facet (``3905/Shape_Selfheating/main.cpp:872-882``,
+  read by ``3905/Thermal/NominalPole/main.cpp:436-449``); the crater model's
+  global view factors are built from them.
+* ``<shape>_photovectors.txt`` -- three floats per facet
+  (``3905/Shape_Selfheating/main.cpp:884-887``).
 * ``<shape>_temperature(TI).txt`` -- vertices, facets, then ``NF*NTAU``
   surface temperatures, facet-major (``main.cpp:2290-2308``).
 * ``<shape>_shadow.txt`` / ``_visibility.txt`` -- same header, then
@@ -51,6 +57,32 @@ def write_selfheating_list(path, ptr, idx, vf) -> None:
                 fh.write("".join("%d\t" % i for i in idx[a:b]))
                 fh.write("".join(_g6(v) + "\t" for v in vf[a:b]))
             fh.write("\n")
+
+
+def read_float_stream(path, n: int) -> np.ndarray:
+    """The first n whitespace-separated floats of a file (float32, as the
+    reference's ``operator>>`` into ``float``)."""
+    with open(path) as fh:
+        tok = fh.read().split()
+    if len(tok) < n:
+        raise ValueError(f"{path}: {len(tok)} values, {n} expected")
+    return np.array(tok[:n], dtype=np.float64).astype(np.float32)
+
+
+def write_selfheating_vectors(path, ptr, vec) -> None:
+    """One line per facet: the three vector components of each dependency."""
+    vec = np.asarray(vec).reshape(-1, 3)
+    with open(path, "w") as fh:
+        for f in range(len(ptr) - 1):
+            a, b = int(ptr[f]), int(ptr[f + 1])
+            fh.write("".join("%s\t%s\t%s\t" % (_g6(x[0]), _g6(x[1]), _g6(x[2])) for x in vec[a:b]))
+            fh.write("\n")
+
+
+def write_photovectors(path, pv) -> None:
+    with open(path, "w") as fh:
+        for x in np.asarray(pv).reshape(-1, 3):
+            fh.write("%s\t%s\t%s\n" % (_g6(x[0]), _g6(x[1]), _g6(x[2])))
 
 
 def _header(fh, v, f):

@@ -84,6 +84,23 @@ _SIGS = {
                                            C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "atpm_viewfactors_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_viewfactors_free": (C.c_int, [C.c_void_p]),
+    "atpm_crater_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_void_p)]),
+    "atpm_crater_destroy": (C.c_int, [C.c_void_p]),
+    "atpm_crater_set_model": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_float]),
+    "atpm_crater_set_properties": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_crater_get_properties": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_crater_set_array": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "atpm_crater_get_array": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "atpm_crater_partial_shadow": (C.c_int, [C.c_void_p]),
+    "atpm_crater_scattering": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_int32]),
+    "atpm_crater_zero_temperatures": (C.c_int, [C.c_void_p]),
+    "atpm_crater_initialise_temperatures": (C.c_int, [C.c_void_p, C.c_float, C.c_float]),
+    "atpm_crater_inertia_difference": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float]),
+    "atpm_crater_inst_equilibrium": (C.c_int, [C.c_void_p, C.c_float, C.c_float]),
+    "atpm_crater_converged": (C.c_int, [C.c_void_p, C.c_float]),
+    "atpm_crater_get_temperatures": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -391,6 +408,95 @@ class Server:
             rc = load().atpm_server_destroy(self.h)
             self.h = None
             _ck(rc)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Crater:
+    """Per-facet crater (surface roughness) state on the GPU: the calls of the
+    reference's roughness GPU module (3905/Thermal/NominalPole/GPU_code.cu:600-1026)
+    with runtime sizes.  Sub-facet arrays are [facet][step][sub-facet]."""
+
+    # set_array / get_array slots
+    SHADOW, SFC_SHADOW, SUN_VECTOR, SFC_SUN_ANGLE, ILLUMINATION, GLOBAL_ILLUMINATION, GLOBAL_HEATING = range(7)
+
+    def __init__(self, ctx: Context, nf: int, ntau: int, nx: int, nsf: int = 100, precision: int = REFERENCE):
+        h = C.c_void_p()
+        _ck(load().atpm_crater_create(ctx.h, nf, ntau, nx, nsf, precision, C.byref(h)))
+        self.h, self.nf, self.ntau, self.nx, self.nsf = h, nf, ntau, nx, nsf
+
+    def set_model(self, vertices, facets, trivectors, viewfactors, rotation_period_s: float):
+        v = np.ascontiguousarray(vertices, np.float32)
+        f = np.ascontiguousarray(facets, np.int32)
+        t = np.ascontiguousarray(trivectors, np.float32)
+        vf = np.ascontiguousarray(viewfactors, np.float32)
+        _ck(load().atpm_crater_set_model(self.h, len(v), _p(v), _p(f), _p(t), _p(vf), float(rotation_period_s)))
+
+    def set_properties(self, converged=None, albedo=None, thermal_inertia=None):
+        c = None if converged is None else np.ascontiguousarray(converged, np.uint8)
+        a = None if albedo is None else np.ascontiguousarray(albedo, np.float32)
+        t = None if thermal_inertia is None else np.ascontiguousarray(thermal_inertia, np.float32)
+        _ck(load().atpm_crater_set_properties(self.h, _p(c), _p(a), _p(t)))
+
+    def converged(self) -> np.ndarray:
+        out = np.zeros(self.nf, np.uint8)
+        _ck(load().atpm_crater_get_properties(self.h, _p(out), None, None))
+        return out
+
+    def _shape(self, which: int):
+        if which == self.SHADOW:
+            return (self.nf, self.ntau), np.int32
+        if which == self.SUN_VECTOR:
+            return (self.nf, self.ntau, 3), np.float32
+        return (self.nf, self.ntau, self.nsf), np.float32
+
+    def set_array(self, which: int, data):
+        shape, dt = self._shape(which)
+        a = np.ascontiguousarray(np.asarray(data, dt).reshape(shape))
+        _ck(load().atpm_crater_set_array(self.h, which, _p(a)))
+
+    def get_array(self, which: int) -> np.ndarray:
+        shape, dt = self._shape(which)
+        out = np.zeros(shape, dt)
+        _ck(load().atpm_crater_get_array(self.h, which, _p(out)))
+        return out
+
+    def partial_shadow(self):
+        _ck(load().atpm_crater_partial_shadow(self.h))
+
+    def scattering(self, solar: float, accuracy: float = 1e-4, multiple: bool = True):
+        _ck(load().atpm_crater_scattering(self.h, solar, accuracy, 1 if multiple else 0))
+
+    def zero_temperatures(self):
+        _ck(load().atpm_crater_zero_temperatures(self.h))
+
+    def initialise_temperatures(self, eps: float = 0.9, sigma: float = 5.67e-8):
+        _ck(load().atpm_crater_initialise_temperatures(self.h, eps, sigma))
+
+    def inertia_difference(self, eps: float = 0.9, sigma: float = 5.67e-8, tacc: float = 0.005):
+        _ck(load().atpm_crater_inertia_difference(self.h, eps, sigma, tacc))
+
+    def inst_equilibrium(self, eps: float = 0.9, sigma: float = 5.67e-8):
+        _ck(load().atpm_crater_inst_equilibrium(self.h, eps, sigma))
+
+    def update_converged(self, tacc: float = 0.005):
+        _ck(load().atpm_crater_converged(self.h, tacc))
+
+    def temperatures(self):
+        s0 = np.zeros((self.nf, self.ntau, self.nsf), np.float32)
+        s1 = np.zeros_like(s0)
+        t = np.zeros((self.nf, self.nx + 1, self.nsf), np.float32)
+        _ck(load().atpm_crater_get_temperatures(self.h, _p(s0), _p(s1), _p(t)))
+        return s0, s1, t
+
+    def close(self):
+        if self.h:
+            load().atpm_crater_destroy(self.h)
+            self.h = None
 
     def __del__(self):
         try:

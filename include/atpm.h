@@ -184,6 +184,51 @@ ATPM_API atpm_status atpm_viewfactors_get(const atpm_vf_result* r, int32_t* dep_
                                           float* dep_vec, float* photovectors);
 ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
 
+/* ---- crater (surface roughness) module ----
+ * Runtime-sized counterpart of the reference's Thermal GPU module
+ * (3905/Thermal/NominalPole/GPU_code.cu:600-1026).  Arrays are
+ * [facet][step][sub-facet] like the module's structs; nsf = crater
+ * sub-facets (100 for the shipped crater).  REFERENCE precision follows the
+ * module's float expressions operand by operand (no contraction, this host's
+ * libm powf), FAST contracts. */
+typedef struct atpm_crater atpm_crater;
+/* initialise_GPU_*_arrays (GPU_code.cu:696-768) */
+ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t ntau, int32_t nx, int32_t nsf,
+                                        int32_t precision, atpm_crater** out);
+/* freeup_GPU_*_arrays (774-812) */
+ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c);
+/* initialise_GPU_constants (611-690): crater vertices [nsv][3], facets
+ * [nsf][3], sub-triangle vectors [nsf][2][3], view factors V[i][j] [nsf][nsf] */
+ATPM_API atpm_status atpm_crater_set_model(atpm_crater* c, int32_t nsv, const float* vertices, const int32_t* facets,
+                                           const float* trivectors, const float* viewfactors, float rot_period);
+/* set_GPU_facet_properties / obtain_GPU_facet_properties (818-825, 857-863) */
+ATPM_API atpm_status atpm_crater_set_properties(atpm_crater* c, const uint8_t* converged, const float* albedo,
+                                                const float* thermal_inertia);
+ATPM_API atpm_status atpm_crater_get_properties(atpm_crater* c, uint8_t* converged, float* albedo,
+                                                float* thermal_inertia);
+/* which: 0 facet shadow (int32 [nf][ntau]), 1 sub-facet shadow, 2 crater Sun
+ * vector ([nf][ntau][3]), 3 sub-facet Sun angle, 4 illumination, 5 global
+ * illumination, 6 global heating ([nf][ntau][nsf] floats) -- the fields of
+ * Roughness_Shadow / Illumination / Globalillumination / Globalheating
+ * (GPU_code.cu:85-124; load_GPU_* 831-851, obtain_GPU_* 866-903) */
+ATPM_API atpm_status atpm_crater_set_array(atpm_crater* c, int32_t which, const void* data);
+ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* data);
+/* GPU_sfcpartialshadow (909-921): every step in one launch */
+ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c);
+/* GPU_single_scattering / GPU_multiple_scattering (927-949) */
+ATPM_API atpm_status atpm_crater_scattering(atpm_crater* c, float solar, float accuracy, int32_t multiple);
+/* GPU_zero_temperatures / GPU_initialise_temperatures (955-976) */
+ATPM_API atpm_status atpm_crater_zero_temperatures(atpm_crater* c);
+ATPM_API atpm_status atpm_crater_initialise_temperatures(atpm_crater* c, float eps, float sigma);
+/* GPU_inertia_difference (982-998): one revolution, one launch */
+ATPM_API atpm_status atpm_crater_inertia_difference(atpm_crater* c, float eps, float sigma, float tacc);
+/* GPU_inst_equilibrium (1004-1015) */
+ATPM_API atpm_status atpm_crater_inst_equilibrium(atpm_crater* c, float eps, float sigma);
+/* GPU_converged (1021-1026) */
+ATPM_API atpm_status atpm_crater_converged(atpm_crater* c, float tacc);
+/* obtain_GPU_roughness_temperatures (879-886): [nf][ntau][nsf], temp [nf][nx+1][nsf] */
+ATPM_API atpm_status atpm_crater_get_temperatures(atpm_crater* c, float* stemp0, float* stemp1, float* temp);
+
 /* ---- serving: continuous batching on one GPU ----
  * A server keeps many solves resident and advances them together: shapes
  * are registered once (geometry, shadowing and scattering computed and kept

@@ -240,7 +240,9 @@ template <> struct Real<float> {
 template <> struct Real<double> {
     static double pw4(double x) { double t2 = x * x; return t2 * t2; }
     static double pw3(double x) { return (x * x) * x; }
-    static double pwq(double x) { return std::pow(x, 0.25); }
+    // FP64 mode defines x^0.25 as two correctly rounded square roots (the
+    // GPU's FP64 path evaluates the same expression)
+    static double pwq(double x) { return std::sqrt(std::sqrt(x)); }
     static double cosv(double a) { return cos(a); }
 };
 

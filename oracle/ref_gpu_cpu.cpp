@@ -240,7 +240,7 @@ void k_converged(int b, float TACC) {
 }
 }  // namespace
 
-// ---- the 20 extern "C" entry points (GPU_code.cu:600-1026) ----
+// ---- the 27 extern "C" entry points (GPU_code.cu:600-1026) ----
 extern "C" {
 void set_cuda_device() {}
 

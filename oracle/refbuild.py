@@ -14,7 +14,7 @@ the top of its source (``3905/Thermal/NominalPole/main.cpp:17-76``,
 ``-ffp-contract=off`` pins the x86-64 reference semantics (no fused
 multiply-add) on every host, so an aarch64 build gives the same floats.
 
-The Thermal driver links against the 20 ``extern "C"`` symbols of its GPU
+The Thermal driver links against the 27 ``extern "C"`` symbols of its GPU
 module (``3905/Thermal/NominalPole/GPU_code.cu:600-1026``); for GPU-free runs
 they come from ``oracle/ref_gpu_cpu.cpp``, a CPU restatement of that module.
 
@@ -129,6 +129,30 @@ static void __oracle_dump_temps(Asteroid& A, float ti) {
 '''
 
 
+# Extra instrumentation when the crater (roughness) model is on: per-revolution
+# roughness convergence counts and a dump of the crater forcing.
+_ROUGH_HOOKS = r'''
+static void __oracle_dump_rough_forcing(Asteroid& A) {
+	FILE* fp = fopen("oracle_rough_forcing.bin", "wb");
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = (C->beginsf() + j)->rtnshadow(s); fwrite(&v, 4, 1, fp); }
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = (C->beginsf() + j)->rtnillumangle(s); fwrite(&v, 4, 1, fp); }
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = (C->beginsf() + j)->rtntotalillumination(s); fwrite(&v, 4, 1, fp); }
+	fclose(fp);
+}
+static void __oracle_rough_rev(Asteroid& A, int rev, float ti) {
+	FILE* fp = fopen("oracle_rough_revs.txt", "a");
+	fprintf(fp, "%.9g %d %d\n", ti, rev, A.rtnsfcnumconverged());
+	fclose(fp);
+}
+'''
+
+
 def thermal_defaults() -> dict:
     return dict(
         nv=642, nf=1280, shape="shape", ntau=720, nx=56,
@@ -192,6 +216,15 @@ def patch_thermal(cfg: dict) -> str:
     j = src.find("__oracle_rev_end(A, rev, t_inertia);", i)
     src = _insert_after(src, j, "if (roughness_thermal_model == 1) { retrieve_GPU_roughness_temperatures(A); }",
                         "\n\t\t__oracle_dump_temps(A, t_inertia);")
+    if c["roughness"]:
+        src = src[:i] + _ROUGH_HOOKS + "\n" + src[i:]
+        i = src.find("void single_model(Asteroid& A, Surface& S) {")
+        src = _insert_after(src, i, "retrieve_GPU_roughness_illumination(A);",
+                            "\n\t\t__oracle_dump_rough_forcing(A);")
+        src = _replace_from(src, i, "while (A.rtnsfcconverged() == 0 && rev < 301) {",
+                            "while (A.rtnsfcconverged() == 0 && rev < ORACLE_REVCAP) {")
+        j = src.find("while (A.rtnsfcconverged() == 0 && rev < ORACLE_REVCAP) {", i)
+        src = _replace_from(src, j, "rev = rev + 1;", "__oracle_rough_rev(A, rev, t_inertia);\n\t\t\t\trev = rev + 1;")
     return src
 
 
@@ -263,6 +296,64 @@ def build_thermal_dropin(cfg: dict, lib_dir: Path, include_dir: Path, glue_dir: 
            str(HERE / "ref_gpu_cpu.cpp"), "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir),
            "-o", str(exe)]
     subprocess.run(cmd, check=True)
+    return exe
+
+
+GPU_MODULE_SRC = "3905/Thermal/NominalPole/GPU_code.cu"
+
+
+def gpu_module_source(cfg: dict) -> Path:
+    """Scratch copy of the reference's own GPU module (GPU_code.cu) with the
+    driver's sizes, beside the driver's scratch copy."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    d = thermal_source(full).parent
+    out = d / "GPU_code.cu"
+    if not out.exists():
+        if not (REF_ROOT / GPU_MODULE_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch GPU module in " + str(d))
+        src = (REF_ROOT / GPU_MODULE_SRC).read_text(errors="replace")
+        src = _sub_const(src, "ASTNUMFACE", str(full["nf"]))
+        src = _sub_const(src, "NTAU", str(full["ntau"]))
+        src = _sub_const(src, "NX", str(full["nx"]))
+        out.write_text(src)
+    return out
+
+
+def build_thermal_shim(cfg: dict, lib_dir: Path, include_dir: Path, shim: Path, precision: str = "REFERENCE") -> Path:
+    """The reference Thermal driver, unmodified flow, with its GPU module
+    replaced by binarytpm_gb300/driver/atpm_ref_gpu_shim.cpp over libatpm
+    (crater precision ATPM_REFERENCE or ATPM_FAST)."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    src_path = thermal_source(full)
+    tag = "" if precision == "REFERENCE" else "_" + precision.lower()
+    exe = src_path.parent / ("thermal_shim%s_t%d_r%d" % (tag, full["threads"], full["revcap"]))
+    cmd = ["g++", *CXXFLAGS, *_gpu_module_defines(full), "-DORACLE_THREADS=%d" % full["threads"],
+           "-DATPM_REF_GPU_PRECISION=ATPM_" + precision,
+           "-DORACLE_REVCAP=%d" % full["revcap"], "-I", str(include_dir), str(src_path), str(shim),
+           "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir), "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def build_thermal_refgpu(cfg: dict, cuda_home: str = "/usr/local/cuda") -> Path:
+    """The reference Thermal driver linked with the reference's own GPU module
+    (scratch copy of GPU_code.cu, nvcc for sm_103a with nvcc's defaults, as the
+    reference's Makefile builds it).  Runs only on a GPU host."""
+    full = dict(thermal_defaults())
+    full.update(cfg)
+    src_path = thermal_source(full)
+    cu = gpu_module_source(full)
+    d = src_path.parent
+    obj = d / "gpu_code_sm103a.o"
+    exe = d / ("thermal_refgpu_t%d_r%d" % (full["threads"], full["revcap"]))
+    subprocess.run([cuda_home + "/bin/nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w",
+                    "-c", str(cu), "-o", str(obj)], check=True)
+    subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % full["threads"],
+                    "-DORACLE_REVCAP=%d" % full["revcap"], str(src_path), str(obj),
+                    "-L", cuda_home + "/lib64", "-lcudart", "-Wl,-rpath," + cuda_home + "/lib64",
+                    "-o", str(exe)], check=True)
     return exe
 
 

@@ -37,7 +37,14 @@ CASES = {
                         albedo=0.02, tacc=0.005),
     "vis_s3s1": dict(kind="visibility", mesh=("binary", 3, 1), ntau=48,
                      pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
+    # crater (roughness) model on: TI 0 (instantaneous equilibrium) then 200
+    "rough_s1s1": dict(kind="thermal", rough=True, mesh=("binary", 1, 1), ntau=48, nx=8, ti=[0.0, 200.0],
+                       pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9,
+                       albedo=0.02, tacc=0.005),
 }
+
+# byte-compared outputs (oracle_revs.txt also holds wall times: its counts are stored instead)
+ROUGH_OUTPUTS = ["oracle_rough_forcing.bin", "oracle_rough_revs.txt", "oracle_forcing.bin"]
 
 
 def case_mesh(spec):
@@ -55,15 +62,45 @@ def thermal_cfg(name: str, threads: int = 1, revcap: int = 301) -> dict:
                 rotation_period_s=c["period_h"] * 3600.0, albedo=c["albedo"], tacc=c["tacc"],
                 ti_min=c["ti"][0], ti_max=c["ti"][-1],
                 ti_step=(c["ti"][1] - c["ti"][0]) if len(c["ti"]) > 1 else 10.0,
-                threads=threads, revcap=revcap)
+                threads=threads, revcap=revcap,
+                **(dict(roughness=1, write_roughness_temperature=1) if c.get("rough") else {}))
 
 
-def write_thermal_inputs(wd: Path, vertices, facets, dep_ptr, dep_idx, dep_vf) -> None:
-    """Input files the reference Thermal driver reads (main.cpp:400-460)."""
+def rough_output_files(name: str) -> list[str]:
+    """Files a roughness run writes whose bytes the parity tests compare."""
+    c = CASES[name]
+    out = list(ROUGH_OUTPUTS)
+    for ti in c["ti"]:
+        out.append("shape_roughness_temperature(%g).dat" % ti)
+        out.append("oracle_temps_%g.bin" % ti)
+    return out
+
+
+def write_crater_files(wd: Path, texts: dict) -> None:
+    """The crater model files the driver reads (roughness_filename + .txt,
+    _selfheating_list.txt, _photovectors.txt)."""
+    for n, t in texts.items():
+        (wd / n).write_text(t, newline="")
+
+
+def crater_texts_from(fix) -> dict:
+    return {str(k): str(v) for k, v in zip(fix["crater_names"], fix["crater_texts"])}
+
+
+def write_thermal_inputs(wd: Path, vertices, facets, dep_ptr, dep_idx, dep_vf, dep_vec=None, photo=None) -> None:
+    """Input files the reference Thermal driver reads (main.cpp:400-460).  The
+    dependency vectors and photon-momentum vectors only matter with the crater
+    model on; without them the files are written empty / zero."""
     mesh.write_shape(wd / "shape.txt", vertices, facets)
     formats.write_selfheating_list(wd / "shape_selfheating_list.txt", dep_ptr, dep_idx, dep_vf)
-    (wd / "shape_selfheating_vector_list.txt").write_text("")
-    (wd / "shape_photovectors.txt").write_text("0 0 0\n" * len(facets))
+    if dep_vec is None:
+        (wd / "shape_selfheating_vector_list.txt").write_text("")
+    else:
+        formats.write_selfheating_vectors(wd / "shape_selfheating_vector_list.txt", dep_ptr, dep_vec)
+    if photo is None:
+        (wd / "shape_photovectors.txt").write_text("0 0 0\n" * len(facets))
+    else:
+        formats.write_photovectors(wd / "shape_photovectors.txt", photo)
 
 
 def prepare_sources() -> None:
@@ -72,6 +109,8 @@ def prepare_sources() -> None:
     for name, c in CASES.items():
         if c["kind"] == "thermal":
             refbuild.thermal_source(thermal_cfg(name))
+            if c.get("rough"):
+                refbuild.gpu_module_source(thermal_cfg(name))
 
 
 def run_case(name: str, c: dict, threads: int = 8) -> dict:
@@ -84,7 +123,28 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
         refbuild.run(sh, wd)
         ptr, idx, vf = formats.read_selfheating_list(wd / "shape_selfheating_list.txt", nf)
         out = dict(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf)
-        if c["kind"] == "thermal":
+        if c.get("rough"):
+            out["dep_vec"] = formats.read_float_stream(wd / "shape_selfheating_vector_list.txt", 3 * len(idx))
+            out["photovectors"] = formats.read_float_stream(wd / "shape_photovectors.txt", 3 * nf)
+        if c.get("rough"):
+            import hashlib
+            texts = refbuild.crater_files()
+            write_thermal_inputs(wd, v, f, ptr, idx, vf, out["dep_vec"], out["photovectors"])
+            write_crater_files(wd, texts)
+            exe = refbuild.build_thermal(thermal_cfg(name))   # one thread: a deterministic schedule
+            refbuild.run(exe, wd)
+            names = rough_output_files(name)
+            out["files"] = np.array(names)
+            out["sha256"] = np.array([hashlib.sha256((wd / n).read_bytes()).hexdigest() for n in names])
+            out["crater_names"] = np.array(list(texts))
+            out["crater_texts"] = np.array(list(texts.values()))
+            rr = np.loadtxt(wd / "oracle_rough_revs.txt", ndmin=2)
+            out["rough_counts"] = rr[:, 2].astype(np.int32)
+            out["rough_ti"] = rr[:, 0].astype(np.float32)
+            out["shape_counts"] = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)[:, 2].astype(np.int32)
+            T = np.fromfile(wd / ("shape_roughness_temperature(%g).dat" % c["ti"][-1]), dtype=np.float32)
+            out["rough_stemp1_head"] = T[61 * 3 + 100 * 3:][:100 * c["ntau"]].copy()   # first facet
+        elif c["kind"] == "thermal":
             exe = refbuild.build_thermal(thermal_cfg(name))
             refbuild.run(exe, wd)
             ntau = c["ntau"]

@@ -49,3 +49,20 @@ def test_no_gpu_is_an_error_not_a_fallback():
 
     with pytest.raises(lib.AtpmError):
         lib.Context(0)
+
+
+def test_reference_gpu_module_shim_defines_every_symbol(tmp_path):
+    """binarytpm_gb300/driver/atpm_ref_gpu_shim.cpp defines, with C linkage,
+    every function include/atpm_ref_gpu.h declares (the 27 entry points of the
+    reference's roughness GPU module)."""
+    hdr = (ROOT / "include" / "atpm_ref_gpu.h").read_text()
+    body = hdr[hdr.index('extern "C" {'):]
+    declared = set(re.findall(r"\bvoid\s+(\w+)\s*\(", body))
+    assert len(declared) == 27
+    obj = tmp_path / "shim.o"
+    subprocess.run(["g++", "-std=c++14", "-c", "-DREF_ASTNUMFACE=4", "-DREF_NTAU=8", "-DREF_NX=8",
+                    "-I", str(ROOT / "include"), str(ROOT / "binarytpm_gb300" / "driver" / "atpm_ref_gpu_shim.cpp"),
+                    "-o", str(obj)], check=True)
+    out = subprocess.run(["nm", "--defined-only", str(obj)], capture_output=True, text=True, check=True).stdout
+    defined = set(re.findall(r"\s[Tt]\s+(\w+)$", out, re.M))
+    assert declared <= defined, declared - defined

@@ -47,3 +47,27 @@ def test_golden_cases_exercise_the_path():
     assert prob.nnz > 10000
     assert ref["shadow"].sum() < (ref["cosillum"] > 0).sum()
     assert len(ref["counts_list"]) == 2 and ref["counts_list"][1][-1] == prob.nf
+
+
+def test_crater_oracle_reproduces_golden_digests(tmp_path):
+    """The reference Thermal driver with its crater (roughness) model on, linked
+    with the CPU restatement of its GPU module (oracle/ref_gpu_cpu.cpp), writes
+    the bytes the golden digests record on this host too."""
+    import hashlib
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden
+    from oracle import refbuild
+
+    prob, ref = golden("rough_s1s1")
+    make_golden.write_thermal_inputs(tmp_path, prob.vertices, prob.facets, prob.dep_ptr, prob.dep_idx, prob.dep_vf,
+                                     ref["dep_vec"], ref["photovectors"])
+    make_golden.write_crater_files(tmp_path, make_golden.crater_texts_from(ref))
+    refbuild.run(refbuild.build_thermal(make_golden.thermal_cfg("rough_s1s1")), tmp_path)
+    for name, want in zip(ref["files"], ref["sha256"]):
+        assert hashlib.sha256((tmp_path / str(name)).read_bytes()).hexdigest() == str(want), name
+    # both TI branches ran: equilibrium (TI 0) and conduction (TI 200), each to full convergence
+    assert set(ref["rough_ti"].tolist()) == {0.0, 200.0}
+    assert ref["rough_counts"][-1] == prob.nf
