@@ -75,7 +75,8 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
         return atpm::fail_status(ATPM_E_INVALID, "crater_create: bad arguments (nsf <= 128)");
     if (precision != ATPM_REFERENCE && precision != ATPM_FAST)
         return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: REFERENCE or FAST precision");
-    if (!crater_nx_supported(nx)) return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: nx not built");
+    const bool thermal = nx != 0;  // nx = 0: shadow arrays only (Visibility)
+    if (thermal && !crater_nx_supported(nx)) return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: nx not built");
     if ((size_t)nsf * nsf * 4 + nsf * 8 > 200 * 1024)
         return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_create: crater matrix too large for shared memory");
     CC(cudaSetDevice(ctx->device), "device");
@@ -89,11 +90,11 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
     c->nx = nx;
     c->nsf = nsf;
     c->precision = precision;
-    const size_t fs = (size_t)nf * ntau, fss = fs * nsf;
+    const size_t fs = (size_t)nf * ntau, fss = fs * nsf, th = thermal ? fss * 4 : 0;
     const size_t sz[] = {(size_t)nsf * nsf * 4, 128 * 3 * 4, (size_t)nsf * 3 * 4, (size_t)nsf * 6 * 4, 100 * 2 * 4,
                          (size_t)nf, (size_t)nf * 4, (size_t)nf * 4, (size_t)nf, fs * 4, fss * 4, fs * 12, fss * 4,
-                         fss * 4, fss * 4, fss * 4, fss * 4, fss * 4, (size_t)nf * (nx + 1) * nsf * 4, 16,
-                         (size_t)nf * nsf * 8};
+                         th, th, th, th, th, thermal ? (size_t)nf * (nx + 1) * nsf * 4 : 0, 16,
+                         thermal ? (size_t)nf * nsf * 8 : 0};
     const int n = sizeof(sz) / sizeof(sz[0]);
     size_t total = 0;
     for (int i = 0; i < n; ++i) total += al(sz[i]);
@@ -108,7 +109,7 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
     char* p = static_cast<char*>(c->mem);
     void* ptr[32];
     for (int i = 0; i < n; ++i) {
-        ptr[i] = p;
+        ptr[i] = sz[i] ? p : nullptr;
         p += al(sz[i]);
     }
     CraterDev& d = c->d;
@@ -152,12 +153,13 @@ ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c) {
 
 ATPM_API atpm_status atpm_crater_set_model(atpm_crater* c, int32_t nsv, const float* vertices, const int32_t* facets,
                                            const float* trivectors, const float* viewfactors, float rot_period) {
-    if (!c || nsv < 3 || nsv > 128 || !vertices || !facets || !trivectors || !viewfactors)
+    if (!c || nsv < 3 || nsv > 128 || !vertices || !facets || !trivectors || (!viewfactors && c->nx != 0))
         return atpm::fail_status(ATPM_E_INVALID, "crater_set_model: bad arguments");
     for (int i = 0; i < 3 * c->nsf; ++i)
         if (facets[i] < 0 || facets[i] >= nsv) return atpm::fail_status(ATPM_E_INVALID, "crater_set_model: facet index");
     CC(cudaSetDevice(c->ctx->device), "device");
-    CC(cudaMemcpy((void*)c->d.V, viewfactors, (size_t)c->nsf * c->nsf * 4, cudaMemcpyHostToDevice), "model");
+    if (viewfactors)
+        CC(cudaMemcpy((void*)c->d.V, viewfactors, (size_t)c->nsf * c->nsf * 4, cudaMemcpyHostToDevice), "model");
     CC(cudaMemcpy((void*)c->d.cverts, vertices, (size_t)nsv * 12, cudaMemcpyHostToDevice), "model");
     CC(cudaMemcpy((void*)c->d.cfac, facets, (size_t)c->nsf * 12, cudaMemcpyHostToDevice), "model");
     CC(cudaMemcpy((void*)c->d.ctri, trivectors, (size_t)c->nsf * 24, cudaMemcpyHostToDevice), "model");
@@ -190,6 +192,7 @@ ATPM_API atpm_status atpm_crater_get_properties(atpm_crater* c, uint8_t* converg
 // 4 illumination, 5 global illumination, 6 global heating (sub-facet arrays [nf][ntau][nsf])
 ATPM_API atpm_status atpm_crater_set_array(atpm_crater* c, int32_t which, const void* data) {
     if (!c || !data || which < 0 || which > 6) return atpm::fail_status(ATPM_E_INVALID, "crater_set_array");
+    if (which > 3 && c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "crater_set_array: shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const size_t fs = (size_t)c->nf * c->ntau, fss = fs * c->nsf;
     void* dst[] = {(void*)c->d.shadow, c->d.sfc_shadow, (void*)c->d.illumvec, (void*)c->d.illumangle, c->d.RI,
@@ -201,6 +204,7 @@ ATPM_API atpm_status atpm_crater_set_array(atpm_crater* c, int32_t which, const 
 
 ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* data) {
     if (!c || !data || which < 0 || which > 6) return atpm::fail_status(ATPM_E_INVALID, "crater_get_array");
+    if (which > 3 && c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "crater_get_array: shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const size_t fs = (size_t)c->nf * c->ntau, fss = fs * c->nsf;
     const void* src[] = {c->d.shadow, c->d.sfc_shadow, c->d.illumvec, c->d.illumangle, c->d.RI, c->d.RGI, c->d.RGH};
@@ -216,13 +220,15 @@ ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c) {
 }
 
 ATPM_API atpm_status atpm_crater_scattering(atpm_crater* c, float solar, float accuracy, int32_t multiple) {
-    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    if (!c || !c->have_model || c->nx == 0)
+        return atpm::fail_status(ATPM_E_STATE, "crater: model not set or shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     return launch(c, 1, {solar, accuracy, multiple ? 1.0f : 0.0f});
 }
 
 ATPM_API atpm_status atpm_crater_zero_temperatures(atpm_crater* c) {
     if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    if (c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const size_t fss = (size_t)c->nf * c->ntau * c->nsf;
     CC(cudaMemset(c->d.stemp0, 0, fss * 4), "zero");
@@ -235,7 +241,8 @@ ATPM_API atpm_status atpm_crater_zero_temperatures(atpm_crater* c) {
 // flux -> 4th root -> crater self-heating of that temperature -> second mean
 // -> 4th root -> every depth and step
 ATPM_API atpm_status atpm_crater_initialise_temperatures(atpm_crater* c, float eps, float sigma) {
-    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    if (!c || !c->have_model || c->nx == 0)
+        return atpm::fail_status(ATPM_E_STATE, "crater: model not set or shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const float es = eps * sigma;
     const size_t n = (size_t)c->nf * c->nsf;
@@ -264,7 +271,8 @@ ATPM_API atpm_status atpm_crater_initialise_temperatures(atpm_crater* c, float e
 
 // GPU_inertia_difference (GPU_code.cu:982-998): one revolution
 ATPM_API atpm_status atpm_crater_inertia_difference(atpm_crater* c, float eps, float sigma, float tacc) {
-    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    if (!c || !c->have_model || c->nx == 0)
+        return atpm::fail_status(ATPM_E_STATE, "crater: model not set or shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const float es = eps * sigma, es4 = 4.0f * es;
     const float dz = 8.0f / c->nx;
@@ -275,19 +283,22 @@ ATPM_API atpm_status atpm_crater_inertia_difference(atpm_crater* c, float eps, f
 }
 
 ATPM_API atpm_status atpm_crater_inst_equilibrium(atpm_crater* c, float eps, float sigma) {
-    if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
+    if (!c || !c->have_model || c->nx == 0)
+        return atpm::fail_status(ATPM_E_STATE, "crater: model not set or shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     return launch(c, 3, {eps * sigma});
 }
 
 ATPM_API atpm_status atpm_crater_converged(atpm_crater* c, float tacc) {
     if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    if (c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     return launch(c, 4, {tacc});
 }
 
 ATPM_API atpm_status atpm_crater_get_temperatures(atpm_crater* c, float* stemp0, float* stemp1, float* temp) {
     if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    if (c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "shadow-only crater");
     CC(cudaSetDevice(c->ctx->device), "device");
     const size_t fss = (size_t)c->nf * c->ntau * c->nsf;
     if (stemp0) CC(cudaMemcpy(stemp0, c->d.stemp0, fss * 4, cudaMemcpyDeviceToHost), "get");

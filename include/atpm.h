@@ -192,13 +192,17 @@ ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
  * module's float expressions operand by operand (no contraction, this host's
  * libm powf), FAST contracts. */
 typedef struct atpm_crater atpm_crater;
-/* initialise_GPU_*_arrays (GPU_code.cu:696-768) */
+/* initialise_GPU_*_arrays (GPU_code.cu:696-768).  nx = 0 creates a
+ * shadow-only crater (the Visibility stage's module,
+ * 3905/Visibility/NominalPole/GPU_code.cu:146-283): only the shadow arrays
+ * (set/get_array 0-3) are held, the thermal calls return ATPM_E_STATE. */
 ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t ntau, int32_t nx, int32_t nsf,
                                         int32_t precision, atpm_crater** out);
 /* freeup_GPU_*_arrays (774-812) */
 ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c);
 /* initialise_GPU_constants (611-690): crater vertices [nsv][3], facets
- * [nsf][3], sub-triangle vectors [nsf][2][3], view factors V[i][j] [nsf][nsf] */
+ * [nsf][3], sub-triangle vectors [nsf][2][3], view factors V[i][j] [nsf][nsf]
+ * (may be NULL for a shadow-only crater) */
 ATPM_API atpm_status atpm_crater_set_model(atpm_crater* c, int32_t nsv, const float* vertices, const int32_t* facets,
                                            const float* trivectors, const float* viewfactors, float rot_period);
 /* set_GPU_facet_properties / obtain_GPU_facet_properties (818-825, 857-863) */

@@ -2,7 +2,7 @@
  * atpm_ref_gpu.h -- the reference Thermal driver's GPU-module interface,
  * exported by binarytpm_gb300/driver/atpm_ref_gpu_shim.cpp over libatpm.
  *
- * The reference driver (3905/Thermal/NominalPole/main.cpp) declares these 20
+ * The reference driver (3905/Thermal/NominalPole/main.cpp) declares these 27
  * functions itself (main.cpp:1850-2411) and links the module that defines
  * them (GPU_code.cu:600-1026).  Like that module, this interface is sized at
  * compile time: define REF_ASTNUMFACE, REF_NTAU and REF_NX to the driver's

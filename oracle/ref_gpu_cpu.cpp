@@ -9,6 +9,11 @@
 //
 // Sizes come from -DREF_ASTNUMFACE / -DREF_NTAU / -DREF_NX (the reference
 // fixes them as compile-time constants, GPU_code.cu:6-12).
+//
+// With -DREF_VISIBILITY_MODULE the file instead provides the six symbols of
+// the Visibility driver's GPU module (3905/Visibility/NominalPole/
+// GPU_code.cu:146-283), whose partial-visibility kernel is the same
+// sfcpartialshadow toward the observer.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -16,6 +21,9 @@
 
 #ifndef REF_ASTNUMFACE
 #error "REF_ASTNUMFACE required"
+#endif
+#if defined(REF_VISIBILITY_MODULE) && !defined(REF_NX)
+#define REF_NX 1
 #endif
 
 namespace {
@@ -240,6 +248,29 @@ void k_converged(int b, float TACC) {
 }
 }  // namespace
 
+#ifdef REF_VISIBILITY_MODULE
+namespace {
+void set_constants(const GPU_Surface& S_H);
+}
+// ---- the six entry points of the Visibility module (GPU_code.cu:146-283) ----
+extern "C" {
+void set_cuda_device() {}
+void initialise_GPU_constants(GPU_Surface S_H) { set_constants(S_H); }
+void initialise_GPU_shadow_arrays() { RS_D = alloc<Roughness_Shadow>(ASTNUMFACE); }
+void freeup_GPU_shadow_arrays() { std::free(RS_D); RS_D = nullptr; }
+void obtain_GPU_roughness_shadows(Roughness_Shadow* H) { std::memcpy(H, RS_D, sizeof(*H) * ASTNUMFACE); }
+void GPU_sfcpartialshadow(Roughness_Shadow* RS_H) {
+    std::memcpy(RS_D, RS_H, sizeof(Roughness_Shadow) * ASTNUMFACE);
+    for (int step = 0; step != NTAU; ++step) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < ASTNUMFACE; ++b) k_sfcpartialshadow(b, step);
+    }
+}
+}
+#else
+namespace {
+void set_constants(const GPU_Surface& S_H);
+}
 // ---- the 27 extern "C" entry points (GPU_code.cu:600-1026) ----
 extern "C" {
 void set_cuda_device() {}
@@ -249,25 +280,7 @@ void initialise_GPU_constants(float rot_period_H, float viewfactors_H[SFCNUMFACE
     c_rot_period = rot_period_H;
     if (!vf_D) vf_D = alloc<float>(SFCNUMFACE * SFCNUMFACE);
     std::memcpy(vf_D, viewfactors_H, sizeof(float) * SFCNUMFACE * SFCNUMFACE);
-    for (int i = 0; i != SFCNUMVTX; ++i)
-        for (int k = 0; k < 3; ++k) c_vertex[i][k] = S_H.SV[i].pos[k];
-    for (int j = 0; j != SFCNUMFACE; ++j) {
-        for (int k = 0; k < 3; ++k) c_facet[j][k] = S_H.SF[j].sfcvertices[k];
-        for (int a = 0; a < 2; ++a)
-            for (int k = 0; k < 3; ++k) c_trivector[j][a][k] = S_H.SF[j].trivector[a][k];
-    }
-    for (int k = 1; k != m + 1; ++k)
-        for (int l = 1; l != k + 1; ++l) {
-            int p = ((k - 1) * (k - 1)) + (2 * (l - 1));
-            c_mult[p][0] = (float)k - (1.0f / 3.0f);
-            c_mult[p][1] = (float)l - (2.0f / 3.0f);
-        }
-    for (int k = 2; k != m + 1; ++k)
-        for (int l = 1; l != k; ++l) {
-            int p = ((k - 1) * (k - 1)) + (2 * (l - 1)) + 1;
-            c_mult[p][0] = (float)k - (2.0f / 3.0f);
-            c_mult[p][1] = (float)l - (1.0f / 3.0f);
-        }
+    set_constants(S_H);
 }
 void initialise_GPU_facet_properties_arrays() { FP_D = alloc<Facet_Properties>(ASTNUMFACE); }
 void initialise_GPU_shadow_arrays() { RS_D = alloc<Roughness_Shadow>(ASTNUMFACE); }
@@ -333,3 +346,29 @@ void GPU_converged(float TACC) {
     for (int b = 0; b < ASTNUMFACE; ++b) k_converged(b, TACC);
 }
 }
+#endif
+
+namespace {
+// crater geometry and the 10x10 sub-point multipliers (GPU_code.cu:611-690)
+void set_constants(const GPU_Surface& S_H) {
+    for (int i = 0; i != SFCNUMVTX; ++i)
+        for (int k = 0; k < 3; ++k) c_vertex[i][k] = S_H.SV[i].pos[k];
+    for (int j = 0; j != SFCNUMFACE; ++j) {
+        for (int k = 0; k < 3; ++k) c_facet[j][k] = S_H.SF[j].sfcvertices[k];
+        for (int a = 0; a < 2; ++a)
+            for (int k = 0; k < 3; ++k) c_trivector[j][a][k] = S_H.SF[j].trivector[a][k];
+    }
+    for (int k = 1; k != m + 1; ++k)
+        for (int l = 1; l != k + 1; ++l) {
+            int p = ((k - 1) * (k - 1)) + (2 * (l - 1));
+            c_mult[p][0] = (float)k - (1.0f / 3.0f);
+            c_mult[p][1] = (float)l - (2.0f / 3.0f);
+        }
+    for (int k = 2; k != m + 1; ++k)
+        for (int l = 1; l != k; ++l) {
+            int p = ((k - 1) * (k - 1)) + (2 * (l - 1)) + 1;
+            c_mult[p][0] = (float)k - (2.0f / 3.0f);
+            c_mult[p][1] = (float)l - (1.0f / 3.0f);
+        }
+}
+}  // namespace

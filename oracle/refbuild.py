@@ -395,29 +395,84 @@ def patch_visibility(cfg: dict) -> str:
     src = _sub_const(src, "ob2", _d(c["observer"][2]))
     src = _sub_const(src, "NTAU", str(c["ntau"]))
     src = _sub_const(src, "num_threads", str(c["threads"]))
-    src = _sub_const(src, "roughness_visibility_test", "0")
-    src = _sub_const(src, "write_roughness_visibility", "0")
+    rough = str(int(c.get("roughness", 0)))
+    src = _sub_const(src, "roughness_visibility_test", rough)
+    src = _sub_const(src, "write_roughness_visibility", rough)
     src = _sub_const(src, "shape_visibility_test", "1")
     src = _sub_const(src, "write_shape_visibility", "1")
     return src
 
 
-def build_visibility(cfg: dict) -> Path:
-    """Reference Visibility driver (all-pairs occultation toward an observer)."""
+def visibility_source(cfg: dict) -> Path:
+    """Write (once) the scratch copy of the Visibility driver for ``cfg``."""
     full = dict(nv=642, nf=1280, shape="shape", ntau=720, rot=(3.14159265358979 / 2, 0.0),
                 observer=(1.0, 0.0, 0.0), threads=1)
     full.update(cfg)
     d = OUT_ROOT / _tag("visibility", full)
-    exe = d / "visibility"
     src_path = d / "main.cpp"
-    if exe.exists():
-        return exe
-    d.mkdir(parents=True, exist_ok=True)
     if not src_path.exists():
         if not (REF_ROOT / VISIB_SRC).exists():
             raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        d.mkdir(parents=True, exist_ok=True)
         src_path.write_text(patch_visibility(full))
-    subprocess.run(["g++", *CXXFLAGS, str(src_path), str(HERE / "ref_vis_stub.cpp"), "-o", str(exe)], check=True)
+    return src_path
+
+
+def _vis_defines(cfg: dict) -> list[str]:
+    return ["-DREF_VISIBILITY_MODULE", f"-DREF_ASTNUMFACE={cfg['nf']}", f"-DREF_NTAU={cfg['ntau']}"]
+
+
+def build_visibility(cfg: dict) -> Path:
+    """Reference Visibility driver (all-pairs occultation toward an observer;
+    with ``roughness`` the crater partial visibility too, through the CPU
+    restatement of its GPU module)."""
+    src_path = visibility_source(cfg)
+    exe = src_path.parent / "visibility"
+    if exe.exists():
+        return exe
+    subprocess.run(["g++", *CXXFLAGS, *_vis_defines(cfg), str(src_path), str(HERE / "ref_gpu_cpu.cpp"),
+                    "-o", str(exe)], check=True)
+    return exe
+
+
+def build_visibility_shim(cfg: dict, lib_dir: Path, include_dir: Path, shim: Path) -> Path:
+    """The Visibility driver with its GPU module replaced by
+    binarytpm_gb300/driver/atpm_ref_vis_gpu_shim.cpp over libatpm."""
+    src_path = visibility_source(cfg)
+    exe = src_path.parent / "visibility_shim"
+    subprocess.run(["g++", *CXXFLAGS, *_vis_defines(cfg), "-I", str(include_dir), str(src_path), str(shim),
+                    "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir), "-o", str(exe)], check=True)
+    return exe
+
+
+VIS_GPU_MODULE_SRC = "3905/Visibility/NominalPole/GPU_code.cu"
+
+
+def visibility_gpu_module_source(cfg: dict) -> Path:
+    """Scratch copy of the Visibility driver's own GPU module with its sizes."""
+    d = visibility_source(cfg).parent
+    out = d / "GPU_code.cu"
+    if not out.exists():
+        if not (REF_ROOT / VIS_GPU_MODULE_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch GPU module in " + str(d))
+        src = (REF_ROOT / VIS_GPU_MODULE_SRC).read_text(errors="replace")
+        src = _sub_const(src, "ASTNUMFACE", str(cfg["nf"]))
+        src = _sub_const(src, "NTAU", str(cfg["ntau"]))
+        out.write_text(src)
+    return out
+
+
+def build_visibility_refgpu(cfg: dict, cuda_home: str = "/usr/local/cuda") -> Path:
+    """The Visibility driver linked with its own GPU module (nvcc, sm_103a)."""
+    src_path = visibility_source(cfg)
+    cu = visibility_gpu_module_source(cfg)
+    d = src_path.parent
+    obj = d / "vis_gpu_code_sm103a.o"
+    exe = d / "visibility_refgpu"
+    subprocess.run([cuda_home + "/bin/nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w",
+                    "-c", str(cu), "-o", str(obj)], check=True)
+    subprocess.run(["g++", *CXXFLAGS, str(src_path), str(obj), "-L", cuda_home + "/lib64", "-lcudart",
+                    "-Wl,-rpath," + cuda_home + "/lib64", "-o", str(exe)], check=True)
     return exe
 
 

@@ -37,6 +37,9 @@ CASES = {
                         albedo=0.02, tacc=0.005),
     "vis_s3s1": dict(kind="visibility", mesh=("binary", 3, 1), ntau=48,
                      pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
+    # crater partial visibility toward the observer (Visibility's GPU module)
+    "vis_rough_s1s1": dict(kind="visibility", rough=True, mesh=("binary", 1, 1), ntau=48,
+                           pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
     # crater (roughness) model on: TI 0 (instantaneous equilibrium) then 200
     "rough_s1s1": dict(kind="thermal", rough=True, mesh=("binary", 1, 1), ntau=48, nx=8, ti=[0.0, 200.0],
                        pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9,
@@ -103,10 +106,21 @@ def write_thermal_inputs(wd: Path, vertices, facets, dep_ptr, dep_idx, dep_vf, d
         formats.write_photovectors(wd / "shape_photovectors.txt", photo)
 
 
+def visibility_cfg(name: str, threads: int = 1) -> dict:
+    """The compile-time configuration of the reference Visibility run of a case."""
+    c = CASES[name]
+    v, f = case_mesh(c["mesh"])
+    return dict(nv=len(v), nf=len(f), ntau=c["ntau"], rot=c["pole"], observer=c["observer"], threads=threads,
+                **(dict(roughness=1) if c.get("rough") else {}))
+
+
 def prepare_sources() -> None:
-    """Write the scratch copies of the golden Thermal configurations (so a host
-    without the reference checkout can compile them)."""
+    """Write the scratch copies of the golden Thermal and Visibility
+    configurations (so a host without the reference checkout can compile them)."""
     for name, c in CASES.items():
+        if c["kind"] == "visibility" and c.get("rough"):
+            refbuild.visibility_source(visibility_cfg(name))
+            refbuild.visibility_gpu_module_source(visibility_cfg(name))
         if c["kind"] == "thermal":
             refbuild.thermal_source(thermal_cfg(name))
             if c.get("rough"):
@@ -123,10 +137,10 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
         refbuild.run(sh, wd)
         ptr, idx, vf = formats.read_selfheating_list(wd / "shape_selfheating_list.txt", nf)
         out = dict(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf)
-        if c.get("rough"):
+        if c["kind"] == "thermal" and c.get("rough"):
             out["dep_vec"] = formats.read_float_stream(wd / "shape_selfheating_vector_list.txt", 3 * len(idx))
             out["photovectors"] = formats.read_float_stream(wd / "shape_photovectors.txt", 3 * nf)
-        if c.get("rough"):
+        if c["kind"] == "thermal" and c.get("rough"):
             import hashlib
             texts = refbuild.crater_files()
             write_thermal_inputs(wd, v, f, ptr, idx, vf, out["dep_vec"], out["photovectors"])
@@ -164,11 +178,23 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
             out["counts"] = np.concatenate(counts)
             out["counts_split"] = np.array([len(x) for x in counts], np.int32)
         else:
-            cfg = dict(nv=nv, nf=nf, ntau=c["ntau"], rot=c["pole"], observer=c["observer"], threads=threads)
+            cfg = visibility_cfg(name, threads=1 if c.get("rough") else threads)
+            if c.get("rough"):
+                import hashlib
+                texts = refbuild.crater_files()
+                write_crater_files(wd, texts)
+                out["crater_names"] = np.array(list(texts))
+                out["crater_texts"] = np.array(list(texts.values()))
             exe = refbuild.build_visibility(cfg)
             refbuild.run(exe, wd)
             flags = formats.read_values_after_header(wd / "shape_visibility.txt", nv, nf, np.int32)
             out["visibility"] = np.packbits(flags.reshape(nf, c["ntau"]).astype(np.uint8))
+            if c.get("rough"):
+                raw = (wd / "shape_roughness_visibility.dat").read_bytes()
+                out["files"] = np.array(["shape_roughness_visibility.dat"])
+                out["sha256"] = np.array([hashlib.sha256(raw).hexdigest()])
+                vis = np.frombuffer(raw, dtype=np.float32)[61 * 3 + 100 * 3:].reshape(nf, 100, c["ntau"])
+                out["rough_vis_mean"] = vis.mean(axis=1).astype(np.float32)   # per facet and step
     out["case"] = np.array(json.dumps(c))
     return out
 

@@ -51,18 +51,21 @@ def test_no_gpu_is_an_error_not_a_fallback():
         lib.Context(0)
 
 
-def test_reference_gpu_module_shim_defines_every_symbol(tmp_path):
-    """binarytpm_gb300/driver/atpm_ref_gpu_shim.cpp defines, with C linkage,
-    every function include/atpm_ref_gpu.h declares (the 27 entry points of the
-    reference's roughness GPU module)."""
-    hdr = (ROOT / "include" / "atpm_ref_gpu.h").read_text()
+@pytest.mark.parametrize("header,shim,count,defines", [
+    ("atpm_ref_gpu.h", "atpm_ref_gpu_shim.cpp", 27, ["-DREF_ASTNUMFACE=4", "-DREF_NTAU=8", "-DREF_NX=8"]),
+    ("atpm_ref_vis_gpu.h", "atpm_ref_vis_gpu_shim.cpp", 6, ["-DREF_ASTNUMFACE=4", "-DREF_NTAU=8"]),
+])
+def test_reference_gpu_module_shim_defines_every_symbol(tmp_path, header, shim, count, defines):
+    """Each shim in binarytpm_gb300/driver defines, with C linkage, every
+    function its header declares (the Thermal driver's 27-entry roughness
+    module, the Visibility driver's 6-entry crater-visibility module)."""
+    hdr = (ROOT / "include" / header).read_text()
     body = hdr[hdr.index('extern "C" {'):]
     declared = set(re.findall(r"\bvoid\s+(\w+)\s*\(", body))
-    assert len(declared) == 27
+    assert len(declared) == count
     obj = tmp_path / "shim.o"
-    subprocess.run(["g++", "-std=c++14", "-c", "-DREF_ASTNUMFACE=4", "-DREF_NTAU=8", "-DREF_NX=8",
-                    "-I", str(ROOT / "include"), str(ROOT / "binarytpm_gb300" / "driver" / "atpm_ref_gpu_shim.cpp"),
-                    "-o", str(obj)], check=True)
+    subprocess.run(["g++", "-std=c++14", "-c", *defines, "-I", str(ROOT / "include"),
+                    str(ROOT / "binarytpm_gb300" / "driver" / shim), "-o", str(obj)], check=True)
     out = subprocess.run(["nm", "--defined-only", str(obj)], capture_output=True, text=True, check=True).stdout
     defined = set(re.findall(r"\s[Tt]\s+(\w+)$", out, re.M))
     assert declared <= defined, declared - defined

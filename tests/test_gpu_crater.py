@@ -139,3 +139,57 @@ def test_fast_crater_within_tolerance_of_reference(gpu_ctx, tmp_path):
         b = _rough_temps(wd_orc, ti, nf, ntau).astype(np.float64)
         lit = es * b ** 4 > 1.0
         assert np.quantile(np.abs(a - b)[lit], 0.9999) < 0.01, ti
+
+
+VIS_CASE = "vis_rough_s1s1"
+
+
+def _vis_inputs(wd: Path):
+    import make_golden
+    from binarytpm_gb300 import mesh
+
+    prob, ref = golden(VIS_CASE)
+    mesh.write_shape(wd / "shape.txt", prob.vertices, prob.facets)
+    make_golden.write_crater_files(wd, make_golden.crater_texts_from(ref))
+    return prob, ref
+
+
+def test_reference_visibility_driver_crater_through_shim_bit_exact(gpu_ctx, tmp_path):
+    """The Visibility driver's crater partial visibility through
+    binarytpm_gb300/driver/atpm_ref_vis_gpu_shim.cpp: the same bytes as the
+    CPU restatement of its GPU module, and the same shape flags."""
+    import make_golden
+    from binarytpm_gb300 import build, formats
+    from oracle import refbuild
+
+    lib = build.build()
+    exe = refbuild.build_visibility_shim(make_golden.visibility_cfg(VIS_CASE), lib.parent, ROOT / "include",
+                                         ROOT / "binarytpm_gb300" / "driver" / "atpm_ref_vis_gpu_shim.cpp")
+    prob, ref = _vis_inputs(tmp_path)
+    refbuild.run(exe, tmp_path)
+    raw = (tmp_path / "shape_roughness_visibility.dat").read_bytes()
+    assert hashlib.sha256(raw).hexdigest() == str(ref["sha256"][0])
+    flags = formats.read_values_after_header(tmp_path / "shape_visibility.txt", prob.nv, prob.nf, np.int32)
+    assert np.array_equal(flags.reshape(prob.nf, prob.ntau), ref["visibility"])
+
+
+def test_reference_visibility_gpu_module_pins_the_restatement(gpu_ctx, tmp_path):
+    """The Visibility driver's own GPU module (nvcc, sm_103a) against its CPU
+    restatement: sub-facet visibilities equal except where a rim sub-point
+    changes sides under multiply-add contraction (one sub-point = 0.01)."""
+    import make_golden
+    from oracle import refbuild
+
+    cfg = make_golden.visibility_cfg(VIS_CASE)
+    wd_ref, wd_orc = tmp_path / "refgpu", tmp_path / "oracle"
+    wd_ref.mkdir()
+    wd_orc.mkdir()
+    prob, _ = _vis_inputs(wd_ref)
+    _vis_inputs(wd_orc)
+    refbuild.run(refbuild.build_visibility_refgpu(cfg), wd_ref)
+    refbuild.run(refbuild.build_visibility(cfg), wd_orc)
+    a = np.fromfile(wd_ref / "shape_roughness_visibility.dat", dtype=np.float32)[61 * 3 + 100 * 3:]
+    b = np.fromfile(wd_orc / "shape_roughness_visibility.dat", dtype=np.float32)[61 * 3 + 100 * 3:]
+    d = np.abs(a - b)
+    assert d.max() <= 0.0100001
+    assert np.sum(d > 0) <= 1e-4 * d.size

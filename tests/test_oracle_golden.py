@@ -71,3 +71,23 @@ def test_crater_oracle_reproduces_golden_digests(tmp_path):
     # both TI branches ran: equilibrium (TI 0) and conduction (TI 200), each to full convergence
     assert set(ref["rough_ti"].tolist()) == {0.0, 200.0}
     assert ref["rough_counts"][-1] == prob.nf
+
+
+def test_crater_visibility_oracle_reproduces_golden_digest(tmp_path):
+    """The reference Visibility driver with crater visibility on, linked with
+    the CPU restatement of its GPU module, writes the golden bytes."""
+    import hashlib
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden
+    from binarytpm_gb300 import mesh
+    from oracle import refbuild
+
+    prob, ref = golden("vis_rough_s1s1")
+    mesh.write_shape(tmp_path / "shape.txt", prob.vertices, prob.facets)
+    make_golden.write_crater_files(tmp_path, make_golden.crater_texts_from(ref))
+    refbuild.run(refbuild.build_visibility(make_golden.visibility_cfg("vis_rough_s1s1")), tmp_path)
+    raw = (tmp_path / "shape_roughness_visibility.dat").read_bytes()
+    assert hashlib.sha256(raw).hexdigest() == str(ref["sha256"][0])
