@@ -174,8 +174,8 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
     extern __shared__ float sm[];
     const int nsf = c.nsf, ntau = c.ntau, f = blockIdx.x;
     if (c.conv[f]) return;  // block-uniform (sfc_converged)
-    float* Vs = sm;              // nsf*nsf
-    float* W = Vs + nsf * nsf;   // nsf: eps sigma T_prev^4 of this step
+    float* Vs = sm;                           // nsf*nsf
+    float* W = Vs + ((nsf * nsf + 3) & ~3);   // nsf, 16-byte aligned: eps sigma T_prev^4 of this step
     for (int k = threadIdx.x; k < nsf * nsf; k += blockDim.x) Vs[k] = c.V[k];
     const int j = threadIdx.x;
     const bool act = j < nsf;
@@ -189,8 +189,23 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
     bool hot = false;
     int flags = 0;
     const size_t base = (size_t)f * ntau * nsf;
+    // the step's forcing and previous-revolution temperature are loaded one
+    // step ahead (they are not written by the current step), so the HBM
+    // latency overlaps the current step's sweep
+    float nx_old = 0.0f, nx_rgh = 0.0f, nx_ri = 0.0f;
+    if (act) {
+        nx_old = c.stemp1[base + j];
+        nx_rgh = c.RGH[base + j];
+        nx_ri = c.RI[base + j];
+    }
     for (int s = 0; s < ntau; ++s) {
         const size_t o = base + (size_t)s * nsf + j;
+        const float old = nx_old, rgh = nx_rgh, ri = nx_ri;
+        if (act && s + 1 < ntau) {
+            nx_old = c.stemp1[o + nsf];
+            nx_rgh = c.RGH[o + nsf];
+            nx_ri = c.RI[o + nsf];
+        }
         // finite_difference (GPU_code.cu:377-412)
         if (act) {
             float t0 = T[0];
@@ -203,17 +218,43 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
             T[NX] = T[NX - 1];
         }
         // boundary_condition (GPU_code.cu:418-490)
-        float old = 0.0f;
         if (act) {
-            old = c.stemp1[o];
             c.stemp0[o] = old;
             W[j] = A::mul(es, cpow4<MODE>(p4, old, c.status));
         }
         __syncthreads();
         if (act) {
-            float inc = c.RGH[o];
-            for (int i = 0; i != nsf; ++i) inc = A::add(inc, A::mul(W[i], Vs[i * nsf + j]));
-            const float m2 = A::add(A::mul(oma, c.RI[o]), inc);
+            // W is read four at a time (one broadcast 16-byte load); the
+            // sum keeps the module's order in REFERENCE precision
+            const float4* W4 = reinterpret_cast<const float4*>(W);
+            const int n4 = nsf >> 2;
+            float inc;
+            if constexpr (MODE == MODE_REF) {
+                inc = rgh;
+                for (int q = 0; q < n4; ++q) {
+                    const float4 w = W4[q];
+                    const float* v = Vs + (4 * q) * nsf + j;
+                    inc = A::add(inc, A::mul(w.x, v[0]));
+                    inc = A::add(inc, A::mul(w.y, v[nsf]));
+                    inc = A::add(inc, A::mul(w.z, v[2 * nsf]));
+                    inc = A::add(inc, A::mul(w.w, v[3 * nsf]));
+                }
+                for (int i = 4 * n4; i < nsf; ++i) inc = A::add(inc, A::mul(W[i], Vs[i * nsf + j]));
+            } else {
+                // four interleaved partial sums: a quarter of the dependent chain
+                float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+                for (int q = 0; q < n4; ++q) {
+                    const float4 w = W4[q];
+                    const float* v = Vs + (4 * q) * nsf + j;
+                    a0 += w.x * v[0];
+                    a1 += w.y * v[nsf];
+                    a2 += w.z * v[2 * nsf];
+                    a3 += w.w * v[3 * nsf];
+                }
+                for (int i = 4 * n4; i < nsf; ++i) a0 += W[i] * Vs[i * nsf + j];
+                inc = rgh + ((a0 + a1) + (a2 + a3));
+            }
+            const float m2 = A::add(A::mul(oma, ri), inc);
             float TR0 = T[0], TR1 = T[0], DT = 1.0f;
             int it = 0;
             while (DT >= tacc2) {
@@ -360,7 +401,7 @@ int crater_launch(int what, const CraterDev& c, const PowTab& p4, const PowTab& 
             break;
         }
         case 2: {  // revolution: fargs = {es, es4, m0, dz, tacc, tacc2}
-            const size_t sm = smv + c.nsf * 4;
+            const size_t sm = (size_t)(((c.nsf * c.nsf + 3) & ~3) + c.nsf) * 4;
 #define NX_CASE(n)                                                                                         \
     case n:                                                                                                \
         if (c.mode == MODE_FAST) {                                                                         \

@@ -213,6 +213,61 @@ ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* 
     return ATPM_OK;
 }
 
+namespace {
+// device base and per-facet bytes of array `which` (0-6 as set/get_array,
+// 7 stemp0, 8 stemp1, 9 depth columns)
+bool array_view(atpm_crater* c, int which, void** dev, size_t* per_facet) {
+    const size_t st = (size_t)c->ntau, sf = st * c->nsf;
+    switch (which) {
+        case 0: *dev = (void*)c->d.shadow; *per_facet = st * 4; return true;
+        case 1: *dev = (void*)c->d.sfc_shadow; *per_facet = sf * 4; return true;
+        case 2: *dev = (void*)c->d.illumvec; *per_facet = st * 12; return true;
+        case 3: *dev = (void*)c->d.illumangle; *per_facet = sf * 4; return true;
+        case 4: *dev = (void*)c->d.RI; *per_facet = sf * 4; break;
+        case 5: *dev = (void*)c->d.RGI; *per_facet = sf * 4; break;
+        case 6: *dev = (void*)c->d.RGH; *per_facet = sf * 4; break;
+        case 7: *dev = (void*)c->d.stemp0; *per_facet = sf * 4; break;
+        case 8: *dev = (void*)c->d.stemp1; *per_facet = sf * 4; break;
+        case 9: *dev = (void*)c->d.temp; *per_facet = (size_t)(c->nx + 1) * c->nsf * 4; break;
+        default: return false;
+    }
+    return c->nx != 0;  // 4-9 exist only on a thermal crater
+}
+}  // namespace
+
+ATPM_API atpm_status atpm_crater_set_array_strided(atpm_crater* c, int32_t which, const void* base,
+                                                   uint64_t facet_stride) {
+    void* dev = nullptr;
+    size_t per = 0;
+    if (!c || !base || !array_view(c, which, &dev, &per) || facet_stride < per)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_set_array_strided: bad arguments");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    if (facet_stride == per)
+        CC(cudaMemcpy(dev, base, per * c->nf, cudaMemcpyHostToDevice), "set_array_strided");
+    else
+        CC(cudaMemcpy2D(dev, per, base, facet_stride, per, c->nf, cudaMemcpyHostToDevice), "set_array_strided");
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_get_array_strided(atpm_crater* c, int32_t which, void* base, uint64_t facet_stride) {
+    void* dev = nullptr;
+    size_t per = 0;
+    if (!c || !base || !array_view(c, which, &dev, &per) || facet_stride < per)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_get_array_strided: bad arguments");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    if (facet_stride == per) {
+        CC(cudaMemcpy(base, dev, per * c->nf, cudaMemcpyDeviceToHost), "get_array_strided");
+        return ATPM_OK;
+    }
+    // a strided copy into freshly allocated (never touched) host memory is
+    // slow when the copy engine meets its page faults row by row: touch the
+    // destination rows first
+    char* b = static_cast<char*>(base);
+    for (int f = 0; f < c->nf; ++f) std::memset(b + (size_t)f * facet_stride, 0, per);
+    CC(cudaMemcpy2D(base, facet_stride, dev, per, per, c->nf, cudaMemcpyDeviceToHost), "get_array_strided");
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c) {
     if (!c || !c->have_model) return atpm::fail_status(ATPM_E_STATE, "crater: model not set");
     CC(cudaSetDevice(c->ctx->device), "device");

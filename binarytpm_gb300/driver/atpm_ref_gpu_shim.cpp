@@ -4,16 +4,16 @@
 // Compile it with the driver instead of GPU_code.cu, with the driver's sizes:
 //   g++ -DREF_ASTNUMFACE=<ASTNUMFACE> -DREF_NTAU=<NTAU> -DREF_NX=<NX>
 //       -I include main.cpp atpm_ref_gpu_shim.cpp -L<dir of libatpm.so> -latpm
-// Each function converts between the module's per-facet structs and the
-// [facet][step][sub-facet] arrays of the runtime-sized ABI (one memcpy per
-// facet and field) and forwards the call; the device state lives in one
-// atpm_crater object, like the module's global device pointers.
+// Each function forwards to the runtime-sized ABI; the module's per-facet
+// structs are transferred field by field with one strided copy each
+// (atpm_crater_{set,get}_array_strided), so nothing is repacked on the host.
+// The device state lives in one atpm_crater object, like the module's global
+// device pointers.
 // ATPM_REF_GPU_PRECISION selects ATPM_REFERENCE (default: bit-identical to a
 // CPU restatement of the module, no contraction) or ATPM_FAST.
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
-#include <cstring>
 #include <vector>
 
 #include "atpm.h"
@@ -53,19 +53,16 @@ atpm_crater* crater() {
     return g_cr;
 }
 
-// per-facet struct field <-> [facet][...] array
-template <class S, class T>
-void gather(const S* aos, size_t field_off, size_t per_facet, std::vector<T>& out) {
-    out.resize((size_t)NF * per_facet);
-    for (int f = 0; f < NF; ++f)
-        std::memcpy(&out[(size_t)f * per_facet], reinterpret_cast<const char*>(&aos[f]) + field_off,
-                    per_facet * sizeof(T));
+// one field of every facet's struct <-> device array `which`
+template <class S>
+void put(int which, const S* aos, size_t field_off) {
+    check(atpm_crater_set_array_strided(crater(), which, reinterpret_cast<const char*>(aos) + field_off, sizeof(S)),
+          "copy to device");
 }
-template <class S, class T>
-void scatter(S* aos, size_t field_off, size_t per_facet, const std::vector<T>& in) {
-    for (int f = 0; f < NF; ++f)
-        std::memcpy(reinterpret_cast<char*>(&aos[f]) + field_off, &in[(size_t)f * per_facet],
-                    per_facet * sizeof(T));
+template <class S>
+void get(int which, S* aos, size_t field_off) {
+    check(atpm_crater_get_array_strided(crater(), which, reinterpret_cast<char*>(aos) + field_off, sizeof(S)),
+          "copy to host");
 }
 
 }  // namespace
@@ -124,59 +121,36 @@ void obtain_GPU_facet_properties(Facet_Properties* FP_H) {
 }
 
 void load_GPU_globalillumination(Roughness_Globalillumination* H) {
-    std::vector<float> a;
-    gather(H, offsetof(Roughness_Globalillumination, sfc_globalillumination), (size_t)NTAU * SFCNUMFACE, a);
-    check(atpm_crater_set_array(crater(), 5, a.data()), "global illumination");
+    put(5, H, offsetof(Roughness_Globalillumination, sfc_globalillumination));
 }
 
 void load_GPU_globalheating(Roughness_Globalheating* H) {
-    std::vector<float> a;
-    gather(H, offsetof(Roughness_Globalheating, sfc_globalheating), (size_t)NTAU * SFCNUMFACE, a);
-    check(atpm_crater_set_array(crater(), 6, a.data()), "global heating");
+    put(6, H, offsetof(Roughness_Globalheating, sfc_globalheating));
 }
 
 void GPU_sfcpartialshadow(Roughness_Shadow* RS_H) {
-    std::vector<int32_t> sh;
-    std::vector<float> ssh, iv, ia;
-    gather(RS_H, offsetof(Roughness_Shadow, shadow), (size_t)NTAU, sh);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_shadow), (size_t)NTAU * SFCNUMFACE, ssh);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_illumvector), (size_t)NTAU * 3, iv);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_illumangle), (size_t)NTAU * SFCNUMFACE, ia);
-    atpm_crater* c = crater();
-    check(atpm_crater_set_array(c, 0, sh.data()), "shadow");
-    check(atpm_crater_set_array(c, 1, ssh.data()), "shadow");
-    check(atpm_crater_set_array(c, 2, iv.data()), "shadow");
-    check(atpm_crater_set_array(c, 3, ia.data()), "shadow");
-    check(atpm_crater_partial_shadow(c), "partial shadow");
+    put(0, RS_H, offsetof(Roughness_Shadow, shadow));
+    put(1, RS_H, offsetof(Roughness_Shadow, sfc_shadow));
+    put(2, RS_H, offsetof(Roughness_Shadow, sfc_illumvector));
+    put(3, RS_H, offsetof(Roughness_Shadow, sfc_illumangle));
+    check(atpm_crater_partial_shadow(crater()), "partial shadow");
 }
 
 void obtain_GPU_roughness_shadows(Roughness_Shadow* RS_H) {
-    std::vector<int32_t> sh((size_t)NF * NTAU);
-    std::vector<float> ssh((size_t)NF * NTAU * SFCNUMFACE), iv((size_t)NF * NTAU * 3), ia(ssh.size());
-    atpm_crater* c = crater();
-    check(atpm_crater_get_array(c, 0, sh.data()), "shadow");
-    check(atpm_crater_get_array(c, 1, ssh.data()), "shadow");
-    check(atpm_crater_get_array(c, 2, iv.data()), "shadow");
-    check(atpm_crater_get_array(c, 3, ia.data()), "shadow");
-    scatter(RS_H, offsetof(Roughness_Shadow, shadow), (size_t)NTAU, sh);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_shadow), (size_t)NTAU * SFCNUMFACE, ssh);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_illumvector), (size_t)NTAU * 3, iv);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_illumangle), (size_t)NTAU * SFCNUMFACE, ia);
+    get(0, RS_H, offsetof(Roughness_Shadow, shadow));
+    get(1, RS_H, offsetof(Roughness_Shadow, sfc_shadow));
+    get(2, RS_H, offsetof(Roughness_Shadow, sfc_illumvector));
+    get(3, RS_H, offsetof(Roughness_Shadow, sfc_illumangle));
 }
 
 void obtain_GPU_roughness_illumination(Roughness_Illumination* RI_H) {
-    std::vector<float> a((size_t)NF * NTAU * SFCNUMFACE);
-    check(atpm_crater_get_array(crater(), 4, a.data()), "illumination");
-    scatter(RI_H, offsetof(Roughness_Illumination, sfc_illumination), (size_t)NTAU * SFCNUMFACE, a);
+    get(4, RI_H, offsetof(Roughness_Illumination, sfc_illumination));
 }
 
 void obtain_GPU_roughness_temperatures(Roughness_Temperatures* RT_H) {
-    const size_t fss = (size_t)NF * NTAU * SFCNUMFACE;
-    std::vector<float> s0(fss), s1(fss), t((size_t)NF * (NX + 1) * SFCNUMFACE);
-    check(atpm_crater_get_temperatures(crater(), s0.data(), s1.data(), t.data()), "temperatures");
-    scatter(RT_H, offsetof(Roughness_Temperatures, sfc_stemp0), (size_t)NTAU * SFCNUMFACE, s0);
-    scatter(RT_H, offsetof(Roughness_Temperatures, sfc_stemp1), (size_t)NTAU * SFCNUMFACE, s1);
-    scatter(RT_H, offsetof(Roughness_Temperatures, sfc_temp), (size_t)(NX + 1) * SFCNUMFACE, t);
+    get(7, RT_H, offsetof(Roughness_Temperatures, sfc_stemp0));
+    get(8, RT_H, offsetof(Roughness_Temperatures, sfc_stemp1));
+    get(9, RT_H, offsetof(Roughness_Temperatures, sfc_temp));
 }
 
 void GPU_single_scattering(float solar) { check(atpm_crater_scattering(crater(), solar, 0.0f, 0), "scattering"); }

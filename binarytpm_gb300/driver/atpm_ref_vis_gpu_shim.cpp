@@ -11,7 +11,6 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
-#include <cstring>
 #include <vector>
 
 #include "atpm.h"
@@ -38,16 +37,15 @@ atpm_crater* crater() {
     return g_cr;
 }
 
-template <class T>
-void gather(const Roughness_Shadow* rs, size_t off, size_t per, std::vector<T>& out) {
-    out.resize((size_t)NF * per);
-    for (int f = 0; f < NF; ++f)
-        std::memcpy(&out[(size_t)f * per], reinterpret_cast<const char*>(&rs[f]) + off, per * sizeof(T));
+template <class S>
+void put(int which, const S* aos, size_t field_off) {
+    check(atpm_crater_set_array_strided(crater(), which, reinterpret_cast<const char*>(aos) + field_off, sizeof(S)),
+          "copy to device");
 }
-template <class T>
-void scatter(Roughness_Shadow* rs, size_t off, size_t per, const std::vector<T>& in) {
-    for (int f = 0; f < NF; ++f)
-        std::memcpy(reinterpret_cast<char*>(&rs[f]) + off, &in[(size_t)f * per], per * sizeof(T));
+template <class S>
+void get(int which, S* aos, size_t field_off) {
+    check(atpm_crater_get_array_strided(crater(), which, reinterpret_cast<char*>(aos) + field_off, sizeof(S)),
+          "copy to host");
 }
 
 }  // namespace
@@ -76,32 +74,18 @@ void initialise_GPU_shadow_arrays() { crater(); }
 void freeup_GPU_shadow_arrays() {}
 
 void GPU_sfcpartialshadow(Roughness_Shadow* RS_H) {
-    std::vector<int32_t> sh;
-    std::vector<float> ssh, iv, ia;
-    gather(RS_H, offsetof(Roughness_Shadow, shadow), (size_t)NTAU, sh);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_shadow), (size_t)NTAU * SFCNUMFACE, ssh);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_illumvector), (size_t)NTAU * 3, iv);
-    gather(RS_H, offsetof(Roughness_Shadow, sfc_illumangle), (size_t)NTAU * SFCNUMFACE, ia);
-    atpm_crater* c = crater();
-    check(atpm_crater_set_array(c, 0, sh.data()), "shadow");
-    check(atpm_crater_set_array(c, 1, ssh.data()), "shadow");
-    check(atpm_crater_set_array(c, 2, iv.data()), "shadow");
-    check(atpm_crater_set_array(c, 3, ia.data()), "shadow");
-    check(atpm_crater_partial_shadow(c), "partial shadow");
+    put(0, RS_H, offsetof(Roughness_Shadow, shadow));
+    put(1, RS_H, offsetof(Roughness_Shadow, sfc_shadow));
+    put(2, RS_H, offsetof(Roughness_Shadow, sfc_illumvector));
+    put(3, RS_H, offsetof(Roughness_Shadow, sfc_illumangle));
+    check(atpm_crater_partial_shadow(crater()), "partial shadow");
 }
 
 void obtain_GPU_roughness_shadows(Roughness_Shadow* RS_H) {
-    std::vector<int32_t> sh((size_t)NF * NTAU);
-    std::vector<float> ssh((size_t)NF * NTAU * SFCNUMFACE), iv((size_t)NF * NTAU * 3), ia(ssh.size());
-    atpm_crater* c = crater();
-    check(atpm_crater_get_array(c, 0, sh.data()), "shadow");
-    check(atpm_crater_get_array(c, 1, ssh.data()), "shadow");
-    check(atpm_crater_get_array(c, 2, iv.data()), "shadow");
-    check(atpm_crater_get_array(c, 3, ia.data()), "shadow");
-    scatter(RS_H, offsetof(Roughness_Shadow, shadow), (size_t)NTAU, sh);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_shadow), (size_t)NTAU * SFCNUMFACE, ssh);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_illumvector), (size_t)NTAU * 3, iv);
-    scatter(RS_H, offsetof(Roughness_Shadow, sfc_illumangle), (size_t)NTAU * SFCNUMFACE, ia);
+    get(0, RS_H, offsetof(Roughness_Shadow, shadow));
+    get(1, RS_H, offsetof(Roughness_Shadow, sfc_shadow));
+    get(2, RS_H, offsetof(Roughness_Shadow, sfc_illumvector));
+    get(3, RS_H, offsetof(Roughness_Shadow, sfc_illumangle));
 }
 
 }  // extern "C"

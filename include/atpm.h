@@ -217,6 +217,15 @@ ATPM_API atpm_status atpm_crater_get_properties(atpm_crater* c, uint8_t* converg
  * (GPU_code.cu:85-124; load_GPU_* 831-851, obtain_GPU_* 866-903) */
 ATPM_API atpm_status atpm_crater_set_array(atpm_crater* c, int32_t which, const void* data);
 ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* data);
+/* The same transfers straight from / into an array of per-facet structs:
+ * facet f's block of array `which` starts at base + f * facet_stride bytes
+ * (the module's AoS layout: pass the field's address in element 0 and
+ * sizeof the struct).  which 7, 8, 9 are stemp0, stemp1 ([nf][ntau][nsf]) and
+ * the depth columns ([nf][nx+1][nsf]) of Roughness_Temperatures.  One strided
+ * copy each way, no host-side repacking. */
+ATPM_API atpm_status atpm_crater_set_array_strided(atpm_crater* c, int32_t which, const void* base,
+                                                   uint64_t facet_stride);
+ATPM_API atpm_status atpm_crater_get_array_strided(atpm_crater* c, int32_t which, void* base, uint64_t facet_stride);
 /* GPU_sfcpartialshadow (909-921): every step in one launch */
 ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c);
 /* GPU_single_scattering / GPU_multiple_scattering (927-949) */
