@@ -83,6 +83,35 @@ atpm_status ensure_qroot_table(atpm_context* c) {
     return ATPM_OK;
 }
 
+// pole transformation matrix, heliocentric body centre and rotation table of
+// the reference's asteroidgeometry (main.cpp:894-958), with this host's libm
+void geometry_tables(const atpm_params& P, double* tm9, double* car, std::vector<double>& rot) {
+    const double r0 = P.pole[0], r1 = P.pole[1];
+    const double gamma = std::acos(std::cos(r0) * std::sin(std::fabs(r1)));
+    double tm[3][3];
+    tm[0][0] = std::sin(r0) / std::sin(gamma);
+    tm[0][1] = -1.0 * std::cos(r0) * std::cos(r0) * std::sin(r1) * std::cos(r1) / std::sin(gamma);
+    tm[0][2] = std::cos(r0) * std::cos(r1);
+    tm[1][0] = 0.0;
+    tm[1][1] = ((std::sin(r0) * std::sin(r0)) + (std::cos(r0) * std::cos(r0) * std::cos(r1) * std::cos(r1))) /
+               std::sin(gamma);
+    tm[1][2] = std::cos(r0) * std::sin(r1);
+    tm[2][0] = -1.0 * std::cos(r0) * std::cos(r1) / std::sin(gamma);
+    tm[2][1] = -1.0 * std::sin(r0) * std::cos(r0) * std::sin(r1) / std::sin(gamma);
+    tm[2][2] = std::sin(r0);
+    for (int i = 0; i < 9; ++i) tm9[i] = tm[i / 3][i % 3];
+    car[0] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::cos(P.polar[2]);
+    car[1] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::sin(P.polar[2]);
+    car[2] = kAU * P.polar[0] * std::sin(P.polar[1]);
+    const int ntau = P.ntau;
+    rot.assign(2 * (size_t)ntau, 0.0);
+    for (int step = 0; step < ntau; ++step) {
+        const double ang = 2.0 * kPI * step / ntau;
+        rot[2 * step] = std::cos(ang);
+        rot[2 * step + 1] = std::sin(ang);
+    }
+}
+
 PowTab view(const HostPowTab& h) {
     PowTab t;
     t.slots = h.slots_dev;
@@ -714,29 +743,8 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     const int ntau = P.ntau;
     // host: pole matrix, heliocentric centre, rotation table (main.cpp:894-958)
     GeomWork g{};
-    const double r0 = P.pole[0], r1 = P.pole[1];
-    const double gamma = std::acos(std::cos(r0) * std::sin(std::fabs(r1)));
-    double tm[3][3];
-    tm[0][0] = std::sin(r0) / std::sin(gamma);
-    tm[0][1] = -1.0 * std::cos(r0) * std::cos(r0) * std::sin(r1) * std::cos(r1) / std::sin(gamma);
-    tm[0][2] = std::cos(r0) * std::cos(r1);
-    tm[1][0] = 0.0;
-    tm[1][1] = ((std::sin(r0) * std::sin(r0)) + (std::cos(r0) * std::cos(r0) * std::cos(r1) * std::cos(r1))) /
-               std::sin(gamma);
-    tm[1][2] = std::cos(r0) * std::sin(r1);
-    tm[2][0] = -1.0 * std::cos(r0) * std::cos(r1) / std::sin(gamma);
-    tm[2][1] = -1.0 * std::sin(r0) * std::cos(r0) * std::sin(r1) / std::sin(gamma);
-    tm[2][2] = std::sin(r0);
-    for (int i = 0; i < 9; ++i) g.tm[i] = tm[i / 3][i % 3];
-    g.car[0] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::cos(P.polar[2]);
-    g.car[1] = kAU * P.polar[0] * std::cos(P.polar[1]) * std::sin(P.polar[2]);
-    g.car[2] = kAU * P.polar[0] * std::sin(P.polar[1]);
-    std::vector<double> rot(2 * (size_t)ntau);
-    for (int step = 0; step < ntau; ++step) {
-        const double ang = 2.0 * kPI * step / ntau;
-        rot[2 * step] = std::cos(ang);
-        rot[2 * step + 1] = std::sin(ang);
-    }
+    std::vector<double> rot;
+    geometry_tables(P, g.tm, g.car, rot);
     const size_t nt = (size_t)s->nf * ntau;
     const size_t bytes = align256((size_t)s->nv * ntau * 24) + align256(nt * 24) * 2 + align256(nt * 8) +
                          align256((size_t)ntau * 16);
@@ -1027,6 +1035,65 @@ ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp) {
     CK(cudaSetDevice(s->ctx->device));
     if (s->rs == 8) return get_transposed<double>(s, s->ds.temp, s->P.nx + 1, s->nf, temp, nullptr);
     return get_transposed<float>(s, s->ds.temp, s->P.nx + 1, s->nf, temp, nullptr);
+}
+
+// observe (3905/Observe/NominalPole/wise_main.cpp:662-730), smooth surface,
+// FP64 on the device; constants wise_main.cpp:10-12
+ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
+                                    double emissivity, int32_t nwl, const double* wavelength_um, double* flux) {
+    if (!s || !observer || !wavelength_um || !flux || nwl < 1 || nwl > kMaxFluxWavelengths)
+        return fail(ATPM_E_INVALID, "disk_flux: bad arguments (1 <= nwl <= %d)", kMaxFluxWavelengths);
+    if (!s->have_temps && s->ti != 0.0f) return fail(ATPM_E_STATE, "disk_flux: no temperatures yet");
+    CK(cudaSetDevice(s->ctx->device));
+    const atpm_params& P = s->P;
+    const int nf = s->nf, ntau = P.ntau;
+    FluxArgs a{};
+    std::vector<double> rot;
+    geometry_tables(P, a.tm, a.car, rot);
+    // the stage places the body at AU(m) x polar and the observer at the body
+    // minus its geocentric vector (wise_main.cpp:8, 530-538)
+    const double AUm = 149.6e9;
+    a.car[0] = AUm * P.polar[0] * std::cos(P.polar[1]) * std::cos(P.polar[2]);
+    a.car[1] = AUm * P.polar[0] * std::cos(P.polar[1]) * std::sin(P.polar[2]);
+    a.car[2] = AUm * P.polar[0] * std::sin(P.polar[1]);
+    a.obs[0] = a.car[0] - (AUm * observer[0] * std::cos(observer[1]) * std::cos(observer[2]));
+    a.obs[1] = a.car[1] - (AUm * observer[0] * std::cos(observer[1]) * std::sin(observer[2]));
+    a.obs[2] = a.car[2] - (AUm * observer[0] * std::sin(observer[1]));
+    a.eps = emissivity;
+    const double cvel = 299792458.0, hcon = 6.626068963e-34, kcon = 1.380650424e-23;
+    a.nwl = nwl;
+    a.hc = hcon * cvel;
+    for (int l = 0; l < nwl; ++l) {
+        const double wl = wavelength_um[l] * 1.0e-6;
+        a.b1[l] = (2.0 * hcon * cvel * cvel) / std::pow(wl, 5.0);
+        a.lk[l] = wl * kcon;
+    }
+    std::vector<uint8_t> vis;
+    if (visibility) {
+        vis.resize((size_t)nf * ntau);
+        for (size_t i = 0; i < vis.size(); ++i) vis[i] = visibility[i] ? 1 : 0;
+    }
+    const size_t b_rot = align256(rot.size() * 8), b_part = align256(flux_partial_bytes(s->ds, nwl)),
+                 b_out = align256((size_t)ntau * nwl * 8), b_vis = align256(vis.size());
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, b_rot + b_part + b_out + b_vis, s->st));
+    char* t = static_cast<char*>(tmp);
+    a.rot = reinterpret_cast<const double*>(t);
+    a.partial = reinterpret_cast<double*>(t + b_rot);
+    a.out = reinterpret_cast<double*>(t + b_rot + b_part);
+    a.visible = visibility ? reinterpret_cast<const uint8_t*>(t + b_rot + b_part + b_out) : nullptr;
+    cudaError_t e = cudaMemcpyAsync((void*)a.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess && visibility)
+        e = cudaMemcpyAsync((void*)a.visible, vis.data(), vis.size(), cudaMemcpyHostToDevice, s->st);
+    int rc = 0;
+    if (e == cudaSuccess) rc = launch_disk_flux(s->ds, a, s->st);
+    if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(flux, a.out, (size_t)ntau * nwl * 8, cudaMemcpyDeviceToHost, s->st);
+    cudaFreeAsync(tmp, s->st);
+    cudaError_t e2 = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "disk_flux: %s", cudaGetErrorString(e));
+    if (rc) return fail(ATPM_E_CUDA, "disk_flux launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "disk_flux: %s", cudaGetErrorString(e2));
+    return ATPM_OK;
 }
 
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted, double* mean_t) {

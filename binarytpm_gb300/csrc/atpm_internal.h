@@ -165,6 +165,25 @@ int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);
 // T0 = ((1-A) mean / (eps sigma))^0.25 (x^0.25 exact to libm through pq in REFERENCE)
 int launch_fill_initial(const DevSolve& s, const void* mean, const PowTab& pq, stream_t st);
 int launch_energy_balance(const DevSolve& s, stream_t st);
+
+// disk-integrated flux (atpm_flux.cu)
+constexpr int kMaxFluxWavelengths = 8;
+struct FluxArgs {
+    const double* rot;       // [ntau][2] cos, sin of the rotation angle (host libm)
+    double tm[9];            // pole matrix
+    double car[3];           // body centre (km)
+    double obs[3];           // observer (km)
+    double eps;
+    const uint8_t* visible;  // [nf][ntau] or null (horizon test only)
+    int nwl;
+    double b1[kMaxFluxWavelengths];  // 2 h c^2 / lambda^5
+    double lk[kMaxFluxWavelengths];  // lambda * k
+    double hc;                       // h * c
+    double* partial;         // [ntau][blocks][nwl]
+    double* out;             // [ntau][nwl]
+};
+size_t flux_partial_bytes(const DevSolve& s, int nwl);
+int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t st);
 // tensor-core self-heating (atpm_spmm_tc.cu)
 int launch_w_bf16(const Batch& b, stream_t st);
 int launch_w_bf16_one(const DevSolve& s, stream_t st);

@@ -65,6 +65,8 @@ _SIGS = {
     "atpm_get_surface_temperature64": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_disk_flux": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p,
+                                 C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -279,6 +281,18 @@ class Solve:
         t = np.zeros((self.nf, self.nx + 1), np.float32)
         _ck(load().atpm_get_depth_temperature(self.h, _p(t)))
         return t
+
+    def disk_flux(self, observer, wavelengths_um=(12.0,), visibility=None, emissivity=0.9):
+        """FP64 disk-integrated flux [ntau][nwl]; `observer` is the body's
+        geocentric (AU, lat, lon) -- the solve's own polar means seen from the
+        Sun; `visibility` [nf][ntau] flags or None for each facet's own
+        horizon test."""
+        ob = np.ascontiguousarray(observer, np.float64)
+        wl = np.ascontiguousarray(wavelengths_um, np.float64)
+        vis = None if visibility is None else np.ascontiguousarray(visibility, np.int32)
+        out = np.zeros((self.ntau, len(wl)), np.float64)
+        _ck(load().atpm_disk_flux(self.h, _p(ob), _p(vis), float(emissivity), len(wl), _p(wl), _p(out)))
+        return out
 
     def energy_balance(self):
         a, e, m = C.c_double(), C.c_double(), C.c_double()

@@ -158,6 +158,24 @@ ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t 
  * current surface temperatures ([ntau][nf] step-major), through the solve's
  * own path (list-order gather, or the BF16 tensor-core product for FAST). */
 ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q);
+/* Disk-integrated thermal flux seen by an observer, FP64 on the device: the
+ * smooth-surface sum of the Observe stage's observe
+ * (3905/Observe/NominalPole/wise_main.cpp:662-730, its geometry 555-645).
+ * observer: the body's position as seen by the observer (distance in AU,
+ * ecliptic latitude, longitude in rad: the stage's obs_polar0..2,
+ * wise_main.cpp:27-29); the body is at the solve's polar; observer = polar
+ * means seen from the Sun (zero phase).  Like the stage, positions are in
+ * metres (its AU = 149.6e9 m) while the shape keeps its own units;
+ * visibility: [nf][ntau] flags toward the observer (the Visibility stage's
+ * output, e.g. atpm_get_shadow of a solve with the observer as polar and
+ * shadowing 2), or NULL for each facet's own horizon test only; wavelengths
+ * emissivity: the stage's double EPS (wise_main.cpp:13); wavelengths in
+ * micrometres (1..8 of them); flux: [ntau][nwl], Planck radiance times
+ * eps * area * cos(e) / distance^2.  Uses the
+ * solve's current surface temperatures; facet sums run in a fixed order
+ * (deterministic). */
+ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
+                                    double emissivity, int32_t nwl, const double* wavelength_um, double* flux);
 /* FP64 diagnostics of the last revolution: sum over facets and steps of the
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,

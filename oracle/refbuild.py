@@ -39,6 +39,7 @@ OUT_ROOT = HERE / "_ref"
 THERMAL_SRC = "3905/Thermal/NominalPole/main.cpp"
 SELFHEAT_SRC = "3905/Shape_Selfheating/main.cpp"
 VISIB_SRC = "3905/Visibility/NominalPole/main.cpp"
+OBSERVE_SRC = "3905/Observe/NominalPole/wise_main.cpp"
 CRATER_FILES = ["new_crater2.txt", "new_crater2_selfheating_list.txt",
                 "new_crater2_photovectors.txt"]
 CRATER_DIR = "3905/Thermal/NominalPole"
@@ -473,6 +474,61 @@ def build_visibility_refgpu(cfg: dict, cuda_home: str = "/usr/local/cuda") -> Pa
                     "-c", str(cu), "-o", str(obj)], check=True)
     subprocess.run(["g++", *CXXFLAGS, str(src_path), str(obj), "-L", cuda_home + "/lib64", "-lcudart",
                     "-Wl,-rpath," + cuda_home + "/lib64", "-o", str(exe)], check=True)
+    return exe
+
+
+_OBSERVE_HOOK = r'''
+#include <cstdio>
+static void __oracle_dump_flux(const double* smooth) {
+	FILE* fp = fopen("oracle_flux.bin", "ab");
+	fwrite(smooth, sizeof(double), num_wavelengths, fp);
+	fclose(fp);
+}
+'''
+
+
+def patch_observe(cfg: dict) -> str:
+    """The Observe stage with its constants set and the raw smooth flux of
+    every step dumped (binary, before the colour-correction fit)."""
+    src = (REF_ROOT / OBSERVE_SRC).read_text(errors="replace")
+    c = cfg
+    src = _sub_const(src, "ASTNUMVTX", str(c["nv"]))
+    src = _sub_const(src, "ASTNUMFACE", str(c["nf"]))
+    src = _sub_const(src, "NTAU", str(c["ntau"]))
+    src = _sub_const(src, "shape_filename", '"%s"' % c.get("shape", "shape"))
+    for k, name in enumerate(("hel_polar0", "hel_polar1", "hel_polar2")):
+        src = _sub_const(src, name, _d(c["polar"][k]))
+    for k, name in enumerate(("obs_polar0", "obs_polar1", "obs_polar2")):
+        src = _sub_const(src, name, _d(c["observer"][k]))
+    src = _sub_const(src, "rot0", _d(c["rot"][0]))
+    src = _sub_const(src, "rot1", _d(c["rot"][1]))
+    src = _sub_const(src, "minimum_thermal_inertia", str(int(c["ti"])))
+    src = _sub_const(src, "maximum_thermal_inertia", str(int(c["ti"])))
+    i = src.find("void observe(Surface &S, Asteroid &A, string smooth_outname, string rough_outname) {")
+    if i < 0:
+        raise RuntimeError("observe() not found")
+    src = src[:i] + _OBSERVE_HOOK + "\n" + src[i:]
+    src = _insert_after(src, i, "\t\tchisqr_smooth=100.0, chisqr_rough=100.0;", "")
+    j = src.find("\t\tchisqr_smooth=100.0, chisqr_rough=100.0;", i)
+    src = src[:j] + "\t\t__oracle_dump_flux(astsmoothfluxtotal);\n" + src[j:]
+    return src
+
+
+def build_observe(cfg: dict) -> Path:
+    """Reference Observe stage (disk-integrated flux), scratch copy."""
+    full = dict(shape="shape")
+    full.update(cfg)
+    d = OUT_ROOT / _tag("observe", full)
+    exe = d / "observe"
+    src_path = d / "wise_main.cpp"
+    if exe.exists():
+        return exe
+    d.mkdir(parents=True, exist_ok=True)
+    if not src_path.exists():
+        if not (REF_ROOT / OBSERVE_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        src_path.write_text(patch_observe(full))
+    subprocess.run(["g++", *CXXFLAGS, str(src_path), "-o", str(exe)], check=True)
     return exe
 
 
