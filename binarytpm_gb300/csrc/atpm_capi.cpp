@@ -248,6 +248,11 @@ int cond_variant() {
     return 3;
 }
 
+bool shadow_cull_enabled() {
+    const char* e = std::getenv("ATPM_SHADOW_CULL");
+    return !(e && e[0] == '0');
+}
+
 bool tc_enabled() {
     const char* e = std::getenv("ATPM_TC");
     return !(e && e[0] == '0');
@@ -763,8 +768,15 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     cudaError_t e = cudaMemcpyAsync((void*)g.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, s->st);
     int rc = 0;
     if (e == cudaSuccess) rc = launch_geometry(s->ds, g, s->st);
-    if (e == cudaSuccess && !rc && P.shadowing == 1 && s->nnz > 0) rc = launch_shadow_deplist(s->ds, g, s->st);
-    if (e == cudaSuccess && !rc && P.shadowing == 2) rc = launch_shadow_allpairs(s->ds, g, s->st);
+    // shadow drivers: the projected-box cull in front of the exact test (the
+    // same flags); ATPM_SHADOW_CULL=0 runs the plain drivers
+    const bool shadows = (P.shadowing == 1 && s->nnz > 0) || P.shadowing == 2;
+    if (e == cudaSuccess && !rc && shadows) {
+        int cr = shadow_cull_enabled() ? launch_shadow_culled(s->ds, g, P.shadowing == 2, s->st) : -1;
+        if (cr == -1) cr = (P.shadowing == 2) ? launch_shadow_allpairs(s->ds, g, s->st)
+                                              : launch_shadow_deplist(s->ds, g, s->st);
+        rc = cr;
+    }
     cudaFreeAsync(tmp, s->st);
     cudaError_t e2 = cudaStreamSynchronize(s->st);  // `rot` must outlive the copy
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "geometry upload: %s", cudaGetErrorString(e));

@@ -10,6 +10,20 @@
 //                    (3905/Visibility/NominalPole/main.cpp:674-704)
 //   dev_shadowtest   astshadowtest (main.cpp:1187-1247)
 //
+// Culled drivers (same flags, far fewer exact tests): every ray starts at the
+// origin (the Sun, or the observer in the Visibility stage), so the test is
+// two-dimensional in the central projection onto the plane normal to the
+// body's direction.  If the exact test puts the ray's point inside facet h,
+// the projection of g's midpoint lies inside h's projected triangle, hence
+// inside its bounding box: a box test (FP32, padded far beyond the FP64
+// test's rounding) rejects every other pair before the exact FP64 test.
+//   k_proj           projected vertex coordinates of every step
+//   k_shadow_dep_cull the dependent-list driver with the box test in front
+//   k_grid_*         a uniform grid per step over the projected facets
+//                    (one cell per facet, by its box centre; cell size the
+//                    largest box), built by counting sort
+//   k_shadow_grid    the all-pairs driver over the 3 x 3 cells around g
+//
 // Every operation uses round-to-nearest intrinsics in the reference's operand
 // order, with the rotation cos/sin and the pole matrix computed on the host by
 // the same libm the reference uses, so positions, normals and shadow flags
@@ -21,6 +35,9 @@
 // consecutive steps of one facet reads each neighbour's data as one
 // contiguous segment.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
 
 #include "atpm_internal.h"
 
@@ -184,6 +201,285 @@ __global__ void __launch_bounds__(256) k_shadow_all(GeomArgs a) {
         }
     }
     if (valid && !lit) a.s.shadow[o] = 0;
+}
+
+// ------------------------------------------------------------- culled drivers
+struct ProjArgs {
+    double c[3], e1[3], e2[3];  // projection frame: body direction and two normals
+    double scale;               // |body centre|: projected coordinates in km
+    float pad;                  // box padding (km)
+    float2* uv;                 // [nv][ntau]
+    unsigned* stats;            // [0] max |u|,|v| (float bits), [1] max box extent, [2] bad-projection flag
+};
+
+__global__ void __launch_bounds__(256) k_proj(GeomArgs a, ProjArgs p) {
+    const int nv = a.s.nv, ntau = a.s.ntau;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nv * ntau) return;
+    const double* P = a.g.hp + (size_t)i * 3;   // [v][s][3], i = v * ntau + s
+    const double d = P[0] * p.c[0] + P[1] * p.c[1] + P[2] * p.c[2];
+    const double n2 = P[0] * P[0] + P[1] * P[1] + P[2] * P[2];
+    if (!(d > 0.5 * sqrt(n2))) { atomicOr(&p.stats[2], 1u); return; }
+    const double u = (P[0] * p.e1[0] + P[1] * p.e1[1] + P[2] * p.e1[2]) / d * p.scale;
+    const double v = (P[0] * p.e2[0] + P[1] * p.e2[1] + P[2] * p.e2[2]) / d * p.scale;
+    p.uv[i] = make_float2((float)u, (float)v);
+    const float m = fmaxf(fabsf((float)u), fabsf((float)v));
+    atomicMax(&p.stats[0], __float_as_uint(m));
+}
+
+__device__ __forceinline__ float4 facet_box(const GeomArgs& a, const ProjArgs& p, int h, int s) {
+    const int* hv = a.s.fac + 3 * h;
+    const int ntau = a.s.ntau;
+    const float2 q0 = p.uv[(size_t)hv[0] * ntau + s], q1 = p.uv[(size_t)hv[1] * ntau + s],
+                 q2 = p.uv[(size_t)hv[2] * ntau + s];
+    return make_float4(fminf(q0.x, fminf(q1.x, q2.x)) - p.pad, fmaxf(q0.x, fmaxf(q1.x, q2.x)) + p.pad,
+                       fminf(q0.y, fminf(q1.y, q2.y)) - p.pad, fmaxf(q0.y, fmaxf(q1.y, q2.y)) + p.pad);
+}
+
+__device__ __forceinline__ float2 mid_uv(const GeomArgs& a, const ProjArgs& p, int g, int s) {
+    const double* G = a.g.hm + ((size_t)g * a.s.ntau + s) * 3;
+    const double d = G[0] * p.c[0] + G[1] * p.c[1] + G[2] * p.c[2];
+    return make_float2((float)((G[0] * p.e1[0] + G[1] * p.e1[1] + G[2] * p.e1[2]) / d * p.scale),
+                       (float)((G[0] * p.e2[0] + G[1] * p.e2[1] + G[2] * p.e2[2]) / d * p.scale));
+}
+
+__device__ __forceinline__ bool in_box(float2 q, float4 b) {
+    return q.x >= b.x && q.x <= b.y && q.y >= b.z && q.y <= b.w;
+}
+
+// dependent-list shadowing with the box test in front of the exact test
+__global__ void __launch_bounds__(256) k_shadow_dep_cull(GeomArgs a, ProjArgs p) {
+    const int nf = a.s.nf, ntau = a.s.ntau;
+    const int g = blockIdx.y * blockDim.y + threadIdx.y;
+    const int s = blockIdx.x * 32 + threadIdx.x;
+    if (g >= nf) return;
+    const int d0 = a.s.dep_ptr[g], d1 = a.s.dep_ptr[g + 1];
+    if (d0 == d1) return;
+    const bool valid = s < ntau;
+    const size_t o = (size_t)g * ntau + (valid ? s : 0);
+    bool lit = valid && a.s.shadow[o] == 1;
+    const double gd = a.g.dist[o];
+    const float2 q = valid ? mid_uv(a, p, g, s) : make_float2(0.f, 0.f);
+    for (int k = d0; k < d1; ++k) {
+        if (!__any_sync(0xffffffffu, lit)) break;
+        const int h = __ldg(&a.s.dep_idx[k]);
+        if (lit && in_box(q, facet_box(a, p, h, s))) {
+            const double hd = a.g.dist[(size_t)h * ntau + s];
+            if (gd > hd && dev_shadowtest(a, g, h, s) == 0) lit = false;
+        }
+    }
+    if (valid && !lit) a.s.shadow[o] = 0;
+}
+
+struct GridArgs {
+    int G;          // cells per side
+    float cell;     // cell size (km)
+    float origin;   // grid spans [origin, origin + G * cell) on both axes
+    int s0, ns;     // steps of this chunk
+    int* key;       // [ns][nf] cell of each facet
+    int* start;     // [ns][G*G + 1] exclusive scan of the cell counts
+    int* cursor;    // [ns][G*G]
+    int* list;      // [ns][nf] facets by cell
+};
+
+__device__ __forceinline__ int cell_of(const GridArgs& gr, float x) {
+    int c = (int)floorf((x - gr.origin) / gr.cell);
+    return c < 0 ? 0 : (c >= gr.G ? gr.G - 1 : c);
+}
+
+__global__ void __launch_bounds__(256) k_grid_extent(GeomArgs a, ProjArgs p) {
+    const int nf = a.s.nf, ntau = a.s.ntau;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nf * ntau) return;
+    const int f = (int)(i / ntau), s = (int)(i % ntau);
+    const float4 b = facet_box(a, p, f, s);
+    atomicMax(&p.stats[1], __float_as_uint(fmaxf(b.y - b.x, b.w - b.z)));
+}
+
+__global__ void __launch_bounds__(256) k_grid_count(GeomArgs a, ProjArgs p, GridArgs gr) {
+    const int nf = a.s.nf;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nf * gr.ns) return;
+    const int k = (int)(i / nf), f = (int)(i % nf), s = gr.s0 + k;
+    const float4 b = facet_box(a, p, f, s);
+    const int c = cell_of(gr, 0.5f * (b.z + b.w)) * gr.G + cell_of(gr, 0.5f * (b.x + b.y));
+    gr.key[i] = c;
+    atomicAdd(&gr.start[(size_t)k * (gr.G * gr.G + 1) + c + 1], 1);
+}
+
+// in-place inclusive scan of start[k][1..G*G] (so start[k][c] = first slot of cell c)
+__global__ void __launch_bounds__(1024) k_grid_scan(GridArgs gr) {
+    __shared__ int carry;
+    __shared__ int part[1024];
+    const int n = gr.G * gr.G;
+    int* st = gr.start + (size_t)blockIdx.x * (n + 1);
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 1; base <= n; base += 1024) {
+        const int j = base + threadIdx.x;
+        int v = j <= n ? st[j] : 0;
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int w = 1; w < 1024; w <<= 1) {
+            const int t = threadIdx.x >= w ? part[threadIdx.x - w] : 0;
+            __syncthreads();
+            part[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (j <= n) st[j] = part[threadIdx.x] + carry;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += part[1023];
+        __syncthreads();
+    }
+    int* cu = gr.cursor + (size_t)blockIdx.x * n;
+    for (int c = threadIdx.x; c < n; c += 1024) cu[c] = st[c];
+}
+
+__global__ void __launch_bounds__(256) k_grid_fill(GeomArgs a, GridArgs gr) {
+    const int nf = a.s.nf;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nf * gr.ns) return;
+    const int k = (int)(i / nf), f = (int)(i % nf);
+    const int slot = atomicAdd(&gr.cursor[(size_t)k * gr.G * gr.G + gr.key[i]], 1);
+    gr.list[(size_t)k * nf + slot] = f;
+}
+
+// all pairs over the grid: the candidates of g are the facets filed in the
+// 3 x 3 cells around g's projected midpoint (a cell is as wide as the
+// largest box, so every box containing the point is filed there)
+__global__ void __launch_bounds__(256) k_shadow_grid(GeomArgs a, ProjArgs p, GridArgs gr) {
+    const int nf = a.s.nf, ntau = a.s.ntau;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nf * gr.ns) return;
+    const int k = (int)(i / nf), g = (int)(i % nf), s = gr.s0 + k;
+    const size_t o = (size_t)g * ntau + s;
+    if (a.s.shadow[o] != 1) return;
+    const double gd = a.g.dist[o];
+    const float2 q = mid_uv(a, p, g, s);
+    const int cx = cell_of(gr, q.x), cy = cell_of(gr, q.y);
+    const int n = gr.G * gr.G;
+    const int* st = gr.start + (size_t)k * (n + 1);
+    const int* li = gr.list + (size_t)k * nf;
+    for (int y = max(cy - 1, 0); y <= min(cy + 1, gr.G - 1); ++y)
+        for (int x = max(cx - 1, 0); x <= min(cx + 1, gr.G - 1); ++x) {
+            const int c = y * gr.G + x;
+            for (int j = st[c]; j < st[c + 1]; ++j) {
+                const int h = li[j];
+                if (h == g || !in_box(q, facet_box(a, p, h, s))) continue;
+                const double hd = a.g.dist[(size_t)h * ntau + s];
+                const bool g_tested = (g < h) ? (gd > hd) : !(hd > gd);
+                if (g_tested && dev_shadowtest(a, g, h, s) == 0) {
+                    a.s.shadow[o] = 0;
+                    return;
+                }
+            }
+        }
+}
+
+namespace {
+// projection frame of the body direction; returns false when the body is
+// too close to the origin for a central projection (the caller then runs
+// the plain drivers)
+bool make_frame(const GeomWork& g, ProjArgs& p) {
+    const double n = sqrt(g.car[0] * g.car[0] + g.car[1] * g.car[1] + g.car[2] * g.car[2]);
+    if (!(n > 0.0)) return false;
+    for (int k = 0; k < 3; ++k) p.c[k] = g.car[k] / n;
+    // e1: the coordinate axis least aligned with c, made orthogonal
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+        if (fabs(p.c[k]) < fabs(p.c[ax])) ax = k;
+    double t[3] = {0, 0, 0};
+    t[ax] = 1.0;
+    const double dt = t[0] * p.c[0] + t[1] * p.c[1] + t[2] * p.c[2];
+    for (int k = 0; k < 3; ++k) p.e1[k] = t[k] - dt * p.c[k];
+    const double n1 = sqrt(p.e1[0] * p.e1[0] + p.e1[1] * p.e1[1] + p.e1[2] * p.e1[2]);
+    for (int k = 0; k < 3; ++k) p.e1[k] /= n1;
+    p.e2[0] = p.c[1] * p.e1[2] - p.c[2] * p.e1[1];
+    p.e2[1] = p.c[2] * p.e1[0] - p.c[0] * p.e1[2];
+    p.e2[2] = p.c[0] * p.e1[1] - p.c[1] * p.e1[0];
+    p.scale = n;
+    // 1 cm: orders of magnitude beyond the FP64 test's rounding at 1 AU
+    // (3e-8 km) and the float rounding of projected km-scale coordinates
+    p.pad = 1e-5f;
+    return true;
+}
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+// returns 0 when the culled driver ran, -1 when the caller should fall back
+int launch_shadow_culled(const DevSolve& s, const GeomWork& g, bool all_pairs, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    GeomArgs a{s, g};
+    ProjArgs p{};
+    if (!make_frame(g, p)) return -1;
+    const long long nvt = (long long)s.nv * s.ntau, nft = (long long)s.nf * s.ntau;
+    void* mem = nullptr;
+    const size_t b_uv = al256((size_t)nvt * sizeof(float2));
+    if (cudaMallocAsync(&mem, b_uv + 256, st) != cudaSuccess) return 2;
+    p.uv = static_cast<float2*>(mem);
+    p.stats = reinterpret_cast<unsigned*>(static_cast<char*>(mem) + b_uv);
+    cudaMemsetAsync(p.stats, 0, 16, st);
+    k_proj<<<(unsigned)((nvt + 255) / 256), 256, 0, st>>>(a, p);
+    if (all_pairs) k_grid_extent<<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a, p);
+    unsigned stats[3] = {0, 0, 0};
+    if (cudaMemcpyAsync(stats, p.stats, 12, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaFreeAsync(mem, st);
+        return 2;
+    }
+    if (stats[2]) {  // a vertex too far off the body direction: no projection
+        cudaFreeAsync(mem, st);
+        return -1;
+    }
+    int rc = 0;
+    if (!all_pairs) {
+        dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
+        k_shadow_dep_cull<<<grd, blk, 0, st>>>(a, p);
+    } else {
+        float umax, ext;
+        memcpy(&umax, &stats[0], 4);
+        memcpy(&ext, &stats[1], 4);
+        GridArgs gr{};
+        gr.cell = ext * 1.0001f + 1e-6f;
+        gr.origin = -(umax + 2.0f * p.pad) - gr.cell;
+        long long G = (long long)ceilf(2.0f * -gr.origin / gr.cell) + 1;
+        if (G > 2048) {  // a few huge facets: coarser cells, still correct
+            G = 2048;
+            gr.cell = 2.0f * -gr.origin / 2000.0f;
+        }
+        gr.G = (int)G;
+        const size_t n = (size_t)G * G;
+        // steps per chunk: at most ~64 M grid entries at once
+        int sc = (int)std::max<size_t>(1, std::min<size_t>((size_t)s.ntau, (64u << 20) / (n + 1)));
+        const size_t b_key = al256((size_t)sc * s.nf * 4), b_st = al256((size_t)sc * (n + 1) * 4),
+                     b_cu = al256((size_t)sc * n * 4);
+        void* gm = nullptr;
+        if (cudaMallocAsync(&gm, 2 * b_key + b_st + b_cu, st) != cudaSuccess) {
+            cudaFreeAsync(mem, st);
+            return 2;
+        }
+        char* t = static_cast<char*>(gm);
+        gr.key = reinterpret_cast<int*>(t);
+        gr.list = reinterpret_cast<int*>(t + b_key);
+        gr.start = reinterpret_cast<int*>(t + 2 * b_key);
+        gr.cursor = reinterpret_cast<int*>(t + 2 * b_key + b_st);
+        for (int s0 = 0; s0 < s.ntau && !rc; s0 += sc) {
+            gr.s0 = s0;
+            gr.ns = std::min(sc, s.ntau - s0);
+            const long long m = (long long)s.nf * gr.ns;
+            cudaMemsetAsync(gr.start, 0, (size_t)gr.ns * (n + 1) * 4, st);
+            k_grid_count<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(a, p, gr);
+            k_grid_scan<<<gr.ns, 1024, 0, st>>>(gr);
+            k_grid_fill<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(a, gr);
+            k_shadow_grid<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(a, p, gr);
+            if (cudaGetLastError() != cudaSuccess) rc = 2;
+        }
+        cudaFreeAsync(gm, st);
+    }
+    cudaFreeAsync(mem, st);
+    if (cudaGetLastError() != cudaSuccess) rc = 2;
+    return rc;
 }
 
 int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t stv) {

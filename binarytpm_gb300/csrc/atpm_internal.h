@@ -134,6 +134,10 @@ struct GeomWork {
 int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t st);
 int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t st);
 int launch_shadow_allpairs(const DevSolve& s, const GeomWork& g, stream_t st);
+// the same flags with the projected-box cull in front of the exact test
+// (dependent lists, or all pairs over a per-step grid); -1: not applicable
+// (body too close to the origin for a central projection), use the above
+int launch_shadow_culled(const DevSolve& s, const GeomWork& g, bool all_pairs, stream_t st);
 
 // scattering (atpm_scatter.cu)
 int launch_single_scattering(const DevSolve& s, stream_t st);
