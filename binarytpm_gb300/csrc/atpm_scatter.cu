@@ -9,11 +9,16 @@
 //                     from the last sweep) until every |change| <= accuracy;
 //                     one warp per step, lanes fetch 32 list entries at once
 //                     and the two partial sums are accumulated in list order
+//   k_multi_jacobi    FAST precision: Jacobi sweeps of every facet and step at
+//                     once (warp = 32 steps of one facet, as the single
+//                     scattering), iterated to the same accuracy; the fixed
+//                     point is the reference's, the iterates are not
 //   k_forcing_t       [nf][ntau] -> [ntau][nf] for the conduction sweep
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <mutex>
+#include <utility>
 
 #include "../../include/atpm.h"
 #include "atpm_internal.h"
@@ -141,6 +146,47 @@ __global__ void __launch_bounds__(32) k_multi_gs(DevSolve sv, void* work, int ca
     for (int c = lane; c < nf; c += 32) Efm[(size_t)c * ntau + s] = A::div(pn[c], alb);
 }
 
+// one Jacobi sweep: pn = alb (sp + sum_k v_k po[g_k]) for every (facet, step),
+// [nf][ntau] arrays; *more = 1 if some |pn - po| > accuracy
+__global__ void __launch_bounds__(256) k_multi_jacobi(DevSolve sv, const float* sp, const float* po, float* pn,
+                                                      int* more) {
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int f = blockIdx.y * blockDim.y + threadIdx.y;
+    const int s = blockIdx.x * 32 + threadIdx.x;
+    if (f >= nf) return;
+    const bool ok = s < ntau;
+    const int sc = ok ? s : 0;
+    float a0 = 0.0f, a1 = 0.0f;
+    const int k0 = sv.dep_ptr[f], k1 = sv.dep_ptr[f + 1];
+    int k = k0;
+    for (; k + 1 < k1; k += 2) {
+        a0 += __ldg(&sv.dep_vf[k]) * po[(size_t)__ldg(&sv.dep_idx[k]) * ntau + sc];
+        a1 += __ldg(&sv.dep_vf[k + 1]) * po[(size_t)__ldg(&sv.dep_idx[k + 1]) * ntau + sc];
+    }
+    if (k < k1) a0 += __ldg(&sv.dep_vf[k]) * po[(size_t)__ldg(&sv.dep_idx[k]) * ntau + sc];
+    if (!ok) return;
+    const size_t o = (size_t)f * ntau + s;
+    const float v = sv.alb * (sp[o] + (a0 + a1));
+    pn[o] = v;
+    if (fabsf(v - po[o]) > sv.sacc) *more = 1;
+}
+
+__global__ void k_status_or(int* status, int bits) { atomicOr(status, bits); }
+
+__global__ void __launch_bounds__(256) k_multi_jacobi_init(DevSolve sv, float* sp, float* po) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)sv.nf * sv.ntau) return;
+    const float* cs = static_cast<const float*>(sv.cosil);
+    sp[i] = sv.solar * cs[i] * (float)sv.shadow[i];
+    po[i] = sv.alb * static_cast<const float*>(sv.Efm)[i];
+}
+
+__global__ void __launch_bounds__(256) k_multi_jacobi_out(DevSolve sv, const float* p) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)sv.nf * sv.ntau) return;
+    static_cast<float*>(sv.Efm)[i] = p[i] / sv.alb;
+}
+
 // [nf][ntau] -> [ntau][nf]
 template <class R>
 __global__ void __launch_bounds__(256) k_forcing_t(const R* src, R* dst, int nf, int ntau) {
@@ -180,12 +226,43 @@ int launch_single_scattering(const DevSolve& s, stream_t stv) {
 
 size_t multiple_scattering_work_bytes(const DevSolve& s) {
     const size_t rs = (s.mode == MODE_FP64) ? 8 : 4;
-    return 3 * (size_t)s.ntau * s.nf * rs;
+    return 3 * (size_t)s.ntau * s.nf * rs + 256;
 }
+
+namespace {
+// FAST: Jacobi sweeps until no (facet, step) changes by more than the
+// accuracy; one 4-byte read-back per sweep
+int multiple_scattering_jacobi(const DevSolve& s, void* work, cudaStream_t st, int cap) {
+    const size_t n = (size_t)s.nf * s.ntau;
+    float* sp = static_cast<float*>(work);
+    float* pa = sp + n;
+    float* pb = pa + n;
+    int* more = reinterpret_cast<int*>(pb + n);
+    const int g1 = (int)((n + 255) / 256);
+    k_multi_jacobi_init<<<g1, 256, 0, st>>>(s, sp, pa);
+    dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
+    for (int it = 0;; ++it) {
+        if (it == cap) {
+            k_status_or<<<1, 1, 0, st>>>(s.status, ST_SCATTER_CAP);
+            break;
+        }
+        cudaMemsetAsync(more, 0, 4, st);
+        k_multi_jacobi<<<grd, blk, 0, st>>>(s, sp, pa, pb, more);
+        int m = 0;
+        if (cudaMemcpyAsync(&m, more, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return 2;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
+        std::swap(pa, pb);
+        if (!m) break;
+    }
+    k_multi_jacobi_out<<<g1, 256, 0, st>>>(s, pa);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+}  // namespace
 
 int launch_multiple_scattering(const DevSolve& s, void* work, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const int cap = 1000;  // the reference iterates unbounded; real cases need < 50 sweeps
+    if (s.mode == MODE_FAST) return multiple_scattering_jacobi(s, work, st, cap);
     switch (s.mode) {
         case MODE_REF: k_multi_gs<MODE_REF><<<s.ntau, 32, 0, st>>>(s, work, cap); break;
         case MODE_FP64: k_multi_gs<MODE_FP64><<<s.ntau, 32, 0, st>>>(s, work, cap); break;

@@ -100,3 +100,21 @@ def test_viewfactors_match_reference_lists(gpu_ctx, name):
     # handful of values across a rounding boundary of the printed digits
     assert np.quantile(rel, 0.999) < 5e-6, np.quantile(rel, 0.999)
     assert rel.max() < 1e-4, rel.max()
+
+
+@pytest.mark.parametrize("name", ["single_s2", "binary_s3s1"])
+def test_fast_scattering_within_accuracy(gpu_ctx, name):
+    """FAST multiple scattering (Jacobi over every step at once) converges to
+    the reference's fixed point: within the scattering accuracy (1e-4 W/m^2
+    on albedo x E, i.e. 5e-3 W/m^2 on E at albedo 0.02) plus float rounding of
+    the reference's Gauss-Seidel result."""
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden(name)
+    s = _solve(gpu_ctx, prob, lib.FAST)
+    s.geometry_shadow()
+    s.scattering()
+    e = s.illumination()
+    assert np.array_equal(s.shadow(), ref["shadow"])
+    d = np.abs(e - ref["illumination"])
+    assert np.max(d) <= 2 * 1e-4 / prob.albedo + 1e-6 * np.max(np.abs(ref["illumination"])), np.max(d)
