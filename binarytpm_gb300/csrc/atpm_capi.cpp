@@ -258,14 +258,6 @@ bool tc_enabled() {
     return !(e && e[0] == '0');
 }
 
-uint16_t f2bf(float x) {
-    uint32_t u;
-    std::memcpy(&u, &x, 4);
-    if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
-    u += 0x7fffu + ((u >> 16) & 1u);
-    return (uint16_t)(u >> 16);
-}
-
 // step chunking of the tensor-core product: equal chunks of N <= tc_max_chunk()
 // steps, N a multiple of 16 (720 steps -> 5 chunks of 144)
 void tc_chunks(int ntau, int* n, int* nch) {
@@ -287,74 +279,59 @@ void build_tc_maps(int nf, int ntau, int solve, std::vector<int4>& q) {
 
 // block-sparse BF16 tiles of the view-factor matrix (128 x 64, swizzled)
 atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
+    // tile structure on the host (one pass over the lists): which 64-facet
+    // column blocks each 128-facet row block touches, the largest view factor
+    // of each tile; the BF16 values are filled on the device (k_tc_fill) from
+    // the lists already uploaded
     const int nf = s->nf, ntau = s->P.ntau;
     const int nmb = (nf + 127) / 128, nkb = (nf + 63) / 64;
     int N, nch;
     tc_chunks(ntau, &N, &nch);
-    std::vector<std::vector<int>> cols(nmb);
-    for (int f = 0; f < nf; ++f)
-        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) cols[f / 128].push_back(sh->dep_idx[k] / 64);
-    std::vector<int> tptr(nmb + 1, 0), tcol;
-    std::vector<std::vector<int>> slot(nmb);
+    const size_t ncell = (size_t)nmb * nkb;
+    std::vector<float> vm(ncell, -1.0f);
+    for (int f = 0; f < nf; ++f) {
+        float* row = vm.data() + (size_t)(f / 128) * nkb;
+        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
+            float& c = row[sh->dep_idx[k] / 64];
+            c = std::max(c, std::fabs(sh->dep_vf[k]));
+        }
+    }
+    std::vector<int> tptr(nmb + 1, 0), tcol, slot(ncell, -1), lo_of;
+    int nlo = 0;
     for (int mb = 0; mb < nmb; ++mb) {
-        auto& c = cols[mb];
-        std::sort(c.begin(), c.end());
-        c.erase(std::unique(c.begin(), c.end()), c.end());
-        tptr[mb + 1] = tptr[mb] + (int)c.size();
-        tcol.insert(tcol.end(), c.begin(), c.end());
+        for (int kb = 0; kb < nkb; ++kb) {
+            const float v = vm[(size_t)mb * nkb + kb];
+            if (v < 0.0f) continue;
+            slot[(size_t)mb * nkb + kb] = (int)tcol.size();
+            tcol.push_back(kb);
+            // residual tile V - bf16(V) where the tile holds a view factor >= 1e-4
+            lo_of.push_back(v >= 1e-4f ? nlo++ : -1);
+        }
+        tptr[mb + 1] = (int)tcol.size();
     }
     const size_t ntiles = tcol.size();
     const size_t tile_el = 128 * 64;
-    std::vector<uint16_t> tiles(std::max<size_t>(ntiles, 1) * tile_el, 0);
-    std::vector<float> vmax(std::max<size_t>(ntiles, 1), 0.0f);
-    for (int mb = 0; mb < nmb; ++mb) {
-        const int t0 = tptr[mb];
-        const auto& c = cols[mb];
-        for (int f = mb * 128; f < std::min(nf, (mb + 1) * 128); ++f)
-            for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
-                const int g = sh->dep_idx[k];
-                const int t = t0 + (int)(std::lower_bound(c.begin(), c.end(), g / 64) - c.begin());
-                uint16_t& e = tiles[(size_t)t * tile_el + tc_swizzle_offset((uint32_t)(f % 128), (uint32_t)(g % 64))];
-                e = f2bf(sh->dep_vf[k]);
-                vmax[t] = std::max(vmax[t], std::fabs(sh->dep_vf[k]));
-            }
-    }
-    // residual tiles V - bf16(V) where a tile holds a view factor >= 1e-4
-    std::vector<int> lo_of(std::max<size_t>(ntiles, 1), -1);
-    int nlo = 0;
-    for (size_t t = 0; t < ntiles; ++t)
-        if (vmax[t] >= 1e-4f) lo_of[t] = nlo++;
-    std::vector<uint16_t> lo_tiles(std::max(nlo, 1) * tile_el, 0);
-    for (int mb = 0; mb < nmb; ++mb) {
-        const int t0 = tptr[mb];
-        const auto& c = cols[mb];
-        for (int f = mb * 128; f < std::min(nf, (mb + 1) * 128); ++f)
-            for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
-                const int g = sh->dep_idx[k];
-                const int t = t0 + (int)(std::lower_bound(c.begin(), c.end(), g / 64) - c.begin());
-                if (lo_of[t] < 0) continue;
-                const uint16_t hb = f2bf(sh->dep_vf[k]);
-                uint32_t hu = (uint32_t)hb << 16;
-                float hf;
-                std::memcpy(&hf, &hu, 4);
-                lo_tiles[(size_t)lo_of[t] * tile_el + tc_swizzle_offset((uint32_t)(f % 128), (uint32_t)(g % 64))] =
-                    f2bf(sh->dep_vf[k] - hf);
-            }
-    }
-    const size_t b_tiles = align256(tiles.size() * 2);
+    if (lo_of.empty()) lo_of.push_back(-1);
+    const size_t b_tiles = align256(std::max<size_t>(ntiles, 1) * tile_el * 2);
     const size_t b_ptr = align256((nmb + 1) * 4), b_col = align256(std::max<size_t>(ntiles, 1) * 4);
     const size_t b_w = align256((size_t)nkb * nch * N * 64 * 2 * 2);
-    const size_t b_lo = align256(lo_tiles.size() * 2), b_loi = align256(lo_of.size() * 4);
+    const size_t b_lo = align256((size_t)std::max(nlo, 1) * tile_el * 2), b_loi = align256(lo_of.size() * 4);
+    const size_t b_slot = align256(ncell * 4);
     char* m = nullptr;
-    CK(cudaMalloc((void**)&m, b_tiles + b_ptr + b_col + b_w + b_lo + b_loi));
+    CK(cudaMalloc((void**)&m, b_tiles + b_ptr + b_col + b_w + b_lo + b_loi + b_slot));
     s->tc_mem = m;
     char* p_lo = m + b_tiles + b_ptr + b_col + b_w;
-    CK(cudaMemcpy(m, tiles.data(), tiles.size() * 2, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(m + b_tiles, tptr.data(), (nmb + 1) * 4, cudaMemcpyHostToDevice));
-    if (ntiles) CK(cudaMemcpy(m + b_tiles + b_ptr, tcol.data(), ntiles * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemset(m + b_tiles + b_ptr + b_col, 0, b_w));
-    CK(cudaMemcpy(p_lo, lo_tiles.data(), lo_tiles.size() * 2, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice));
+    int* d_slot = reinterpret_cast<int*>(p_lo + b_lo + b_loi);
+    CK(cudaMemsetAsync(m, 0, b_tiles, s->st));
+    CK(cudaMemcpyAsync(m + b_tiles, tptr.data(), (nmb + 1) * 4, cudaMemcpyHostToDevice, s->st));
+    if (ntiles) CK(cudaMemcpyAsync(m + b_tiles + b_ptr, tcol.data(), ntiles * 4, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemsetAsync(m + b_tiles + b_ptr + b_col, 0, b_w, s->st));
+    CK(cudaMemsetAsync(p_lo, 0, b_lo, s->st));
+    CK(cudaMemcpyAsync(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice, s->st));
+    CK(cudaMemcpyAsync(d_slot, slot.data(), ncell * 4, cudaMemcpyHostToDevice, s->st));
+    if (launch_tc_fill(s->ds, nkb, d_slot, reinterpret_cast<const int*>(p_lo + b_lo), m, p_lo, s->st))
+        return fail(ATPM_E_CUDA, "tile fill launch: %s", cudaGetErrorString(cudaGetLastError()));
+    CK(cudaStreamSynchronize(s->st));  // the host tables must outlive their copies
     DevSolve& d = s->ds;
     d.tc_tiles = m;
     d.tc_ptr = reinterpret_cast<const int*>(m + b_tiles);
@@ -478,15 +455,19 @@ atpm_status check_status(atpm_solve* s, int st) {
 namespace {
 template <class R>
 atpm_status get_transposed(atpm_solve* s, const void* dev, size_t rows, size_t cols, float* out, double* out64) {
-    // dev is [rows][cols]; out is [cols][rows]
-    std::vector<R> h(rows * cols);
-    CK(cudaMemcpyAsync(h.data(), dev, h.size() * sizeof(R), cudaMemcpyDeviceToHost, s->st));
-    CK(cudaStreamSynchronize(s->st));
-    for (size_t i = 0; i < rows; ++i)
-        for (size_t j = 0; j < cols; ++j) {
-            if (out) out[j * rows + i] = (float)h[i * cols + j];
-            if (out64) out64[j * rows + i] = (double)h[i * cols + j];
-        }
+    // dev is [rows][cols]; out is [cols][rows]: transposed (and converted) on
+    // the device, one copy into the caller's buffer
+    void* host = out ? static_cast<void*>(out) : static_cast<void*>(out64);
+    const int ob = out ? 4 : 8;
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, rows * cols * ob, s->st));
+    cudaError_t e = cudaSuccess;
+    if (launch_transpose(dev, (int)sizeof(R), tmp, ob, rows, cols, s->st)) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, rows * cols * ob, cudaMemcpyDeviceToHost, s->st);
+    cudaFreeAsync(tmp, s->st);
+    cudaError_t e2 = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "transpose/copy: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "transpose/copy: %s", cudaGetErrorString(e2));
     return ATPM_OK;
 }
 }  // namespace

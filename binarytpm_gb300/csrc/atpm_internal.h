@@ -145,6 +145,8 @@ int launch_multiple_scattering(const DevSolve& s, void* work, stream_t st);
 size_t multiple_scattering_work_bytes(const DevSolve& s);
 int launch_forcing_transpose(const DevSolve& s, stream_t st);
 int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* illum_d, stream_t st);
+// [rows][cols] -> [cols][rows], element sizes 4 or 8 bytes (float / double)
+int launch_transpose(const void* src, int src_bytes, void* dst, int dst_bytes, size_t rows, size_t cols, stream_t st);
 
 // thermal (atpm_thermal.cu); batched over `n` solves in `tab` (device array)
 struct Batch {
@@ -163,6 +165,11 @@ struct Batch {
     int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
 };
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
+// BF16 view-factor tiles (and residual tiles) of a solve from its uploaded
+// lists: slot[mb * nkb + kb] = tile of (row block, column block), lo_of[t] =
+// residual tile of tile t or -1; tiles must be zeroed (atpm_spmm_tc.cu)
+int launch_tc_fill(const DevSolve& s, int nkb, const int* slot, const int* lo_of, void* tiles, void* lo_tiles,
+                   stream_t st);
 // part 0 W, 1 Q, 2 conduction, 3 convergence, 4 advance
 int launch_revolution_part(const Batch& b, int part, stream_t st);
 int launch_initial_mean(const DevSolve& s, void* mean_out, stream_t st);

@@ -203,6 +203,22 @@ __global__ void __launch_bounds__(256) k_forcing_t(const R* src, R* dst, int nf,
     }
 }
 
+// [rows][cols] -> [cols][rows] with a type conversion, 32 x 32 tiles
+template <class Ri, class Ro>
+__global__ void __launch_bounds__(256) k_transpose(const Ri* src, Ro* dst, size_t rows, size_t cols) {
+    __shared__ Ri sm[32][33];
+    const size_t r0 = (size_t)blockIdx.y * 32, c0 = (size_t)blockIdx.x * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const size_t r = r0 + j, c = c0 + threadIdx.x;
+        sm[j][threadIdx.x] = (r < rows && c < cols) ? src[r * cols + c] : Ri(0);
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const size_t c = c0 + j, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) dst[c * rows + r] = (Ro)sm[threadIdx.x][j];
+    }
+}
+
 template <class R>
 __global__ void k_set_forcing(DevSolve sv, const int32_t* shadow, const float* illum) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -278,6 +294,23 @@ int launch_forcing_transpose(const DevSolve& s, stream_t stv) {
         k_forcing_t<double><<<grd, blk, 0, st>>>(static_cast<const double*>(s.Efm), static_cast<double*>(s.E), s.nf, s.ntau);
     else
         k_forcing_t<float><<<grd, blk, 0, st>>>(static_cast<const float*>(s.Efm), static_cast<float*>(s.E), s.nf, s.ntau);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_transpose(const void* src, int src_bytes, void* dst, int dst_bytes, size_t rows, size_t cols,
+                     stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    dim3 blk(32, 8), grd((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    if (src_bytes == 4 && dst_bytes == 4)
+        k_transpose<float, float><<<grd, blk, 0, st>>>(static_cast<const float*>(src), static_cast<float*>(dst), rows, cols);
+    else if (src_bytes == 8 && dst_bytes == 8)
+        k_transpose<double, double><<<grd, blk, 0, st>>>(static_cast<const double*>(src), static_cast<double*>(dst), rows, cols);
+    else if (src_bytes == 4 && dst_bytes == 8)
+        k_transpose<float, double><<<grd, blk, 0, st>>>(static_cast<const float*>(src), static_cast<double*>(dst), rows, cols);
+    else if (src_bytes == 8 && dst_bytes == 4)
+        k_transpose<double, float><<<grd, blk, 0, st>>>(static_cast<const double*>(src), static_cast<float*>(dst), rows, cols);
+    else
+        return 1;
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

@@ -154,6 +154,44 @@ __host__ __device__ inline int tc_stages(int N) {
 uint32_t tc_swizzle_offset(uint32_t row, uint32_t k) { return swz(row, k); }
 int tc_max_chunk() { return 160; }
 
+// float -> BF16, round to nearest even (quiet NaN for NaN), as the host's f2bf
+__device__ __forceinline__ uint16_t bf16_rne(float x) {
+    uint32_t u = __float_as_uint(x);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+// one warp per facet row: every list entry goes to its swizzled slot of its
+// (row block, column block) tile, plus the BF16 residual where the tile has one
+__global__ void __launch_bounds__(256) k_tc_fill(DevSolve s, int nkb, const int* slot, const int* lo_of,
+                                                 uint16_t* tiles, uint16_t* lo_tiles) {
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (f >= s.nf) return;
+    const int* srow = slot + (size_t)(f >> 7) * nkb;
+    const uint32_t row = (uint32_t)(f & 127);
+    for (int k = s.dep_ptr[f] + lane; k < s.dep_ptr[f + 1]; k += 32) {
+        const int g = s.dep_idx[k];
+        const float v = s.dep_vf[k];
+        const int t = srow[g >> 6];
+        const uint32_t off = swz(row, (uint32_t)(g & 63));
+        const uint16_t hb = bf16_rne(v);
+        tiles[(size_t)t * (TC_M * TC_K) + off] = hb;
+        const int l = lo_of[t];
+        if (l >= 0) lo_tiles[(size_t)l * (TC_M * TC_K) + off] = bf16_rne(__fsub_rn(v, __uint_as_float((uint32_t)hb << 16)));
+    }
+}
+
+int launch_tc_fill(const DevSolve& s, int nkb, const int* slot, const int* lo_of, void* tiles, void* lo_tiles,
+                   stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t threads = (size_t)s.nf * 32;
+    k_tc_fill<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, lo_of, static_cast<uint16_t*>(tiles),
+                                                                   static_cast<uint16_t*>(lo_tiles));
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 // W = eps sigma T^4 in BF16, written as (column block, step chunk) tiles
 __global__ void __launch_bounds__(256) k_w_bf16(Batch b) {
     const int4 t = b.wmap[blockIdx.x];
