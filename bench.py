@@ -294,6 +294,11 @@ def main():
     value = fsteps_all / (dev_ms_max / 1e3)
     wall_value = fsteps_all / _max_over_ranks(wall, dist, dev)
 
+    cond_v, tc_depth, _ = s0.last_run_config()
+    launch_config = {"conduction_variant": cond_v, "tc_pipeline_depth": tc_depth,
+                     "chosen_by": "autotuner: the first batch of this kind (a warm-up step) timed the candidates "
+                                  "on its first 3 revolutions; results do not depend on the choice"}
+
     # per-kernel durations of one instrumented revolution of the same batch
     kern = lib.profile_revolution(solves)
 
@@ -353,6 +358,7 @@ def main():
         "serving": serve,
         "roofline": roof,
         "kernels_ms": kern,
+        "launch_config": launch_config,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),

@@ -248,6 +248,11 @@ int cond_variant() {
     return 3;
 }
 
+bool autotune_enabled() {
+    const char* e = std::getenv("ATPM_AUTOTUNE");
+    return !(e && e[0] == '0');
+}
+
 bool shadow_cull_enabled() {
     const char* e = std::getenv("ATPM_SHADOW_CULL");
     return !(e && e[0] == '0');
@@ -369,6 +374,7 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.nq = 0;
     b.tc_nmax = 0;
     b.cond_variant = cond_variant();
+    b.tc_stages = 0;
     return b;
 }
 
@@ -428,6 +434,89 @@ atpm_status capture_graph(atpm_solve* s, const Batch& b, cudaGraphExec_t* out) {
     e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    return ATPM_OK;
+}
+
+// Autotuner for FAST batches.  Its knobs change launch configurations only,
+// never results: the conduction kernel's register/occupancy variant
+// (k_conduction<FAST, NX, 1|2|3>: one source, three register budgets) and
+// the tensor-core pipeline depth.  The first time a kind of batch (precision,
+// NX, step chunk, size class) runs, its first three revolutions -- real
+// revolutions of the solve, each a different candidate -- are timed part by
+// part with events; the fastest conduction variant and pipeline depth are
+// kept in the context for every later batch of that kind.
+uint64_t tune_key(const Batch& b) {
+    int cls = 0;
+    while ((1 << cls) < b.nfb && cls < 40) ++cls;  // facet blocks, power-of-two class
+    return (uint64_t)b.mode | ((uint64_t)b.nx << 4) | ((uint64_t)b.tc_nmax << 12) | ((uint64_t)cls << 24) |
+           ((uint64_t)(b.nq > 0) << 32);
+}
+
+atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64_t* launches, int* tuned) {
+    atpm_context* c = s0->ctx;
+    const uint64_t key = tune_key(b);
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        auto it = c->tune.find(key);
+        if (it != c->tune.end()) {
+            b.cond_variant = it->second.cond_variant;
+            b.tc_stages = it->second.tc_stages;
+            return ATPM_OK;
+        }
+    }
+    atpm_tune_choice ch;
+    const int smax = b.nq > 0 ? tc_max_stages(b.tc_nmax) : 0;
+    if (maxcap < 3) {  // too short to time: defaults
+        b.cond_variant = 3;
+        b.tc_stages = 0;
+        return ATPM_OK;
+    }
+    // candidates per revolution: conduction variant v, pipeline depth d
+    const int cand_v[3] = {1, 2, 3};
+    const int cand_d[3] = {smax, smax > 2 ? smax - 1 : smax, smax};
+    cudaEvent_t ev[12];
+    for (int i = 0; i < 12; ++i) CK(cudaEventCreate(&ev[i]));
+    int rc = 0;
+    for (int r = 0; r < 3 && !rc; ++r) {
+        b.cond_variant = cand_v[r];
+        b.tc_stages = cand_d[r];
+        rc |= launch_revolution_part(b, 0, s0->st);
+        cudaEventRecord(ev[4 * r], s0->st);
+        rc |= launch_revolution_part(b, 1, s0->st);
+        cudaEventRecord(ev[4 * r + 1], s0->st);
+        rc |= launch_revolution_part(b, 2, s0->st);
+        cudaEventRecord(ev[4 * r + 2], s0->st);
+        rc |= launch_revolution_part(b, 3, s0->st);
+        rc |= launch_revolution_part(b, 4, s0->st);
+        cudaEventRecord(ev[4 * r + 3], s0->st);
+    }
+    cudaError_t e = cudaStreamSynchronize(s0->st);
+    float tc[3] = {0, 0, 0}, cd[3] = {0, 0, 0};
+    for (int r = 0; r < 3 && e == cudaSuccess && !rc; ++r) {
+        cudaEventElapsedTime(&tc[r], ev[4 * r], ev[4 * r + 1]);
+        cudaEventElapsedTime(&cd[r], ev[4 * r + 1], ev[4 * r + 2]);
+    }
+    for (int i = 0; i < 12; ++i) cudaEventDestroy(ev[i]);
+    if (rc) return fail(ATPM_E_CUDA, "revolution launch (autotune): %s", cudaGetErrorString(cudaGetLastError()));
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "autotune: %s", cudaGetErrorString(e));
+    int best = 0;
+    for (int r = 1; r < 3; ++r)
+        if (cd[r] < cd[best]) best = r;
+    ch.cond_variant = cand_v[best];
+    // depth smax ran in revolutions 0 and 2, smax - 1 in revolution 1
+    ch.tc_stages = (smax > 2 && tc[1] < 0.5f * (tc[0] + tc[2])) ? smax - 1 : 0;
+    for (int r = 0; r < 3; ++r) ch.cond_ms[r] = cd[r];
+    ch.tc_ms[0] = 0.5f * (tc[0] + tc[2]);
+    ch.tc_ms[1] = tc[1];
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        c->tune[key] = ch;
+    }
+    b.cond_variant = ch.cond_variant;
+    b.tc_stages = ch.tc_stages;
+    *done_revs = 3;
+    *launches += 3 * (b.nw > 0 || b.nq > 0 ? 5 : 3);
+    *tuned = 1;
     return ATPM_OK;
 }
 
@@ -895,16 +984,28 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     void* tmp = nullptr;
     atpm_status rb = make_batch_for(solves, n, &b, &tmp);
     if (rb) return rb;
-    cudaGraphExec_t gx = nullptr;
-    atpm_status r = capture_graph(s0, b, &gx);
-    if (r) { if (tmp) cudaFree(tmp); return r; }
     int maxcap = 0;
     for (int i = 0; i < n; ++i) maxcap = std::max(maxcap, solves[i]->P.revcap);
     std::vector<Ctl> ctl(n);
     int done_revs = 0;
     int chunk = 4;
-    cudaError_t e = cudaEventRecord(s0->ev0, s0->st);
     int64_t launches = 0;
+    // the timed region starts before any revolution, tuning ones included
+    cudaError_t e = cudaEventRecord(s0->ev0, s0->st);
+    int tuned = 0;
+    if (e == cudaSuccess && b.mode == MODE_FAST) {
+        const bool ok = autotune_enabled();
+        if (!ok) {
+            b.cond_variant = cond_variant();
+            b.tc_stages = 0;
+        } else {
+            atpm_status rt = autotune(s0, b, maxcap, &done_revs, &launches, &tuned);
+            if (rt) { if (tmp) cudaFree(tmp); return rt; }
+        }
+    }
+    cudaGraphExec_t gx = nullptr;
+    atpm_status r = capture_graph(s0, b, &gx);
+    if (r) { if (tmp) cudaFree(tmp); return r; }
     while (e == cudaSuccess && done_revs < maxcap) {
         const int k = std::min(chunk, maxcap - done_revs);
         for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaGraphLaunch(gx, s0->st);
@@ -946,6 +1047,9 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     s0->last_ms = ms;
     s0->last_launches = launches;
     s0->last_facet_steps = fsteps_total;
+    s0->last_cond_variant = b.cond_variant;
+    s0->last_tc_stages = b.nq > 0 ? (b.tc_stages > 0 ? b.tc_stages : tc_max_stages(b.tc_nmax)) : 0;
+    s0->last_tuned = tuned;
     return worst;
 }
 
@@ -1192,6 +1296,15 @@ ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q) {
     } else {
         CK(cudaMemcpy(q, s->ds.Q, nt * 4, cudaMemcpyDeviceToHost));
     }
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_last_run_config(atpm_solve* s, int32_t* cond_variant, int32_t* tc_stages,
+                                          int32_t* tuned) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (cond_variant) *cond_variant = s->last_cond_variant;
+    if (tc_stages) *tc_stages = s->last_tc_stages;
+    if (tuned) *tuned = s->last_tuned;
     return ATPM_OK;
 }
 

@@ -4,11 +4,20 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <vector>
 
 #include "../../include/atpm.h"
 #include "atpm_internal.h"
+
+// launch configuration chosen by the autotuner for one kind of batch
+struct atpm_tune_choice {
+    int cond_variant = 3;  // FAST conduction register/occupancy variant
+    int tc_stages = 0;     // tensor-core pipeline depth (0: deepest)
+    float cond_ms[3] = {0, 0, 0};
+    float tc_ms[2] = {0, 0};
+};
 
 struct atpm_context {
     int device = 0;
@@ -16,6 +25,7 @@ struct atpm_context {
     bool tables = false;
     atpm::HostPowTab p4, p3;
     atpm::HostPowTab pq;  // x^0.25, built on first need
+    std::map<uint64_t, atpm_tune_choice> tune;  // by batch kind
 };
 
 struct atpm_solve {
@@ -42,6 +52,7 @@ struct atpm_solve {
     float ti = 0.0f;
     double last_ms = 0.0;
     int64_t last_launches = 0, last_facet_steps = 0;
+    int last_cond_variant = 0, last_tc_stages = 0, last_tuned = 0;  // configuration of the last batch run
     int last_nrev = 0;
 };
 

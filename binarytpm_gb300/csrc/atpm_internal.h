@@ -163,7 +163,10 @@ struct Batch {
     int nq;
     int tc_nmax;             // largest step chunk in the batch
     int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
+    int tc_stages;           // tensor-core pipeline depth (0: deepest that fits)
 };
+// deepest tensor-core pipeline that fits shared memory for step chunk N
+int tc_max_stages(int N);
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
 // BF16 view-factor tiles (and residual tiles) of a solve from its uploaded
 // lists: slot[mb * nkb + kb] = tile of (row block, column block), lo_of[t] =
@@ -199,7 +202,7 @@ int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t st);
 int launch_w_bf16(const Batch& b, stream_t st);
 int launch_w_bf16_one(const DevSolve& s, stream_t st);
 int launch_spmm_tc(const Batch& b, stream_t st);
-size_t spmm_tc_smem_bytes(int N);
+size_t spmm_tc_smem_bytes(int N, int stages = 0);  // 0: deepest ring that fits
 uint32_t tc_swizzle_offset(uint32_t row, uint32_t k);
 int tc_max_chunk();  // largest step chunk N of the tensor-core product
 bool conduction_nx_supported(int nx);

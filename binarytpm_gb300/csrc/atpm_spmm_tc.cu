@@ -244,7 +244,16 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
     const uint32_t a_bytes = TC_M * TC_K * 2;
     const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;  // hi + lo
     const uint32_t stage_bytes = (2 * a_bytes + b_bytes + 1023) & ~1023u;
-    const int S = tc_stages(N);
+    // ring depth: the requested one, never more than this chunk size allows
+    // nor than the launch's dynamic shared memory holds (solves of one batch
+    // may use different chunk sizes)
+    int S = (b.tc_stages > 0 && b.tc_stages < tc_stages(N)) ? b.tc_stages : tc_stages(N);
+    {
+        uint32_t dsz;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsz));
+        const int fit = (int)((dsz - 1024u) / stage_bytes);
+        if (S > fit) S = fit;
+    }
     const uint32_t ncols = (N <= 32) ? 32 : (N <= 64) ? 64 : (N <= 128) ? 128 : 256;
     if (warp == 0) {
         tc_alloc(&tmem_base, ncols);
@@ -330,15 +339,18 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
     if (warp == 0) tc_dealloc(tmem, ncols);
 }
 
-size_t spmm_tc_smem_bytes(int N) {
+size_t spmm_tc_smem_bytes(int N, int stages) {
     const size_t a = TC_M * TC_K * 2 * 2, bb = (size_t)N * TC_K * 2 * 2;
-    return (size_t)tc_stages(N) * ((a + bb + 1023) & ~(size_t)1023) + 1024;
+    const int S = (stages > 0 && stages < tc_stages(N)) ? stages : tc_stages(N);
+    return (size_t)S * ((a + bb + 1023) & ~(size_t)1023) + 1024;
 }
+
+int tc_max_stages(int N) { return tc_stages(N); }
 
 int launch_spmm_tc(const Batch& b, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     if (b.nq == 0) return 0;
-    const size_t smem = spmm_tc_smem_bytes(b.tc_nmax);
+    const size_t smem = spmm_tc_smem_bytes(b.tc_nmax, b.tc_stages);
     static int attr_dev = -1;
     int dev = 0;
     cudaGetDevice(&dev);

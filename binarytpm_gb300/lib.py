@@ -68,6 +68,7 @@ _SIGS = {
     "atpm_disk_flux": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p,
                                  C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_last_run_config": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -298,6 +299,13 @@ class Solve:
         a, e, m = C.c_double(), C.c_double(), C.c_double()
         _ck(load().atpm_energy_balance(self.h, C.byref(a), C.byref(e), C.byref(m)))
         return a.value, e.value, m.value
+
+    def last_run_config(self):
+        """(conduction variant, tensor-core pipeline depth, tuned-this-run) of
+        the last batch this solve led."""
+        v, d, t = C.c_int32(), C.c_int32(), C.c_int32()
+        _ck(load().atpm_last_run_config(self.h, C.byref(v), C.byref(d), C.byref(t)))
+        return v.value, d.value, bool(t.value)
 
     def last_run_stats(self):
         ms, la, fs = C.c_double(), C.c_int64(), C.c_int64()

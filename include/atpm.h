@@ -180,6 +180,12 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,
                                          double* mean_temperature);
+/* Launch configuration of the last atpm_batch_run led by s (FAST): the
+ * conduction register/occupancy variant (1-3), the tensor-core pipeline
+ * depth, and whether that run timed the candidates (the autotuner does so
+ * on the first three revolutions of the first batch of each kind; its
+ * choices never change results).  ATPM_AUTOTUNE=0 turns it off. */
+ATPM_API atpm_status atpm_last_run_config(atpm_solve* s, int32_t* cond_variant, int32_t* tc_stages, int32_t* tuned);
 /* Device time (ms, CUDA events on the solve's stream) of the last atpm_run /
  * atpm_batch_run revolution loop, and launches issued inside it. */
 ATPM_API atpm_status atpm_last_run_stats(atpm_solve* s, double* device_ms, int64_t* launches,
