@@ -820,6 +820,8 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     GeomWork g{};
     std::vector<double> rot;
     geometry_tables(P, g.tm, g.car, rot);
+    if (s->has_position)
+        for (int k = 0; k < 3; ++k) g.car[k] = s->position[k];
     const size_t nt = (size_t)s->nf * ntau;
     const size_t bytes = align256((size_t)s->nv * ntau * 24) + align256(nt * 24) * 2 + align256(nt * 8) +
                          align256((size_t)ntau * 16);
@@ -1136,6 +1138,39 @@ ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp) {
 
 // observe (3905/Observe/NominalPole/wise_main.cpp:662-730), smooth surface,
 // FP64 on the device; constants wise_main.cpp:10-12
+// orbital_position_geometry (main.cpp:800-810): heliocentric body centre
+// (km) at true anomaly ta_deg of the orbit (a in AU, angles in degrees)
+ATPM_API atpm_status atpm_orbital_position(double a_au, double e, double inc_deg, double node_deg, double peri_deg,
+                                           double ta_deg, double* car_km) {
+    if (!car_km) return fail(ATPM_E_INVALID, "null output");
+    const double r = (a_au * kAU * (1.0 - (e * e))) / (1.0 + (e * std::cos(ta_deg * (kPI / 180.0))));
+    car_km[0] = r * ((std::cos(node_deg * (kPI / 180.0)) * std::cos((peri_deg + ta_deg) * (kPI / 180.0))) -
+                     (std::sin(node_deg * (kPI / 180.0)) * std::sin((peri_deg + ta_deg) * (kPI / 180.0)) *
+                      std::cos(inc_deg * (kPI / 180.0))));
+    car_km[1] = r * ((std::sin(node_deg * (kPI / 180.0)) * std::cos((peri_deg + ta_deg) * (kPI / 180.0))) +
+                     (std::cos(node_deg * (kPI / 180.0)) * std::sin((peri_deg + ta_deg) * (kPI / 180.0)) *
+                      std::cos(inc_deg * (kPI / 180.0))));
+    car_km[2] = r * std::sin((peri_deg + ta_deg) * (kPI / 180.0)) * std::sin(inc_deg * (kPI / 180.0));
+    return ATPM_OK;
+}
+
+// the body centre given directly (orbital sweeps, main.cpp:2612-2640): the
+// heliocentric distance and solar constant follow from it as in
+// asteroidgeometry (main.cpp:901-905)
+ATPM_API atpm_status atpm_set_position(atpm_solve* s, const double* car_km) {
+    if (!s || !car_km) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    for (int k = 0; k < 3; ++k) s->position[k] = car_km[k];
+    s->has_position = true;
+    s->P.polar[0] = std::sqrt((car_km[0] * car_km[0]) + (car_km[1] * car_km[1]) + (car_km[2] * car_km[2])) / kAU;
+    set_scalars(s, s->ti);
+    atpm_status r = upload_table(s);
+    if (r) return r;
+    CK(cudaStreamSynchronize(s->st));
+    s->have_forcing = false;
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
                                     double emissivity, int32_t nwl, const double* wavelength_um, double* flux) {
     if (!s || !observer || !wavelength_um || !flux || nwl < 1 || nwl > kMaxFluxWavelengths)

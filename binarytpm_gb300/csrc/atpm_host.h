@@ -49,6 +49,8 @@ struct atpm_solve {
     std::vector<double> vert_h;
     std::vector<int32_t> fac_h;
     bool have_forcing = false, have_temps = false;
+    bool has_position = false;  // body centre set directly (atpm_set_position)
+    double position[3] = {0, 0, 0};  // km, heliocentric
     float ti = 0.0f;
     double last_ms = 0.0;
     int64_t last_launches = 0, last_facet_steps = 0;

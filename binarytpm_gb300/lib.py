@@ -65,6 +65,9 @@ _SIGS = {
     "atpm_get_surface_temperature64": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_orbital_position": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                        C.c_void_p]),
+    "atpm_set_position": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_disk_flux": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p,
                                  C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -282,6 +285,11 @@ class Solve:
         t = np.zeros((self.nf, self.nx + 1), np.float32)
         _ck(load().atpm_get_depth_temperature(self.h, _p(t)))
         return t
+
+    def set_position(self, car_km):
+        """Place the body at a heliocentric centre (km) instead of its polar."""
+        c = np.ascontiguousarray(car_km, np.float64)
+        _ck(load().atpm_set_position(self.h, _p(c)))
 
     def disk_flux(self, observer, wavelengths_um=(12.0,), visibility=None, emissivity=0.9):
         """FP64 disk-integrated flux [ntau][nwl]; `observer` is the body's
@@ -525,3 +533,67 @@ class Crater:
             self.close()
         except Exception:
             pass
+
+
+def orbital_position(a_au, e, inc_deg, node_deg, peri_deg, ta_deg):
+    """Heliocentric body centre (km) at true anomaly ta_deg (degrees)."""
+    out = np.zeros(3, np.float64)
+    _ck(load().atpm_orbital_position(a_au, e, inc_deg, node_deg, peri_deg, ta_deg, _p(out)))
+    return out
+
+
+def _sweep(ctx, placements, thermal_inertia, precision, revcap):
+    """Solves at (problem, position) placements, swept over thermal inertias
+    with the reference's warm start, all advanced together per inertia."""
+    solves = []
+    for prob, car in placements:
+        s = Solve(ctx, prob, precision=precision, revcap=revcap)
+        s.set_position(car)
+        s.geometry_shadow()
+        s.scattering()
+        solves.append(s)
+    out = {}
+    initialised = False
+    for ti in thermal_inertia:
+        for s in solves:
+            s.set_thermal_inertia(ti)
+        if ti != 0.0 and not initialised:
+            for s in solves:
+                s.initialise_temperatures()
+            initialised = True
+        counts = batch_run(solves)
+        out[ti] = (np.stack([s.surface_temperature()[0] for s in solves]), counts)
+    for s in solves:
+        s.close()
+    return out
+
+
+def orbital_sweep(ctx, problem, elements, norb, thermal_inertia, precision=REFERENCE, revcap=301):
+    """The reference's orbital_model (main.cpp:2612-2810) as one batch per
+    thermal inertia: a solve per orbital point (true anomaly 360 i / norb),
+    each with its own geometry, shadows and scattered sunlight, the thermal
+    inertias swept in order with the reference's warm start, every orbital
+    point advanced together in atpm_batch_run.  elements = (a_au, e, inc_deg,
+    node_deg, peri_deg).  Returns {ti: (temperatures [norb][nf][ntau],
+    convergence counts per point)}."""
+    places = [(problem, orbital_position(*elements, 360.0 * i / norb)) for i in range(norb)]
+    return _sweep(ctx, places, thermal_inertia, precision, revcap)
+
+
+def obliquity_sweep(ctx, problem, elements, norb, nobl, thermal_inertia, js=range(1, 18), precision=REFERENCE,
+                    revcap=301):
+    """The reference's obliquity_model (main.cpp:2816-3003): pole latitude
+    90 - j (90 / nobl) degrees (longitude 0) for each j, at every orbital
+    point, at the one thermal inertia; every (j, point) solve in one batch.
+    Returns (temperatures [len(js) * norb][nf][ntau] in (j, point) order,
+    convergence counts in that order)."""
+    import dataclasses
+    import math
+
+    places = []
+    for j in js:
+        obliquity = 90.0 - (j * (90.0 / nobl))
+        pj = dataclasses.replace(problem, pole=(obliquity * (math.pi / 180.0), 0.0))
+        for i in range(norb):
+            places.append((pj, orbital_position(*elements, 360.0 * i / norb)))
+    return _sweep(ctx, places, [thermal_inertia], precision, revcap)[thermal_inertia]

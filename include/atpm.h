@@ -158,6 +158,16 @@ ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t 
  * current surface temperatures ([ntau][nf] step-major), through the solve's
  * own path (list-order gather, or the BF16 tensor-core product for FAST). */
 ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q);
+/* Orbital sweeps (orbital_model / obliquity_model, main.cpp:2612-3003): the
+ * heliocentric body centre (km) at true anomaly ta_deg of a Keplerian orbit
+ * (orbital_position_geometry, main.cpp:800-810), and a solve placed there
+ * instead of at params.polar (heliocentric distance and solar constant
+ * follow, main.cpp:901-905).  Call atpm_set_position before
+ * atpm_geometry_shadow; solves at different orbital points (or poles) batch
+ * together in atpm_batch_run. */
+ATPM_API atpm_status atpm_orbital_position(double a_au, double e, double inc_deg, double node_deg, double peri_deg,
+                                           double ta_deg, double* car_km);
+ATPM_API atpm_status atpm_set_position(atpm_solve* s, const double* car_km);
 /* Disk-integrated thermal flux seen by an observer, FP64 on the device: the
  * smooth-surface sum of the Observe stage's observe
  * (3905/Observe/NominalPole/wise_main.cpp:662-730, its geometry 555-645).

@@ -154,6 +154,38 @@ static void __oracle_rough_rev(Asteroid& A, int rev, float ti) {
 '''
 
 
+# Orbital sweep instrumentation (orbital_model): per orbital point i, the
+# forcing, the per-revolution counts and the final temperatures.
+_ORBIT_HOOKS = r'''
+static void __oracle_orbit_rev(Asteroid& A, int i, int rev, float ti) {
+	FILE* fp = fopen("oracle_orbit_revs.txt", "a");
+	fprintf(fp, "%d %.9g %d %d\n", i, ti, rev, A.rtnnumconverged());
+	fclose(fp);
+}
+static void __oracle_obl_rev(Asteroid& A, int j, int i, int rev, float ti) {
+	FILE* fp = fopen("oracle_obl_revs.txt", "a");
+	fprintf(fp, "%d %d %.9g %d %d\n", j, i, ti, rev, A.rtnnumconverged());
+	fclose(fp);
+}
+static void __oracle_obl_temps(Asteroid& A, int j, int i, float ti) {
+	FILE* fp = fopen("oracle_obl_temps.bin", "ab");
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = C->rtnstemp(1, s); fwrite(&v, 4, 1, fp); }
+	}
+	fclose(fp);
+}
+static void __oracle_orbit_temps(Asteroid& A, int i, float ti) {
+	char name[96];
+	snprintf(name, sizeof(name), "oracle_orbit_temps_%d_%.9g.bin", i, ti);
+	FILE* fp = fopen(name, "wb");
+	for (AstFacet* C = A.beginf(); C != A.endf(); ++C) {
+		for (int s = 0; s != NTAU; ++s) { float v = C->rtnstemp(1, s); fwrite(&v, 4, 1, fp); }
+	}
+	fclose(fp);
+}
+'''
+
+
 def thermal_defaults() -> dict:
     return dict(
         nv=642, nf=1280, shape="shape", ntau=720, nx=56,
@@ -217,6 +249,51 @@ def patch_thermal(cfg: dict) -> str:
     j = src.find("__oracle_rev_end(A, rev, t_inertia);", i)
     src = _insert_after(src, j, "if (roughness_thermal_model == 1) { retrieve_GPU_roughness_temperatures(A); }",
                         "\n\t\t__oracle_dump_temps(A, t_inertia);")
+    obl = c.get("obliquity")
+    if obl:
+        src = _sub_const(src, "single_run", "0")
+        src = _sub_const(src, "obliquity_run", "1")
+        src = _sub_const(src, "NORB", str(obl["norb"]))
+        src = _sub_const(src, "NOBL", str(obl["nobl"]))
+        for key, name in (("a", "semimajor_axis"), ("e", "eccentricity"), ("inc", "inclination"),
+                          ("node", "ascending_node"), ("peri", "argument_periapsis")):
+            src = _sub_const(src, name, _d(obl[key]))
+        k = src.find("void orbital_model(Asteroid& A, Surface& S) {")
+        src = src[:k] + _ORBIT_HOOKS + "\n" + src[k:]
+        k = src.find("void obliquity_model(Asteroid& A, Surface& S) {")
+        if k < 0:
+            raise RuntimeError("obliquity_model not found")
+        src = _replace_from(src, k, "while (A.rtnconverged() == 0 && rev < 301) {",
+                            "while (A.rtnconverged() == 0 && rev < ORACLE_REVCAP) {")
+        j = src.find("while (A.rtnconverged() == 0 && rev < ORACLE_REVCAP) {", k)
+        # the obliquity model runs the facets' default inertia, the minimum TI
+        src = _replace_from(src, j, "rev = rev + 1;",
+                            "__oracle_obl_rev(A, j, i, rev, minimum_thermal_inertia);\n\t\t\t\trev = rev + 1;")
+        j = src.find("__oracle_obl_rev(A, j, i, rev, minimum_thermal_inertia);", k)
+        src = _insert_after(src, j, "if (roughness_thermal_model == 1) { retrieve_GPU_roughness_temperatures(A); }",
+                            "\n\t\t\t__oracle_obl_temps(A, j, i, minimum_thermal_inertia);")
+    orb = c.get("orbital")
+    if orb:
+        src = _sub_const(src, "single_run", "0")
+        src = _sub_const(src, "orbital_run", "1")
+        src = _sub_const(src, "NORB", str(orb["norb"]))
+        src = _sub_const(src, "semimajor_axis", _d(orb["a"]))
+        src = _sub_const(src, "eccentricity", _d(orb["e"]))
+        src = _sub_const(src, "inclination", _d(orb["inc"]))
+        src = _sub_const(src, "ascending_node", _d(orb["node"]))
+        src = _sub_const(src, "argument_periapsis", _d(orb["peri"]))
+        k = src.find("void orbital_model(Asteroid& A, Surface& S) {")
+        if k < 0:
+            raise RuntimeError("orbital_model not found")
+        src = src[:k] + _ORBIT_HOOKS + "\n" + src[k:]
+        k = src.find("void orbital_model(Asteroid& A, Surface& S) {")
+        src = _replace_from(src, k, "while (A.rtnconverged() == 0 && rev < 301) {",
+                            "while (A.rtnconverged() == 0 && rev < ORACLE_REVCAP) {")
+        j = src.find("while (A.rtnconverged() == 0 && rev < ORACLE_REVCAP) {", k)
+        src = _replace_from(src, j, "rev = rev + 1;", "__oracle_orbit_rev(A, i, rev, t_inertia);\n\t\t\t\trev = rev + 1;")
+        j = src.find("__oracle_orbit_rev(A, i, rev, t_inertia);", k)
+        src = _insert_after(src, j, "if (roughness_thermal_model == 1) { retrieve_GPU_roughness_temperatures(A); }",
+                            "\n\t\t\t__oracle_orbit_temps(A, i, t_inertia);")
     if c["roughness"]:
         src = src[:i] + _ROUGH_HOOKS + "\n" + src[i:]
         i = src.find("void single_model(Asteroid& A, Surface& S) {")

@@ -37,6 +37,14 @@ CASES = {
                         albedo=0.02, tacc=0.005),
     "vis_s3s1": dict(kind="visibility", mesh=("binary", 3, 1), ntau=48,
                      pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
+    # orbital sweep (orbital_model): 3 points of an eccentric orbit, TI 200
+    "orbit_s2": dict(kind="thermal", mesh=("single", 2, 1), ntau=72, nx=8, ti=[200.0],
+                     pole=(math.pi / 2, 0.0), polar=(1.0, 0.0, 0.0), period_h=2.26, albedo=0.02, tacc=0.005,
+                     orbital=dict(norb=3, a=1.698, e=0.508, inc=12.17, node=356.652, peri=224.658)),
+    # obliquity sweep (obliquity_model): the reference's 17 obliquities x 2 orbital points
+    "obliquity_s2": dict(kind="thermal", mesh=("single", 2, 1), ntau=72, nx=8, ti=[200.0],
+                         pole=(math.pi / 2, 0.0), polar=(1.0, 0.0, 0.0), period_h=2.26, albedo=0.02, tacc=0.005,
+                         obliquity=dict(norb=2, nobl=9, a=1.698, e=0.508, inc=12.17, node=356.652, peri=224.658)),
     # crater partial visibility toward the observer (Visibility's GPU module)
     "vis_rough_s1s1": dict(kind="visibility", rough=True, mesh=("binary", 1, 1), ntau=48,
                            pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
@@ -66,7 +74,9 @@ def thermal_cfg(name: str, threads: int = 1, revcap: int = 301) -> dict:
                 ti_min=c["ti"][0], ti_max=c["ti"][-1],
                 ti_step=(c["ti"][1] - c["ti"][0]) if len(c["ti"]) > 1 else 10.0,
                 threads=threads, revcap=revcap,
-                **(dict(roughness=1, write_roughness_temperature=1) if c.get("rough") else {}))
+                **(dict(roughness=1, write_roughness_temperature=1) if c.get("rough") else {}),
+                **(dict(orbital=c["orbital"]) if c.get("orbital") else {}),
+                **(dict(obliquity=c["obliquity"]) if c.get("obliquity") else {}))
 
 
 def rough_output_files(name: str) -> list[str]:
@@ -158,6 +168,29 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
             out["shape_counts"] = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)[:, 2].astype(np.int32)
             T = np.fromfile(wd / ("shape_roughness_temperature(%g).dat" % c["ti"][-1]), dtype=np.float32)
             out["rough_stemp1_head"] = T[61 * 3 + 100 * 3:][:100 * c["ntau"]].copy()   # first facet
+        elif c["kind"] == "thermal" and c.get("obliquity"):
+            import hashlib
+            write_thermal_inputs(wd, v, f, ptr, idx, vf)
+            refbuild.run(refbuild.build_thermal(thermal_cfg(name)), wd)
+            raw = (wd / "oracle_obl_temps.bin").read_bytes()
+            out["obl_temps_sha256"] = np.array(hashlib.sha256(raw).hexdigest())
+            out["obl_temps_nbytes"] = np.array(len(raw))
+            rv = np.loadtxt(wd / "oracle_obl_revs.txt", ndmin=2)
+            out["obl_j"], out["obl_i"] = rv[:, 0].astype(np.int32), rv[:, 1].astype(np.int32)
+            out["obl_counts"] = rv[:, 4].astype(np.int32)
+            T = np.frombuffer(raw, dtype=np.float32).reshape(-1, nf, c["ntau"])
+            out["obl_stemp1_first_last"] = np.stack([T[0], T[-1]])
+        elif c["kind"] == "thermal" and c.get("orbital"):
+            write_thermal_inputs(wd, v, f, ptr, idx, vf)
+            exe = refbuild.build_thermal(thermal_cfg(name))
+            refbuild.run(exe, wd)
+            norb, ntau = c["orbital"]["norb"], c["ntau"]
+            ti = c["ti"][-1]
+            out["orbit_stemp1"] = np.stack([np.fromfile(wd / ("oracle_orbit_temps_%d_%.9g.bin" % (i, ti)), dtype=np.float32)
+                                            .reshape(nf, ntau) for i in range(norb)])
+            rv = np.loadtxt(wd / "oracle_orbit_revs.txt", ndmin=2)
+            out["orbit_counts"] = rv[:, 3].astype(np.int32)
+            out["orbit_index"] = rv[:, 0].astype(np.int32)
         elif c["kind"] == "thermal":
             exe = refbuild.build_thermal(thermal_cfg(name))
             refbuild.run(exe, wd)
