@@ -85,7 +85,10 @@ atpm_status ensure_qroot_table(atpm_context* c) {
 
 // pole transformation matrix, heliocentric body centre and rotation table of
 // the reference's asteroidgeometry (main.cpp:894-958), with this host's libm
-void geometry_tables(const atpm_params& P, double* tm9, double* car, std::vector<double>& rot) {
+// (rotation angle 2 pi step revs / NTAU: revs = 1 for a synchronous body,
+// each body's own number of turns per model period for a non-synchronous
+// binary, 175706/Run-04/thermal.cpp:1347, 1365)
+void geometry_tables(const atpm_params& P, double* tm9, double* car, std::vector<double>& rot, int revs = 1) {
     const double r0 = P.pole[0], r1 = P.pole[1];
     const double gamma = std::acos(std::cos(r0) * std::sin(std::fabs(r1)));
     double tm[3][3];
@@ -106,7 +109,7 @@ void geometry_tables(const atpm_params& P, double* tm9, double* car, std::vector
     const int ntau = P.ntau;
     rot.assign(2 * (size_t)ntau, 0.0);
     for (int step = 0; step < ntau; ++step) {
-        const double ang = 2.0 * kPI * step / ntau;
+        const double ang = 2.0 * kPI * step * revs / ntau;
         rot[2 * step] = std::cos(ang);
         rot[2 * step + 1] = std::sin(ang);
     }
@@ -195,10 +198,18 @@ void set_scalars(atpm_solve* s, float ti) {
     DevSolve& d = s->ds;
     const float PIf = (float)kPI;
     const float DZ = 8.0f / P.nx;
-    const float DTAU = 2.0f * PIf / P.ntau;
+    // per-body rotations per model period (non-synchronous binaries,
+    // 175706/Run-04/thermal.cpp:1925, 1966-1967); 1 for a synchronous body
+    const float nr = (float)s->revs_p, nr2 = (float)s->revs_s;
+    const float DTAU = 2.0f * PIf * nr / (float)P.ntau;
+    const float DTAU2 = 2.0f * PIf * nr2 / (float)P.ntau;
     d.ti = ti;
     d.r = DTAU / (DZ * DZ);
-    d.m1 = ti * std::sqrt(2.0f * PIf / P.rotation_period_s) / DZ;
+    d.m1 = ti * std::sqrt(2.0f * PIf * nr / P.rotation_period_s) / DZ;
+    d.r2 = DTAU2 / (DZ * DZ);
+    d.m1_2 = ti * std::sqrt(2.0f * PIf * nr2 / P.rotation_period_s) / DZ;
+    d.fsplit = s->sec_facet >= 0 ? s->sec_facet : s->nf;
+    d.es_w = s->ir_abs * P.emissivity * kSIGMA;
     d.es = P.emissivity * kSIGMA;
     d.es4 = 4.0f * P.emissivity * kSIGMA;
     d.oma = 1.0f - P.albedo;
@@ -213,10 +224,14 @@ void set_scalars(atpm_solve* s, float ti) {
     // FP64 state: the same expressions with double operands
     const double PId = (double)PIf;
     const double DZd = 8.0 / P.nx;
-    const double DTAUd = 2.0 * PId / P.ntau;
+    const double DTAUd = 2.0 * PId * (double)nr / P.ntau;
+    const double DTAU2d = 2.0 * PId * (double)nr2 / P.ntau;
     d.ti_d = ti;
     d.r_d = DTAUd / (DZd * DZd);
-    d.m1_d = (double)ti * std::sqrt(2.0 * PId / (double)P.rotation_period_s) / DZd;
+    d.m1_d = (double)ti * std::sqrt(2.0 * PId * (double)nr / (double)P.rotation_period_s) / DZd;
+    d.r2_d = DTAU2d / (DZd * DZd);
+    d.m1_2_d = (double)ti * std::sqrt(2.0 * PId * (double)nr2 / (double)P.rotation_period_s) / DZd;
+    d.es_w_d = (double)s->ir_abs * (double)P.emissivity * (double)kSIGMA;
     d.es_d = (double)P.emissivity * (double)kSIGMA;
     d.es4_d = 4.0 * (double)P.emissivity * (double)kSIGMA;
     d.oma_d = 1.0 - (double)P.albedo;
@@ -818,13 +833,16 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     const int ntau = P.ntau;
     // host: pole matrix, heliocentric centre, rotation table (main.cpp:894-958)
     GeomWork g{};
-    std::vector<double> rot;
-    geometry_tables(P, g.tm, g.car, rot);
+    std::vector<double> rot, rot2;
+    geometry_tables(P, g.tm, g.car, rot, s->revs_p);
+    geometry_tables(P, g.tm, g.car, rot2, s->revs_s);
+    rot.insert(rot.end(), rot2.begin(), rot2.end());  // [primary | secondary]
+    g.vsplit = s->sec_vertex >= 0 ? s->sec_vertex : s->nv;
     if (s->has_position)
         for (int k = 0; k < 3; ++k) g.car[k] = s->position[k];
     const size_t nt = (size_t)s->nf * ntau;
     const size_t bytes = align256((size_t)s->nv * ntau * 24) + align256(nt * 24) * 2 + align256(nt * 8) +
-                         align256((size_t)ntau * 16);
+                         align256((size_t)ntau * 32);
     void* tmp = nullptr;
     CK(cudaMallocAsync(&tmp, bytes, s->st));
     char* t = static_cast<char*>(tmp);
@@ -837,6 +855,7 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     g.dist = reinterpret_cast<double*>(t);
     t += align256(nt * 8);
     g.rot = reinterpret_cast<double*>(t);
+    g.rot2 = g.rot + 2 * (size_t)ntau;
     cudaError_t e = cudaMemcpyAsync((void*)g.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, s->st);
     int rc = 0;
     if (e == cudaSuccess) rc = launch_geometry(s->ds, g, s->st);
@@ -1154,6 +1173,43 @@ ATPM_API atpm_status atpm_orbital_position(double a_au, double e, double inc_deg
     return ATPM_OK;
 }
 
+// non-synchronous binary (175706/Run-04/thermal.cpp: asteroidgeometry
+// 1347-1381, set_facet_rotation 860-869, inertiadifference 1925-1967): the
+// first primary_vertices vertices / primary_facets facets are the primary,
+// which turns primary_revs times per model period (params.ntau steps over
+// params.rotation_period_s), the rest turn secondary_revs times
+ATPM_API atpm_status atpm_set_binary_rotation(atpm_solve* s, int32_t primary_vertices, int32_t primary_facets,
+                                              int32_t primary_revs, int32_t secondary_revs) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (primary_vertices < 1 || primary_vertices > s->nv || primary_facets < 1 || primary_facets > s->nf ||
+        primary_revs < 1 || secondary_revs < 1)
+        return fail(ATPM_E_INVALID, "set_binary_rotation: bad split or revolution counts");
+    CK(cudaSetDevice(s->ctx->device));
+    s->sec_vertex = primary_vertices;
+    s->sec_facet = primary_facets;
+    s->revs_p = primary_revs;
+    s->revs_s = secondary_revs;
+    set_scalars(s, s->ti);
+    atpm_status r = upload_table(s);
+    if (r) return r;
+    CK(cudaStreamSynchronize(s->st));
+    s->have_forcing = false;  // the geometry changes: recompute shadows and illumination
+    return ATPM_OK;
+}
+
+// IR absorptivity of the self-heating sum (IR_ABS, 175706/Run-04/thermal.cpp:
+// 72, 1950-1952); 1 unless set
+ATPM_API atpm_status atpm_set_ir_absorptivity(atpm_solve* s, float ir_abs) {
+    if (!s || !(ir_abs >= 0.0f && ir_abs <= 1.0f)) return fail(ATPM_E_INVALID, "set_ir_absorptivity: 0 <= a <= 1");
+    CK(cudaSetDevice(s->ctx->device));
+    s->ir_abs = ir_abs;
+    set_scalars(s, s->ti);
+    atpm_status r = upload_table(s);
+    if (r) return r;
+    CK(cudaStreamSynchronize(s->st));
+    return ATPM_OK;
+}
+
 // the body centre given directly (orbital sweeps, main.cpp:2612-2640): the
 // heliocentric distance and solar constant follow from it as in
 // asteroidgeometry (main.cpp:901-905)
@@ -1180,8 +1236,11 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
     const atpm_params& P = s->P;
     const int nf = s->nf, ntau = P.ntau;
     FluxArgs a{};
-    std::vector<double> rot;
-    geometry_tables(P, a.tm, a.car, rot);
+    std::vector<double> rot, rot2;
+    geometry_tables(P, a.tm, a.car, rot, s->revs_p);
+    geometry_tables(P, a.tm, a.car, rot2, s->revs_s);
+    rot.insert(rot.end(), rot2.begin(), rot2.end());  // [primary | secondary]
+    a.vsplit = s->sec_vertex >= 0 ? s->sec_vertex : s->nv;
     // the stage places the body at AU(m) x polar and the observer at the body
     // minus its geocentric vector (wise_main.cpp:8, 530-538)
     const double AUm = 149.6e9;
@@ -1211,6 +1270,7 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
     CK(cudaMallocAsync(&tmp, b_rot + b_part + b_out + b_vis, s->st));
     char* t = static_cast<char*>(tmp);
     a.rot = reinterpret_cast<const double*>(t);
+    a.rot2 = a.rot + 2 * (size_t)ntau;
     a.partial = reinterpret_cast<double*>(t + b_rot);
     a.out = reinterpret_cast<double*>(t + b_rot + b_part);
     a.visible = visibility ? reinterpret_cast<const uint8_t*>(t + b_rot + b_part + b_out) : nullptr;

@@ -34,7 +34,8 @@ __device__ __forceinline__ double temp_at(const DevSolve& s, int f, int step) {
 
 __device__ __forceinline__ void vertex_at(const DevSolve& s, const FluxArgs& a, int v, int step, double* out) {
     const double* e = s.vert + 3 * v;
-    const double c = a.rot[2 * step], sn = a.rot[2 * step + 1];
+    const double* rt = (v < a.vsplit) ? a.rot : a.rot2;
+    const double c = rt[2 * step], sn = rt[2 * step + 1];
     double rq[3];
     rq[0] = __dsub_rn(__dmul_rn(e[0], c), __dmul_rn(e[1], sn));
     rq[1] = __dadd_rn(__dmul_rn(e[0], sn), __dmul_rn(e[1], c));

@@ -59,7 +59,9 @@ __global__ void __launch_bounds__(256) k_geom_vertices(GeomArgs a) {
     if (i >= (long long)nv * ntau) return;
     const int v = (int)(i / ntau), s = (int)(i % ntau);
     const double* e = a.s.vert + 3 * v;
-    const double c = a.g.rot[2 * s], sn = a.g.rot[2 * s + 1];
+    // a non-synchronous secondary turns at its own rate (its own table)
+    const double* rt = (v < a.g.vsplit) ? a.g.rot : a.g.rot2;
+    const double c = rt[2 * s], sn = rt[2 * s + 1];
     double rq[3];
     rq[0] = DSUB(DMUL(e[0], c), DMUL(e[1], sn));
     rq[1] = DADD(DMUL(e[0], sn), DMUL(e[1], c));

@@ -50,6 +50,11 @@ struct atpm_solve {
     std::vector<int32_t> fac_h;
     bool have_forcing = false, have_temps = false;
     bool has_position = false;  // body centre set directly (atpm_set_position)
+    // non-synchronous binary (atpm_set_binary_rotation): vertices/facets from
+    // sec_vertex/sec_facet on turn revs_s times per model period, the rest
+    // revs_p times; -1: synchronous (one rigid rotation)
+    int sec_vertex = -1, sec_facet = -1, revs_p = 1, revs_s = 1;
+    float ir_abs = 1.0f;  // IR absorptivity in the self-heating sum
     double position[3] = {0, 0, 0};  // km, heliocentric
     float ti = 0.0f;
     double last_ms = 0.0;

@@ -101,6 +101,14 @@ struct DevSolve {
     float ti, oma, es, es4, m1, r, tacc, tacc10, alb, solar, sacc;
     double ti_d, oma_d, es_d, es4_d, m1_d, r_d, tacc_d, tacc10_d, alb_d, solar_d, sacc_d;
     int newton_cap;
+    // non-synchronous binary: facets >= fsplit (the secondary) use r2 / m1_2,
+    // from their own number of rotations per model period; fsplit = nf otherwise
+    int fsplit;
+    float r2, m1_2;
+    double r2_d, m1_2_d;
+    // weight of the self-heating sum: IR absorptivity x eps x sigma
+    float es_w;
+    double es_w_d;
     // FAST precision, tensor-core self-heating (atpm_spmm_tc.cu); null when off
     const int* tc_ptr;       // [nmb+1] tile range of each 128-facet row block
     const int* tc_col;       // [ntiles] 64-facet column block of each tile
@@ -128,6 +136,8 @@ struct GeomWork {
     double* nrm;     // [nf][ntau][3] unit normals
     double* dist;    // [nf][ntau] |hm|
     const double* rot;  // [ntau][2] cos, sin of the rotation angle (host libm)
+    const double* rot2; // the same for vertices >= vsplit (non-synchronous secondary)
+    int vsplit;         // first vertex of the secondary (nv when synchronous)
     double tm[9];    // pole transformation matrix
     double car[3];   // heliocentric centre (km)
 };
@@ -184,6 +194,8 @@ int launch_energy_balance(const DevSolve& s, stream_t st);
 constexpr int kMaxFluxWavelengths = 8;
 struct FluxArgs {
     const double* rot;       // [ntau][2] cos, sin of the rotation angle (host libm)
+    const double* rot2;      // vertices >= vsplit (non-synchronous secondary)
+    int vsplit;
     double tm[9];            // pole matrix
     double car[3];           // body centre (km)
     double obs[3];           // observer (km)

@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) k_w_bf16(Batch b) {
     const int nf = sv.nf, ntau = sv.ntau, N = sv.tc_n, nch = sv.tc_nchunks;
     const float* T = static_cast<const float*>(sv.stemp1);
     __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
-    const float es = sv.es;
+    const float es = sv.es_w;
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const int s = t.z + j, f = t.y + threadIdx.x;
         if (s >= ntau || f >= nf) continue;
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(256) k_w_bf16_one(DevSolve sv) {
     const int s = (int)(i / nf), f = (int)(i % nf);
     const float x = static_cast<const float*>(sv.stemp1)[i];
     const float x2 = x * x;
-    const float w = sv.es * (x2 * x2);
+    const float w = sv.es_w * (x2 * x2);
     __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
     const size_t base = ((size_t)(f / TC_K) * nch + s / N) * (size_t)2 * N * TC_K;
     const __nv_bfloat16 hi = __float2bfloat16_rn(w);

@@ -91,15 +91,21 @@ template <> struct Pw<MODE_FAST> {
 // per-mode scalar views of DevSolve
 template <int MODE> struct Sc {
     using R = typename Ar<MODE>::R;
-    R ti, oma, es, es4, m1, r, tacc, tacc10;
+    R ti, oma, es, es4, m1, r, tacc, tacc10, esw;
     __device__ __forceinline__ void load(const DevSolve& s) {
         if constexpr (MODE == MODE_FP64) {
             ti = s.ti_d; oma = s.oma_d; es = s.es_d; es4 = s.es4_d; m1 = s.m1_d; r = s.r_d;
-            tacc = s.tacc_d; tacc10 = s.tacc10_d;
+            tacc = s.tacc_d; tacc10 = s.tacc10_d; esw = s.es_w_d;
         } else {
             ti = s.ti; oma = s.oma; es = s.es; es4 = s.es4; m1 = s.m1; r = s.r;
-            tacc = s.tacc; tacc10 = s.tacc10;
+            tacc = s.tacc; tacc10 = s.tacc10; esw = s.es_w;
         }
+    }
+    // facet f's own rotation rate (the secondary of a non-synchronous binary)
+    __device__ __forceinline__ void body(const DevSolve& s, int f) {
+        if (f < s.fsplit) return;
+        if constexpr (MODE == MODE_FP64) { m1 = s.m1_2_d; r = s.r2_d; }
+        else { m1 = s.m1_2; r = s.r2; }
     }
 };
 
@@ -121,7 +127,7 @@ __global__ void __launch_bounds__(256) k_selfheat_w(Batch b) {
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const int s = t.z + j, f = t.y + threadIdx.x;
         R v = R(0);
-        if (s < ntau && f < nf) v = A::mul(c.es, Pw<MODE>::p4(b.p4, T[(size_t)s * nf + f], sv.status));
+        if (s < ntau && f < nf) v = A::mul(c.esw, Pw<MODE>::p4(b.p4, T[(size_t)s * nf + f], sv.status));
         sm[j][threadIdx.x] = v;
     }
     __syncthreads();
@@ -176,6 +182,7 @@ __device__ __forceinline__ void column_revolution(const DevSolve& sv, const Batc
     const int nf = sv.nf, ntau = sv.ntau;
     Sc<MODE> c;
     c.load(sv);
+    c.body(sv, f);
     R* temp = static_cast<R*>(sv.temp);
     const R* E = static_cast<const R*>(sv.E);
     const R* Q = static_cast<const R*>(sv.Q);
@@ -229,7 +236,7 @@ __device__ __forceinline__ void column_revolution(const DevSolve& sv, const Batc
 __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float t) {
     const int N = sv.tc_n;
     const float t2 = t * t;
-    const float w = sv.es * (t2 * t2);
+    const float w = sv.es_w * (t2 * t2);
     __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
     const size_t base = ((size_t)(f >> 6) * sv.tc_nchunks + s / N) * (size_t)2 * N * 64;
     const uint32_t o = swz((uint32_t)(s % N), (uint32_t)(f & 63));
@@ -253,7 +260,9 @@ __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float 
 template <int NX>
 __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f) {
     const int nf = sv.nf, ntau = sv.ntau;
-    const float r = sv.r, oma = sv.oma, es = sv.es, es4 = sv.es4, m1 = sv.m1, tacc = sv.tacc, tacc10 = sv.tacc10;
+    const bool sec = f >= sv.fsplit;  // non-synchronous secondary: its own rotation rate
+    const float r = sec ? sv.r2 : sv.r, oma = sv.oma, es = sv.es, es4 = sv.es4, m1 = sec ? sv.m1_2 : sv.m1,
+                tacc = sv.tacc, tacc10 = sv.tacc10;
     float* temp = static_cast<float*>(sv.temp);
     const float* __restrict__ E = static_cast<const float*>(sv.E);
     const float* __restrict__ Q = static_cast<const float*>(sv.Q);
@@ -328,7 +337,7 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         S1[o] = Tsurf;
         if (Wb) {
             const float t2s = Tsurf * Tsurf;
-            const float w = es * (t2s * t2s);
+            const float w = sv.es_w * (t2s * t2s);
             const uint32_t off = (uint32_t)wn * 64u + ((kc ^ ((uint32_t)wn & 7u)) << 3) + k7;
             const __nv_bfloat16 hi = __float2bfloat16_rn(w);
             Wb[wrow + off] = hi;

@@ -68,6 +68,8 @@ _SIGS = {
     "atpm_orbital_position": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_void_p]),
     "atpm_set_position": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_set_binary_rotation": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "atpm_set_ir_absorptivity": (C.c_int, [C.c_void_p, C.c_float]),
     "atpm_disk_flux": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p,
                                  C.c_void_p]),
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -285,6 +287,16 @@ class Solve:
         t = np.zeros((self.nf, self.nx + 1), np.float32)
         _ck(load().atpm_get_depth_temperature(self.h, _p(t)))
         return t
+
+    def set_binary_rotation(self, primary_vertices: int, primary_facets: int, primary_revs: int,
+                            secondary_revs: int):
+        """Non-synchronous binary: the first vertices/facets (the primary)
+        turn primary_revs times per model period, the rest secondary_revs."""
+        _ck(load().atpm_set_binary_rotation(self.h, int(primary_vertices), int(primary_facets), int(primary_revs),
+                                            int(secondary_revs)))
+
+    def set_ir_absorptivity(self, ir_abs: float):
+        _ck(load().atpm_set_ir_absorptivity(self.h, float(ir_abs)))
 
     def set_position(self, car_km):
         """Place the body at a heliocentric centre (km) instead of its polar."""

@@ -158,6 +158,20 @@ ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t 
  * current surface temperatures ([ntau][nf] step-major), through the solve's
  * own path (list-order gather, or the BF16 tensor-core product for FAST). */
 ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q);
+/* Non-synchronous binary (the 175706 Thermal program,
+ * 175706/Run-04/thermal.cpp:1347-1381, 860-869, 1925-1967): the first
+ * primary_vertices vertices and primary_facets facets form the primary,
+ * which turns primary_revs times during the model period (params.ntau steps
+ * over params.rotation_period_s); the other vertices and facets (the
+ * secondary, turning about the same axis) turn secondary_revs times.  Each
+ * body's conduction uses its own time step and skin-depth factor.  Mutual
+ * eclipses need all-pairs shadowing (params.shadowing = 2).  Call before
+ * atpm_geometry_shadow. */
+ATPM_API atpm_status atpm_set_binary_rotation(atpm_solve* s, int32_t primary_vertices, int32_t primary_facets,
+                                              int32_t primary_revs, int32_t secondary_revs);
+/* IR absorptivity applied to the self-heating sum (IR_ABS,
+ * 175706/Run-04/thermal.cpp:72, 1950-1952); 1 unless set. */
+ATPM_API atpm_status atpm_set_ir_absorptivity(atpm_solve* s, float ir_abs);
 /* Orbital sweeps (orbital_model / obliquity_model, main.cpp:2612-3003): the
  * heliocentric body centre (km) at true anomaly ta_deg of a Keplerian orbit
  * (orbital_position_geometry, main.cpp:800-810), and a solve placed there

@@ -40,6 +40,7 @@ THERMAL_SRC = "3905/Thermal/NominalPole/main.cpp"
 SELFHEAT_SRC = "3905/Shape_Selfheating/main.cpp"
 VISIB_SRC = "3905/Visibility/NominalPole/main.cpp"
 OBSERVE_SRC = "3905/Observe/NominalPole/wise_main.cpp"
+NONSYNC_SRC = "175706/Run-04/thermal.cpp"
 CRATER_FILES = ["new_crater2.txt", "new_crater2_selfheating_list.txt",
                 "new_crater2_photovectors.txt"]
 CRATER_DIR = "3905/Thermal/NominalPole"
@@ -432,6 +433,72 @@ def build_thermal_refgpu(cfg: dict, cuda_home: str = "/usr/local/cuda") -> Path:
                     "-DORACLE_REVCAP=%d" % full["revcap"], str(src_path), str(obj),
                     "-L", cuda_home + "/lib64", "-lcudart", "-Wl,-rpath," + cuda_home + "/lib64",
                     "-o", str(exe)], check=True)
+    return exe
+
+
+_NONSYNC_HOOKS = r'''
+#include <cstdio>
+static void __oracle_rev(Asteroid& A, int rev) {
+	FILE* fp = fopen("oracle_revs.txt", "a");
+	fprintf(fp, "%d %d\n", rev, A.rtnnumconverged());
+	fclose(fp);
+}
+'''
+
+
+def patch_nonsync(cfg: dict) -> str:
+    """The reference's non-synchronous binary Thermal program
+    (175706/Run-04/thermal.cpp) for one configuration: one part, roughness
+    off, a fixed thermal inertia, per-revolution convergence counts logged;
+    it writes its full-precision temperatures itself
+    (binary_writeglobaltemperature, thermal.cpp:3291-3316)."""
+    src = (REF_ROOT / NONSYNC_SRC).read_text(errors="replace")
+    c = cfg
+    for name, val in (("ASTNUMVTX", c["nv"]), ("ASTNUMFACE", c["nf"]), ("NUMROUGHFACE", c["nf"]), ("NUMPARTS", 1),
+                      ("PRINUMVTX", c["prinumvtx"]), ("PRINUMFACE", c["prinumface"]),
+                      ("NUMPRIREV", c["prirevs"]), ("NUMSECREV", c["secrevs"]), ("NTAU", c["ntau"]), ("NX", c["nx"]),
+                      ("fixed_thermal_inertia", 1), ("instant_equib_model", 0), ("roughness_thermal_model", 0),
+                      ("load_shape_selfheating", c["selfheating"]), ("multiple_scattering", 1),
+                      ("write_roughness_temperature", 0)):
+        src = _sub_const(src, name, str(val))
+    src = _sub_const(src, "shape_filename", '"%s"' % c.get("shape", "shape"))
+    src = _sub_const(src, "polar0", _d(c["polar"][0]))
+    src = _sub_const(src, "polar1", _d(c["polar"][1]))
+    src = _sub_const(src, "polar2", _d(c["polar"][2]))
+    src = _sub_const(src, "rot0", _d(c["rot"][0]))
+    src = _sub_const(src, "rot1", _d(c["rot"][1]))
+    for name in ("EPS", "rotation_period", "bond_albedo", "thermal_inertia", "TACC", "scattering_accuracy", "IR_ABS"):
+        src = _sub_const(src, name, _f(c[name]))
+    src = _sub_const(src, "num_threads", "ORACLE_THREADS")
+    i = src.find("void single_model(Asteroid &A, Surface &S) {")
+    if i < 0:
+        raise RuntimeError("single_model not found")
+    src = src[:i] + _NONSYNC_HOOKS + "\n" + src[i:]
+    i = src.find("void single_model(Asteroid &A, Surface &S) {")
+    src = _replace_from(src, i, "while (A.rtnconverged()==0 && rev<301) {",
+                        "while (A.rtnconverged()==0 && rev<ORACLE_REVCAP) {")
+    j = src.find("while (A.rtnconverged()==0 && rev<ORACLE_REVCAP) {", i)
+    src = _replace_from(src, j, "rev=rev+1;", "__oracle_rev(A, rev);\n\t\t\t\trev=rev+1;")
+    # the per-part roughness maps are not written: nothing to stitch
+    src = _replace_from(src, i, "\tstitch_temperatures();", "")
+    return src
+
+
+def build_nonsync(cfg: dict, threads: int = 1, revcap: int = 301) -> Path:
+    """Reference non-synchronous Thermal program, scratch copy, compiled with
+    stand-ins for its (unused) roughness GPU module."""
+    d = OUT_ROOT / _tag("nonsync", cfg)
+    src_path = d / "thermal.cpp"
+    exe = d / ("nonsync_t%d_r%d" % (threads, revcap))
+    if exe.exists():
+        return exe
+    d.mkdir(parents=True, exist_ok=True)
+    if not src_path.exists():
+        if not (REF_ROOT / NONSYNC_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        src_path.write_text(patch_nonsync(cfg))
+    subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % threads, "-DORACLE_REVCAP=%d" % revcap, str(src_path),
+                    str(HERE / "ref_nonsync_gpu_stub.cpp"), "-o", str(exe)], check=True)
     return exe
 
 

@@ -34,7 +34,7 @@ def golden(name: str):
     for key in ("shadow", "visibility"):
         if key in ref:
             ref[key] = np.unpackbits(ref[key])[: nf * ntau].reshape(nf, ntau).astype(np.int32)
-    if "counts" in ref:
+    if "counts" in ref and "counts_split" in ref:
         split = np.cumsum(ref["counts_split"])[:-1]
         ref["counts_list"] = np.split(ref["counts"], split)
     return prob, ref

@@ -45,6 +45,15 @@ CASES = {
     "obliquity_s2": dict(kind="thermal", mesh=("single", 2, 1), ntau=72, nx=8, ti=[200.0],
                          pole=(math.pi / 2, 0.0), polar=(1.0, 0.0, 0.0), period_h=2.26, albedo=0.02, tacc=0.005,
                          obliquity=dict(norb=2, nobl=9, a=1.698, e=0.508, inc=12.17, node=356.652, peri=224.658)),
+    # non-synchronous binary (the 175706 program): primary turns 3 times per
+    # model period, secondary once; all-pairs shadowing; without and with
+    # self-heating lists (IR absorptivity 0.9)
+    "nonsync_s2s1": dict(kind="nonsync", mesh=("binary", 2, 1), ntau=72, nx=8, ti=[200.0], prirevs=3, secrevs=1,
+                         pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9, albedo=0.02, tacc=0.005,
+                         selfheating=0, ir_abs=1.0),
+    "nonsync_sh_s2s1": dict(kind="nonsync", mesh=("binary", 2, 1), ntau=72, nx=8, ti=[200.0], prirevs=3, secrevs=1,
+                            pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9, albedo=0.02, tacc=0.005,
+                            selfheating=1, ir_abs=0.9),
     # crater partial visibility toward the observer (Visibility's GPU module)
     "vis_rough_s1s1": dict(kind="visibility", rough=True, mesh=("binary", 1, 1), ntau=48,
                            pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
@@ -116,6 +125,18 @@ def write_thermal_inputs(wd: Path, vertices, facets, dep_ptr, dep_idx, dep_vf, d
         formats.write_photovectors(wd / "shape_photovectors.txt", photo)
 
 
+def nonsync_cfg(name: str) -> dict:
+    """The compile-time configuration of the reference non-synchronous run."""
+    c = CASES[name]
+    v, f = case_mesh(c["mesh"])
+    pv_, pf_ = mesh.perturbed_body(c["mesh"][1], 0.39, 0.05, 2)   # the primary of binary_mesh (listed first)
+    pv, pf = len(pv_), len(pf_)
+    return dict(nv=len(v), nf=len(f), prinumvtx=pv, prinumface=pf, prirevs=c["prirevs"], secrevs=c["secrevs"],
+                ntau=c["ntau"], nx=c["nx"], polar=c["polar"], rot=c["pole"], EPS=0.9,
+                rotation_period=c["period_h"] * 3600.0, bond_albedo=c["albedo"], thermal_inertia=c["ti"][0],
+                TACC=c["tacc"], scattering_accuracy=1e-4, IR_ABS=c["ir_abs"], selfheating=c["selfheating"])
+
+
 def visibility_cfg(name: str, threads: int = 1) -> dict:
     """The compile-time configuration of the reference Visibility run of a case."""
     c = CASES[name]
@@ -168,6 +189,22 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
             out["shape_counts"] = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)[:, 2].astype(np.int32)
             T = np.fromfile(wd / ("shape_roughness_temperature(%g).dat" % c["ti"][-1]), dtype=np.float32)
             out["rough_stemp1_head"] = T[61 * 3 + 100 * 3:][:100 * c["ntau"]].copy()   # first facet
+        elif c["kind"] == "nonsync":
+            cfg = nonsync_cfg(name)
+            if c["selfheating"]:
+                out["dep_vec"] = formats.read_float_stream(wd / "shape_selfheating_vector_list.txt", 3 * len(idx))
+                out["photovectors"] = formats.read_float_stream(wd / "shape_photovectors.txt", 3 * nf)
+                write_thermal_inputs(wd, v, f, ptr, idx, vf, out["dep_vec"], out["photovectors"])
+            else:
+                z = np.zeros(nf + 1, np.int32)
+                write_thermal_inputs(wd, v, f, z, z[:0], np.zeros(0, np.float32))
+            refbuild.run(refbuild.build_nonsync(cfg), wd)
+            raw = np.fromfile(wd / ("shape_temperature(%g).dat" % c["ti"][0]), dtype=np.uint8)
+            off = len(v) * 24 + nf * 12
+            out["stemp1"] = raw[off:].view(np.float32).reshape(nf, c["ntau"]).copy()
+            out["counts"] = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)[:, 1].astype(np.int32)
+            out["prinumvtx"] = np.array(cfg["prinumvtx"])
+            out["prinumface"] = np.array(cfg["prinumface"])
         elif c["kind"] == "thermal" and c.get("obliquity"):
             import hashlib
             write_thermal_inputs(wd, v, f, ptr, idx, vf)
