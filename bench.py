@@ -170,10 +170,11 @@ def prepare():
     return refbuild.thermal_source(_ref_cfg(prob, 200.0, 1, 3))
 
 
-def profile_case():
+def profile_case(nsolves: int = 2):
     """A small, fast case of the same kernels for ncu --set full captures:
     the binary with a subdivision-4 primary (5,120 + 1,280 facets, NX = 56,
-    NTAU = 720), two FAST solves, three instrumented revolutions."""
+    NTAU = 720), ``nsolves`` FAST solves (thermal inertias from the batched
+    sweep), three instrumented revolutions."""
     from binarytpm_gb300 import lib, workloads
 
     ctx = lib.Context(0)
@@ -182,13 +183,17 @@ def profile_case():
     s0.geometry_shadow()
     s0.scattering()
     sh, il = s0.shadow(), s0.illumination()
-    s1 = lib.Solve(ctx, prob, precision=lib.FAST)
-    s1.set_forcing(sh, il)
-    for s, ti in ((s0, 200.0), (s1, 800.0)):
-        s.set_thermal_inertia(ti)
+    solves = [s0]
+    for _ in range(nsolves - 1):
+        s1 = lib.Solve(ctx, prob, precision=lib.FAST)
+        s1.set_forcing(sh, il)
+        solves.append(s1)
+    tis = [200.0, 800.0] if nsolves == 2 else workloads.BATCH_TI
+    for i, s in enumerate(solves):
+        s.set_thermal_inertia(tis[i % len(tis)])
         s.initialise_temperatures()
     for _ in range(3):
-        k = lib.profile_revolution([s0, s1])
+        k = lib.profile_revolution(solves)
     tiles, lo = _tile_stats(prob)
     print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz, "tiles": tiles, "lo_tiles": lo}))
 
@@ -230,6 +235,7 @@ def main():
     ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving run (1/s)")
+    ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: binary 5120+1280 facets, 2 solves, 3 instrumented revolutions")
     args = ap.parse_args()
@@ -237,7 +243,7 @@ def main():
         print(prepare())
         return
     if args.profile_case:
-        profile_case()
+        profile_case(args.profile_solves)
         return
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
@@ -450,31 +456,37 @@ def accuracy(ctx, prob, tis, shadow, illum):
             "schedule": f"{ACC_REVS} revolutions, every facet advancing (freeze off), same forcing"}
 
 
-def _tile_stats(prob):
+def _tile_stats(prob, slices=False):
     """Tile structure of the FAST tensor-core product: 128x64 tiles touched,
-    and how many of them carry the residual (a view factor >= 1e-4)."""
+    how many of them carry the residual (a view factor >= 1e-4), and with
+    ``slices`` the 128x16 K slices holding an entry (all tiles; residual
+    tiles): the products the kernel issues."""
     rows = np.repeat(np.arange(prob.nf), np.diff(prob.dep_ptr))
     key = (rows // 128).astype(np.int64) * ((prob.nf + 63) // 64) + prob.dep_idx // 64
     u, inv = np.unique(key, return_inverse=True)
     vmax = np.zeros(len(u), np.float32)
     np.maximum.at(vmax, inv, np.abs(prob.dep_vf))
-    return len(u), int((vmax >= 1e-4).sum())
+    has_lo = vmax >= 1e-4
+    if not slices:
+        return len(u), int(has_lo.sum())
+    sk = np.unique(inv.astype(np.int64) * 4 + (prob.dep_idx % 64) // 16)
+    return len(u), int(has_lo.sum()), len(sk), int(has_lo[sk // 4].sum())
 
 
 def _roofline(kern, solves, prob, hbm, bf16, kind):
     """Dominant kernel of the revolution loop: the tensor-core self-heating
     product (k_spmm_tc).  Algorithmic FLOP per solve-revolution =
-    2 * nnz * NTAU (the list sum); executed = every 128x64 tile x step chunk x
-    (2 or 3 BF16 products for the hi/lo compensation).  The conduction sweep
+    2 * nnz * NTAU (the list sum); executed = every issued 128x16 K slice x
+    step chunk x (2 or 3 BF16 products for the hi/lo compensation).  The conduction sweep
     is reported beside it: 20 B algorithmic HBM per facet-step."""
     out = {}
     k = kern.get("selfheat_q")
     n = len(solves)
     if k and k["ms"]:
         flops = 2.0 * prob.nnz * prob.ntau * n
-        tiles, lo = _tile_stats(prob)
+        tiles, lo, sl, sl_lo = _tile_stats(prob, slices=True)
         ntau_pad = -(-prob.ntau // 144) * 144 if prob.ntau > 160 else -(-prob.ntau // 16) * 16
-        exe = (2 * tiles + lo) * 128.0 * 64 * ntau_pad * 2 * n
+        exe = (2 * sl + sl_lo) * 128.0 * 16 * ntau_pad * 2 * n
         traffic = None
         tf = ROOT / "profiles" / "spmm_tc_traffic.json"
         if tf.exists():
@@ -484,8 +496,9 @@ def _roofline(kern, solves, prob, hbm, bf16, kind):
         out = {"kernel": "k_spmm_tc", "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
                "frac": ach / bf16, "peak_kind": kind, "traffic": traffic, "algorithmic_flop": flops,
                "executed_tflops": exe / (k["ms"] / 1e3) / 1e12, "executed_frac": exe / (k["ms"] / 1e3) / 1e12 / bf16,
-               "note": "algorithmic = 2 nnz NTAU; executed counts the zero padding of the 128x64 BF16 tiles "
-                       f"({tiles} tiles, {lo} with residual) and the hi/lo products"}
+               "note": "algorithmic = 2 nnz NTAU; executed counts the zero padding of the issued 128x16 K "
+                       f"slices ({sl} of the {4 * tiles} in {tiles} tiles; {sl_lo} in the {lo} tiles with "
+                       "residual) and the hi/lo products"}
     c = kern.get("conduction")
     if c and c["ms"]:
         nx = solves[0].nx

@@ -308,12 +308,17 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     int N, nch;
     tc_chunks(ntau, &N, &nch);
     const size_t ncell = (size_t)nmb * nkb;
+    if (nkb >= (1 << 24)) return fail(ATPM_E_UNSUPPORTED, "tensor-core tiles: %d facets exceed the column-block index", nf);
     std::vector<float> vm(ncell, -1.0f);
+    std::vector<uint8_t> km(ncell, 0);  // which 16-wide K slices of the tile hold an entry
     for (int f = 0; f < nf; ++f) {
         float* row = vm.data() + (size_t)(f / 128) * nkb;
+        uint8_t* mrow = km.data() + (size_t)(f / 128) * nkb;
         for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
-            float& c = row[sh->dep_idx[k] / 64];
+            const int g = sh->dep_idx[k];
+            float& c = row[g / 64];
             c = std::max(c, std::fabs(sh->dep_vf[k]));
+            mrow[g / 64] |= (uint8_t)(1u << ((g % 64) / 16));
         }
     }
     std::vector<int> tptr(nmb + 1, 0), tcol, slot(ncell, -1), lo_of;
@@ -323,7 +328,8 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
             const float v = vm[(size_t)mb * nkb + kb];
             if (v < 0.0f) continue;
             slot[(size_t)mb * nkb + kb] = (int)tcol.size();
-            tcol.push_back(kb);
+            // column block in the low 24 bits, K-slice mask in bits 24-27
+            tcol.push_back(kb | ((int)km[(size_t)mb * nkb + kb] << 24));
             // residual tile V - bf16(V) where the tile holds a view factor >= 1e-4
             lo_of.push_back(v >= 1e-4f ? nlo++ : -1);
         }

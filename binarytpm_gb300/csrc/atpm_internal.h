@@ -111,7 +111,8 @@ struct DevSolve {
     double es_w_d;
     // FAST precision, tensor-core self-heating (atpm_spmm_tc.cu); null when off
     const int* tc_ptr;       // [nmb+1] tile range of each 128-facet row block
-    const int* tc_col;       // [ntiles] 64-facet column block of each tile
+    const int* tc_col;       // [ntiles] 64-facet column block of each tile (bits 0-23), mask of its
+                             // 16-wide K slices that hold an entry (bits 24-27)
     const void* tc_tiles;    // [ntiles][128*64] BF16, swizzled K-major
     const int* tc_lo;        // [ntiles] index into tc_lo_tiles, or -1
     const void* tc_lo_tiles; // [nlo][128*64] BF16 residual V - bf16(V) of tiles with large entries

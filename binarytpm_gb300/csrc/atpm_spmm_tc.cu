@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
             const int st = i % S;
             if (i >= S && !mbar_wait(&empty[st], (uint32_t)((i / S) - 1) & 1u)) { ok = false; break; }
             unsigned char* sa = base + (size_t)st * stage_bytes;
-            const int kb = sv.tc_col[t0 + i];
+            const int kb = sv.tc_col[t0 + i] & 0xffffff;
             const int lo = sv.tc_lo[t0 + i];
             mbar_expect_tx(&full[st], a_bytes + (lo >= 0 ? a_bytes : 0u) + b_bytes);
             bulk_g2s(sa, tiles + (size_t)(t0 + i) * (TC_M * TC_K), a_bytes, &full[st]);
@@ -295,6 +295,7 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
         if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);
     } else if (threadIdx.x == 32) {
         const uint32_t idesc = idesc_bf16(N);
+        uint32_t acc = 0u;  // the first product issued overwrites the accumulator
         bool ok = true;
         for (int i = 0; i < T; ++i) {
             const int st = i % S;
@@ -304,11 +305,16 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
             const uint64_t ad = sw128_desc(sa), al = sw128_desc(sa + a_bytes);
             const uint64_t bh = sw128_desc(sa + 2 * a_bytes), bl = sw128_desc(sa + 2 * a_bytes + b_bytes / 2);
             const bool has_lo = sv.tc_lo[t0 + i] >= 0;
+            // K slices without an entry are zero in both A tiles: their
+            // products would add exact zeros, so they are not issued
+            const uint32_t kmask = (uint32_t)sv.tc_col[t0 + i] >> 24;
 #pragma unroll
             for (int k = 0; k < TC_K / 16; ++k) {
-                tc_mma(tmem, ad + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, (i | k) != 0);
+                if (!((kmask >> k) & 1u)) continue;
+                tc_mma(tmem, ad + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, acc);
                 tc_mma(tmem, ad + (uint64_t)(2 * k), bl + (uint64_t)(2 * k), idesc, 1u);
                 if (has_lo) tc_mma(tmem, al + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, 1u);
+                acc = 1u;
             }
             tc_commit(&empty[st]);
         }
