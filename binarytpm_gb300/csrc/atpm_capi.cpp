@@ -1154,6 +1154,14 @@ ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp
     return get_transposed<float>(s, s->ds.stemp1, s->P.ntau, s->nf, nullptr, stemp1);
 }
 
+ATPM_API atpm_status atpm_get_converged(atpm_solve* s, uint8_t* out) {
+    if (!s || !out) return fail(ATPM_E_INVALID, "null argument");
+    CK(cudaSetDevice(s->ctx->device));
+    CK(cudaMemcpyAsync(out, s->ds.conv, (size_t)s->nf, cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp) {
     if (!s || !temp) return fail(ATPM_E_INVALID, "null argument");
     CK(cudaSetDevice(s->ctx->device));

@@ -257,6 +257,19 @@ __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float 
 //    is still >= TACC/10), and the update of nodes 2..NX-1 -- independent of
 //    the boundary result -- sits in the same basic block, so the scheduler
 //    overlaps it with the Newton dependency chain.
+// per-thread asynchronous copies (cp.async, 4 bytes) for the step prefetch of
+// the FAST sweep: each thread copies and later reads only its own words, so
+// no block barrier is involved
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int kFastPrefetch = 8;  // steps of forcing / flux / previous temperature in flight per facet
+
 template <int NX>
 __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f) {
     const int nf = sv.nf, ntau = sv.ntau;
@@ -282,15 +295,27 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     bool hot = false;
     int flags = 0;
     const int cap = sv.newton_cap;
-    size_t o = (size_t)f;
-    float e_n = E[o], q_n = Q[o], old_n = S1[o];
-    for (int s = 0; s < ntau; ++s, o += nf) {
-        const float e = e_n, q = q_n, old = old_n;
-        if (s + 1 < ntau) {
-            e_n = E[o + nf];
-            q_n = Q[o + nf];
-            old_n = S1[o + nf];
+    // E, Q and the previous temperature of step s + kFastPrefetch are copied
+    // into this thread's shared-memory slots while step s computes: in the
+    // late revolutions a few active facets per SM cannot hide DRAM latency
+    // behind other warps
+    constexpr int D = kFastPrefetch;
+    __shared__ float pre[D][3][128];
+    const int lt = threadIdx.x;
+    for (int j = 0; j < D; ++j) {
+        if (j < ntau) {
+            const size_t oj = (size_t)j * nf + f;
+            cp_async4(&pre[j][0][lt], E + oj);
+            cp_async4(&pre[j][1][lt], Q + oj);
+            cp_async4(&pre[j][2][lt], S1 + oj);
         }
+        cp_async_commit();
+    }
+    size_t o = (size_t)f;
+    int slot = 0;
+    for (int s = 0; s < ntau; ++s, o += nf) {
+        cp_async_wait<D - 1>();  // the copies of step s have landed
+        const float e = pre[slot][0][lt], q = pre[slot][1][lt], old = pre[slot][2][lt];
         S0[o] = old;
         const float t1 = T[1];
         T[1] = fmaf(r, (T[2] + T[0]) - 2.0f * t1, t1);
@@ -346,7 +371,17 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         }
         T[NX] = T[NX - 1];
         hot = hot || (fabsf(Tsurf - old) >= tacc);
+        // refill the slot just read (its words are consumed) with step s + D
+        if (s + D < ntau) {
+            const size_t od = o + (size_t)D * nf;
+            cp_async4(&pre[slot][0][lt], E + od);
+            cp_async4(&pre[slot][1][lt], Q + od);
+            cp_async4(&pre[slot][2][lt], S1 + od);
+        }
+        cp_async_commit();
+        if (++slot == D) slot = 0;
     }
+    cp_async_wait<0>();
     if (!isfinite(T[0] + Tref)) flags |= ST_NONFINITE;
 #pragma unroll
     for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = Tref + T[i];

@@ -64,6 +64,7 @@ _SIGS = {
     "atpm_get_surface_temperature": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_surface_temperature64": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_get_converged": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_orbital_position": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_void_p]),
@@ -282,6 +283,12 @@ class Solve:
         s1 = np.zeros((self.nf, self.ntau), np.float64)
         _ck(load().atpm_get_surface_temperature64(self.h, _p(s1)))
         return s1
+
+    def converged(self) -> np.ndarray:
+        """Per-facet convergence flags after the last revolution (bool [nf])."""
+        out = np.zeros(self.nf, np.uint8)
+        _ck(load().atpm_get_converged(self.h, _p(out)))
+        return out.astype(bool)
 
     def depth_temperature(self):
         t = np.zeros((self.nf, self.nx + 1), np.float32)

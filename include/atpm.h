@@ -149,6 +149,10 @@ ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp
 ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp /* [nf][nx+1] */);
 /* (float)cos of the Sun angle of every facet and step ([nf][ntau]). */
 ATPM_API atpm_status atpm_get_cosillum(atpm_solve* s, float* out);
+/* Per-facet convergence flags after the last revolution, 1 = converged (and
+ * frozen when the solve freezes): the facet property _astconverged
+ * (3905/Thermal/NominalPole/main.cpp:193, 303). */
+ATPM_API atpm_status atpm_get_converged(atpm_solve* s, uint8_t* out /* [nf] */);
 /* One revolution of the given (active) solves with a CUDA event between
  * kernels: kernel_ms[5] = self-heating W, self-heating Q, conduction,
  * convergence, advance.  Advances the solves by one revolution. */

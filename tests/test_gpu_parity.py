@@ -36,6 +36,8 @@ def test_reference_mode_bit_exact(gpu_ctx, name):
     assert np.array_equal(s.depth_temperature().view(np.uint32), ref["temp"].view(np.uint32))
     for got, want in zip(counts, ref["counts_list"]):
         assert np.array_equal(got, want)
+    # per-facet flags after the last revolution agree with its count
+    assert int(s.converged().sum()) == int(counts[-1][-1])
 
 
 def test_visibility_all_pairs_bit_exact(gpu_ctx):
