@@ -131,7 +131,7 @@ struct Layout {
 
 enum {
     B_VERT, B_FAC, B_DPTR, B_DIDX, B_DVF, B_SHADOW, B_COS, B_EFM, B_E, B_S0, B_S1, B_TEMP, B_Q, B_W,
-    B_CONV, B_HOT, B_COUNTS, B_STATUS, B_CTL, B_DIAG, B_MEAN, B_N
+    B_CONV, B_HOT, B_COUNTS, B_STATUS, B_CTL, B_DIAG, B_ACT, B_MEAN, B_N
 };
 
 Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
@@ -158,6 +158,7 @@ Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
     sz[B_STATUS] = 4;
     sz[B_CTL] = sizeof(Ctl);
     sz[B_DIAG] = 4 * 8;
+    sz[B_ACT] = ((size_t)2 * nf + 4) * 4;
     sz[B_MEAN] = (size_t)nf * rs;
     Layout L;
     size_t o = 0;
@@ -270,6 +271,11 @@ bool autotune_enabled() {
 
 bool shadow_cull_enabled() {
     const char* e = std::getenv("ATPM_SHADOW_CULL");
+    return !(e && e[0] == '0');
+}
+
+bool warp_tail_enabled() {
+    const char* e = std::getenv("ATPM_WARP_TAIL");
     return !(e && e[0] == '0');
 }
 
@@ -396,6 +402,11 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.tc_nmax = 0;
     b.cond_variant = cond_variant();
     b.tc_stages = 0;
+    b.warp_tail = warp_tail_enabled() ? 1 : 0;
+    // active facets of the whole batch up to which a revolution runs warp per
+    // facet: about a dozen warps per SM, where one warp per facet still beats
+    // the thread-per-facet sweep's latency-bound last warps
+    b.tail_limit = 12 * ctx->sm_count;
     return b;
 }
 
@@ -686,8 +697,11 @@ ATPM_API atpm_status atpm_context_create(int32_t device, atpm_context** out) {
     CK(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) return fail(ATPM_E_INVALID, "device %d of %d", device, n);
     CK(cudaSetDevice(device));
+    int sms = 1;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     auto* c = new atpm_context();
     c->device = device;
+    c->sm_count = sms;
     *out = c;
     return ATPM_OK;
 }
@@ -766,6 +780,8 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     d.status = reinterpret_cast<int*>(a + L.off[B_STATUS]);
     d.ctl = reinterpret_cast<Ctl*>(a + L.off[B_CTL]);
     d.diag = reinterpret_cast<double*>(a + L.off[B_DIAG]);
+    d.act_list = reinterpret_cast<int*>(a + L.off[B_ACT]);
+    d.act_cnt = d.act_list + (size_t)2 * s->nf;
     set_scalars(s, 0.0f);
     s->vert_h.assign(sh->vertices, sh->vertices + 3 * (size_t)s->nv);
     s->fac_h.assign(sh->facets, sh->facets + 3 * (size_t)s->nf);
@@ -924,6 +940,13 @@ ATPM_API atpm_status atpm_set_forcing(atpm_solve* s, const int32_t* shadow, cons
     return ATPM_OK;
 }
 
+// no active-facet list is valid (counts 0, built for revolution -1)
+cudaError_t reset_active_lists(atpm_solve* s) {
+    cudaError_t e = cudaMemsetAsync(s->ds.act_cnt, 0, 2 * sizeof(int), s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->ds.act_cnt + 2, 0xff, 2 * sizeof(int), s->st);
+    return e;
+}
+
 ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
     if (!s) return fail(ATPM_E_INVALID, "null solve");
     if (!(ti >= 0.0f) || !std::isfinite(ti)) return fail(ATPM_E_INVALID, "thermal inertia %g", (double)ti);
@@ -942,6 +965,7 @@ ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
     CK(cudaMemsetAsync(s->ds.conv, 0, s->nf, s->st));
     CK(cudaMemsetAsync(s->ds.hot, 0, s->nf, s->st));
     CK(cudaMemsetAsync(s->ds.counts, 0, (size_t)s->P.revcap * 4, s->st));
+    CK(reset_active_lists(s));
     CK(cudaStreamSynchronize(s->st));
     return ATPM_OK;
 }
@@ -977,6 +1001,7 @@ ATPM_API atpm_status atpm_revolution(atpm_solve* s, int32_t rev, int32_t* numcon
     c.rev = rev;
     c.active = 1;
     CK(cudaMemcpyAsync(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
+    CK(reset_active_lists(s));  // the caller chooses the revolution: no list carries over
     Batch b = make_batch(s->ctx, s->ds_dev, 1, s->wmap, s->nw, s->fmap, s->nfb, s->P.precision, s->P.nx);
     if (launch_revolution(b, s->st)) return fail(ATPM_E_CUDA, "revolution launch");
     int st = 0;

@@ -21,6 +21,7 @@ struct atpm_tune_choice {
 
 struct atpm_context {
     int device = 0;
+    int sm_count = 1;
     std::mutex mu;
     bool tables = false;
     atpm::HostPowTab p4, p3;

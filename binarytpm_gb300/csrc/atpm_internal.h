@@ -92,6 +92,11 @@ struct DevSolve {
     void* W;                 // [nf][ntau] R
     uint8_t* conv;           // [nf] frozen (reference astconverged)
     uint8_t* hot;            // [nf] some |stemp1-stemp0| >= TACC this revolution
+    // facets still active after each convergence test (FAST, freeze on),
+    // double-buffered by revolution parity: k_converge of revolution r fills
+    // list (r+1)&1, the conduction of r+1 reads it, k_advance of r+1 clears it
+    int* act_list;           // [2][nf]
+    int* act_cnt;            // [4]: counts of the two lists, then the revolution each list is for
     int* counts;             // [revcap] numconverged after each revolution
     int* status;             // ST_* bits
     Ctl* ctl;
@@ -175,6 +180,8 @@ struct Batch {
     int tc_nmax;             // largest step chunk in the batch
     int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
     int tc_stages;           // tensor-core pipeline depth (0: deepest that fits)
+    int warp_tail;           // 1: revolutions with few active facets run warp-per-facet (FAST)
+    int tail_limit;          // active facets of the batch up to which they do
 };
 // deepest tensor-core pipeline that fits shared memory for step chunk N
 int tc_max_stages(int N);

@@ -270,6 +270,22 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 constexpr int kFastPrefetch = 8;  // steps of forcing / flux / previous temperature in flight per facet
 
+// One FTCS node update and one Newton step of the FAST sweep, shared by the
+// thread-per-facet and the warp-per-facet forms so both round alike.
+__device__ __forceinline__ float ftcs_node(float r, float up, float dn, float t) {
+    return fmaf(r, (up + dn) - 2.0f * t, t);
+}
+__device__ __forceinline__ float newton_fast(float th, float Tref, float t1, float a, float m1, float es, float es4,
+                                             float& DT) {
+    const float TR = Tref + th;
+    const float t2 = TR * TR;
+    const float sbc = fmaf(m1, t1 - th, a) - es * (t2 * t2);
+    const float sbcd = fmaf(es4, t2 * TR, m1);
+    const float th1 = th + __fdividef(sbc, sbcd);
+    DT = fabsf(th1 - th);
+    return th1;
+}
+
 template <int NX>
 __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f) {
     const int nf = sv.nf, ntau = sv.ntau;
@@ -318,43 +334,24 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         const float e = pre[slot][0][lt], q = pre[slot][1][lt], old = pre[slot][2][lt];
         S0[o] = old;
         const float t1 = T[1];
-        T[1] = fmaf(r, (T[2] + T[0]) - 2.0f * t1, t1);
+        T[1] = ftcs_node(r, T[2], T[0], t1);
         const float a = fmaf(oma, e, q);
         // Newton iterations 1 and 2 on theta_0 (T_0 = Tref + theta_0)
-        float th = T[0];
-        float TR = Tref + th;
-        float t2 = TR * TR;
-        float sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
-        float sbcd = fmaf(es4, t2 * TR, m1);
-        float th1 = th + __fdividef(sbc, sbcd);
-        float DT = fabsf(th1 - th);
-        if (DT >= tacc10) {
-            th = th1;
-            TR = Tref + th;
-            t2 = TR * TR;
-            sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
-            sbcd = fmaf(es4, t2 * TR, m1);
-            th1 = th + __fdividef(sbc, sbcd);
-            DT = fabsf(th1 - th);
-        }
+        float DT;
+        float th1 = newton_fast(T[0], Tref, T[1], a, m1, es, es4, DT);
+        if (DT >= tacc10) th1 = newton_fast(th1, Tref, T[1], a, m1, es, es4, DT);
         // remaining nodes (independent of the boundary result)
         float tm = t1;
 #pragma unroll
         for (int i = 2; i < NX; ++i) {
             const float ti = T[i];
-            T[i] = fmaf(r, (T[i + 1] + tm) - 2.0f * ti, ti);
+            T[i] = ftcs_node(r, T[i + 1], tm, ti);
             tm = ti;
         }
         int it = 2;
         while (DT >= tacc10) {
             if (it >= cap) { flags |= ST_NEWTON_CAP; break; }
-            th = th1;
-            TR = Tref + th;
-            t2 = TR * TR;
-            sbc = fmaf(m1, T[1] - th, a) - es * (t2 * t2);
-            sbcd = fmaf(es4, t2 * TR, m1);
-            th1 = th + __fdividef(sbc, sbcd);
-            DT = fabsf(th1 - th);
+            th1 = newton_fast(th1, Tref, T[1], a, m1, es, es4, DT);
             ++it;
         }
         T[0] = th1;
@@ -387,6 +384,162 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = Tref + T[i];
     sv.hot[f] = hot ? 1 : 0;
     if (flags) atomicOr(sv.status, flags);
+}
+
+// FAST, late revolutions: one warp per active facet.  Lane l holds depth
+// nodes 2l and 2l+1 (theta offsets, as above); each step exchanges the two
+// neighbours by shuffles, and every lane runs the same Newton boundary solve
+// on the broadcast node 1, so the arithmetic is that of
+// column_revolution_fast step for step.  Forcing, flux and the previous
+// temperature come in blocks of 32 steps (lane j holds step s0 + j, the next
+// block loading while this one runs); the step's outputs collect in the lane
+// of that step and are stored once per block.
+constexpr int kWarpNodes = 64;  // nodes 0..NX a warp can hold
+
+template <int NX>
+__device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f) {
+    static_assert(NX + 1 <= kWarpNodes, "two nodes per lane");
+    constexpr unsigned FULL = 0xffffffffu;
+    const int nf = sv.nf, ntau = sv.ntau;
+    const int lane = threadIdx.x & 31;
+    const bool sec = f >= sv.fsplit;
+    const float r = sec ? sv.r2 : sv.r, oma = sv.oma, es = sv.es, es4 = sv.es4, m1 = sec ? sv.m1_2 : sv.m1,
+                tacc = sv.tacc, tacc10 = sv.tacc10;
+    float* temp = static_cast<float*>(sv.temp);
+    const float* __restrict__ E = static_cast<const float*>(sv.E);
+    const float* __restrict__ Q = static_cast<const float*>(sv.Q);
+    float* __restrict__ S0 = static_cast<float*>(sv.stemp0);
+    float* __restrict__ S1 = static_cast<float*>(sv.stemp1);
+    __nv_bfloat16* Wb = static_cast<__nv_bfloat16*>(sv.Wb);
+    const int N = sv.tc_n;
+    const int na = 2 * lane, nb = 2 * lane + 1;
+    const float Tref = temp[(size_t)NX * nf + f];
+    float Ta = na <= NX ? temp[(size_t)na * nf + f] - Tref : 0.0f;
+    float Tb = nb <= NX ? temp[(size_t)nb * nf + f] - Tref : 0.0f;
+    bool hot = false;
+    int flags = 0;
+    const int cap = sv.newton_cap;
+    float th1 = 0.0f;
+    float ce = 0.0f, cq = 0.0f, co = 0.0f;
+    if (lane < ntau) {
+        const size_t o = (size_t)lane * nf + f;
+        ce = E[o];
+        cq = Q[o];
+        co = S1[o];
+    }
+    for (int s0 = 0; s0 < ntau; s0 += 32) {
+        float ne = 0.0f, nq = 0.0f, no = 0.0f;
+        if (s0 + 32 + lane < ntau) {
+            const size_t o = (size_t)(s0 + 32 + lane) * nf + f;
+            ne = E[o];
+            nq = Q[o];
+            no = S1[o];
+        }
+        float ts = 0.0f;
+        const int nstep = min(32, ntau - s0);
+        for (int j = 0; j < nstep; ++j) {
+            const float e = __shfl_sync(FULL, ce, j), q = __shfl_sync(FULL, cq, j), old = __shfl_sync(FULL, co, j);
+            const float lft = __shfl_up_sync(FULL, Tb, 1);    // node na - 1
+            const float rgt = __shfl_down_sync(FULL, Ta, 1);  // node nb + 1
+            const float th = __shfl_sync(FULL, Ta, 0);        // node 0 (old)
+            float Ta_n = Ta, Tb_n = Tb;
+            if (na >= 1 && na <= NX - 1) Ta_n = ftcs_node(r, Tb, lft, Ta);
+            if (nb <= NX - 1) Tb_n = ftcs_node(r, rgt, Ta, Tb);
+            const float t1n = __shfl_sync(FULL, Tb_n, 0);     // node 1 (new)
+            const float a = fmaf(oma, e, q);
+            float DT;
+            th1 = newton_fast(th, Tref, t1n, a, m1, es, es4, DT);
+            if (DT >= tacc10) th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
+            int it = 2;
+            while (DT >= tacc10) {
+                if (it >= cap) { flags |= ST_NEWTON_CAP; break; }
+                th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
+                ++it;
+            }
+            if (lane == 0) Ta_n = th1;
+            // bottom node: T[NX] = T[NX - 1] (new)
+            const float bot = __shfl_sync(FULL, ((NX - 1) & 1) ? Tb_n : Ta_n, (NX - 1) >> 1);
+            if (lane == (NX >> 1)) {
+                if (NX & 1) Tb_n = bot;
+                else Ta_n = bot;
+            }
+            Ta = Ta_n;
+            Tb = Tb_n;
+            const float Tsurf = Tref + th1;
+            if (lane == j) ts = Tsurf;
+            hot = hot || (fabsf(Tsurf - old) >= tacc);
+        }
+        if (lane < nstep) {
+            const int s = s0 + lane;
+            const size_t o = (size_t)s * nf + f;
+            S0[o] = co;
+            S1[o] = ts;
+            if (Wb) {
+                const float t2s = ts * ts;
+                const float w = sv.es_w * (t2s * t2s);
+                const size_t base = ((size_t)(f >> 6) * sv.tc_nchunks + s / N) * (size_t)2 * N * 64;
+                const uint32_t off = swz((uint32_t)(s % N), (uint32_t)(f & 63));
+                const __nv_bfloat16 hi = __float2bfloat16_rn(w);
+                Wb[base + off] = hi;
+                Wb[base + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
+            }
+        }
+        ce = ne;
+        cq = nq;
+        co = no;
+    }
+    if (!isfinite(th1 + Tref)) flags |= ST_NONFINITE;
+    if (na <= NX) temp[(size_t)na * nf + f] = Tref + Ta;
+    if (nb <= NX) temp[(size_t)nb * nf + f] = Tref + Tb;
+    if (lane == 0) {
+        sv.hot[f] = hot ? 1 : 0;
+        if (flags) atomicOr(sv.status, flags);
+    }
+}
+
+// A revolution of the batch runs warp per facet when every active solve with
+// a depth sweep (TI > 0) freezes converged facets, fits a warp's nodes and
+// has the list of its active facets built for this revolution, and those
+// lists hold at most b.tail_limit facets together.  Both conduction kernels
+// evaluate the same rule on the same words, so exactly one of them advances
+// each facet.
+constexpr int kSparseCtas = 128;  // CTAs (4 warps each) per solve
+__device__ __forceinline__ bool warp_tail_revolution(const Batch& b) {
+    if (!b.warp_tail) return false;
+    int total = 0;
+    for (int i = 0; i < b.n; ++i) {
+        const DevSolve& s = b.tab[i];
+        if (!s.ctl->active || s.ti == 0.0f) continue;
+        const int rev = s.ctl->rev;
+        if (!s.freeze || s.nx + 1 > kWarpNodes || rev < 7 || s.act_cnt[2 + (rev & 1)] != rev) return false;
+        total += s.act_cnt[rev & 1];
+    }
+    return total <= b.tail_limit;
+}
+
+// one thread decides for the CTA
+__device__ __forceinline__ bool cta_warp_tail(const Batch& b) {
+    __shared__ int flag;
+    if (threadIdx.x == 0) flag = warp_tail_revolution(b) ? 1 : 0;
+    __syncthreads();
+    return flag != 0;
+}
+
+template <int NX>
+__global__ void __launch_bounds__(128) k_conduction_warp(Batch b) {
+    const int si = blockIdx.x / kSparseCtas;
+    if (si >= b.n || !b.warp_tail) return;
+    const DevSolve& sv = b.tab[si];
+    if (!sv.ctl->active || sv.ti == 0.0f) return;
+    const int rev = sv.ctl->rev;
+    if (rev < 7 || sv.act_cnt[2 + (rev & 1)] != rev || sv.act_cnt[rev & 1] == 0) return;
+    if (!cta_warp_tail(b)) return;
+    if constexpr (NX + 1 <= kWarpNodes) {
+        const int n = sv.act_cnt[rev & 1];
+        const int* list = sv.act_list + (size_t)(rev & 1) * sv.nf;
+        for (int k = (blockIdx.x % kSparseCtas) * 4 + (threadIdx.x >> 5); k < n; k += 4 * kSparseCtas)
+            column_revolution_warp<NX>(sv, list[k]);
+    }
 }
 
 // instequilibrium (main.cpp:1563-1612): every facet, every step, no depth
@@ -427,12 +580,17 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     const int2 fb = b.fmap[blockIdx.x];
     const DevSolve& sv = b.tab[fb.x];
     if (!sv.ctl->active) return;
+    if constexpr (MODE == MODE_FAST) {
+        if (sv.ti != 0.0f && cta_warp_tail(b)) return;  // k_conduction_warp runs this revolution
+    }
     const int f = fb.y + threadIdx.x;
     if (f >= sv.nf) return;
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
     if (inst) { column_equilibrium<MODE>(sv, b, f); return; }
     if (sv.freeze && sv.conv[f]) return;
-    if constexpr (MODE == MODE_FAST) column_revolution_fast<NX>(sv, f);
+    if constexpr (MODE == MODE_FAST) {
+        column_revolution_fast<NX>(sv, f);
+    }
     else column_revolution<MODE, NX>(sv, b, f);
 }
 
@@ -451,6 +609,17 @@ __global__ void __launch_bounds__(128) k_converge(Batch b) {
     }
     c = __syncthreads_count(c);
     if (threadIdx.x == 0 && c) atomicAdd(&sv.counts[rev], c);
+    // list of the facets still active for the next revolution (FAST, freeze)
+    if (b.mode == MODE_FAST && sv.freeze) {
+        const bool act = f < sv.nf && !sv.conv[f];
+        const unsigned m = __ballot_sync(0xffffffffu, act);
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (fb.y == 0 && threadIdx.x == 0) sv.act_cnt[2 + ((rev + 1) & 1)] = rev + 1;
+        if (lane == 0 && m) base = atomicAdd(&sv.act_cnt[(rev + 1) & 1], __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (act) sv.act_list[(size_t)((rev + 1) & 1) * sv.nf + base + __popc(m & ((1u << lane) - 1u))] = f;
+    }
 }
 
 __global__ void k_advance(Batch b) {
@@ -467,6 +636,9 @@ __global__ void k_advance(Batch b) {
     } else {
         sv.counts[rev] = ctl->numconv;
     }
+    // read by this revolution's conduction; k_converge of rev + 1 refills it
+    sv.act_cnt[rev & 1] = 0;
+    sv.act_cnt[2 + (rev & 1)] = -1;
     ctl->rev = rev + 1;
     if (ctl->converged || rev + 1 >= sv.revcap || (*sv.status & ST_NONFINITE)) ctl->active = 0;
 }
@@ -575,6 +747,15 @@ static int launch_rev_part(const Batch& b, int part, cudaStream_t st) {
             } else {
                 switch (b.nx) {
 #define NX_CASE(n) case n: k_conduction<MODE, n><<<b.nfb, 128, 0, st>>>(b); break;
+                    NX_LIST(NX_CASE)
+#undef NX_CASE
+                    default: return 1;
+                }
+            }
+            if (MODE == MODE_FAST) {
+                const int wgrid = b.n * kSparseCtas;
+                switch (b.nx) {
+#define NX_CASE(n) case n: k_conduction_warp<n><<<wgrid, 128, 0, st>>>(b); break;
                     NX_LIST(NX_CASE)
 #undef NX_CASE
                     default: return 1;
