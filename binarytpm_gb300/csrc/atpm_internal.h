@@ -180,7 +180,8 @@ struct Batch {
     int tc_nmax;             // largest step chunk in the batch
     int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
     int tc_stages;           // tensor-core pipeline depth (0: deepest that fits)
-    int warp_tail;           // 1: revolutions with few active facets run warp-per-facet (FAST)
+    int warp_tail;           // 1: FAST revolutions with few active facets sweep the active list
+                             // (thread per facet; warp per facet below tail_limit)
     int tail_limit;          // active facets of the batch up to which they do
 };
 // deepest tensor-core pipeline that fits shared memory for step chunk N

@@ -581,7 +581,20 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     const DevSolve& sv = b.tab[fb.x];
     if (!sv.ctl->active) return;
     if constexpr (MODE == MODE_FAST) {
-        if (sv.ti != 0.0f && cta_warp_tail(b)) return;  // k_conduction_warp runs this revolution
+        if (sv.ti != 0.0f) {
+            if (cta_warp_tail(b)) return;  // k_conduction_warp runs this revolution
+            // at most half the facets active: the solve's blocks sweep its
+            // list of active facets instead of its facet range, so active
+            // facets fill whole warps and the remaining blocks exit
+            const int rev = sv.ctl->rev;
+            if (b.warp_tail && sv.freeze && rev >= 7 && sv.act_cnt[2 + (rev & 1)] == rev &&
+                2 * sv.act_cnt[rev & 1] <= sv.nf) {
+                const int k = fb.y + threadIdx.x;
+                if (k >= sv.act_cnt[rev & 1]) return;
+                column_revolution_fast<NX>(sv, sv.act_list[(size_t)(rev & 1) * sv.nf + k]);
+                return;
+            }
+        }
     }
     const int f = fb.y + threadIdx.x;
     if (f >= sv.nf) return;
@@ -609,16 +622,25 @@ __global__ void __launch_bounds__(128) k_converge(Batch b) {
     }
     c = __syncthreads_count(c);
     if (threadIdx.x == 0 && c) atomicAdd(&sv.counts[rev], c);
-    // list of the facets still active for the next revolution (FAST, freeze)
+    // list of the facets still active for the next revolution (FAST, freeze):
+    // each block appends its active facets as one segment in facet order, so
+    // a sweep over the list keeps runs of neighbouring facets together
     if (b.mode == MODE_FAST && sv.freeze) {
+        __shared__ int wcnt[4], base;
         const bool act = f < sv.nf && !sv.conv[f];
         const unsigned m = __ballot_sync(0xffffffffu, act);
-        const int lane = threadIdx.x & 31;
-        int base = 0;
-        if (fb.y == 0 && threadIdx.x == 0) sv.act_cnt[2 + ((rev + 1) & 1)] = rev + 1;
-        if (lane == 0 && m) base = atomicAdd(&sv.act_cnt[(rev + 1) & 1], __popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (act) sv.act_list[(size_t)((rev + 1) & 1) * sv.nf + base + __popc(m & ((1u << lane) - 1u))] = f;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) wcnt[warp] = __popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int t = wcnt[0] + wcnt[1] + wcnt[2] + wcnt[3];
+            base = t ? atomicAdd(&sv.act_cnt[(rev + 1) & 1], t) : 0;
+            if (fb.y == 0) sv.act_cnt[2 + ((rev + 1) & 1)] = rev + 1;
+        }
+        __syncthreads();
+        int off = base;
+        for (int w = 0; w < warp; ++w) off += wcnt[w];
+        if (act) sv.act_list[(size_t)((rev + 1) & 1) * sv.nf + off + __popc(m & ((1u << lane) - 1u))] = f;
     }
 }
 

@@ -1,10 +1,12 @@
-"""FAST late revolutions: once few facets are still active, a revolution runs
-one warp per active facet (k_conduction_warp) instead of one thread per facet
-(k_conduction).  The two forms share their arithmetic, so temperatures, depth
-profiles and the per-revolution convergence counts are identical with the
-warp form on (the default) and off (ATPM_WARP_TAIL=0).  Each case is checked
-to have reached the warp form: some revolution from the 7th on started with
-at most 12 active facets per SM over the batch's running solves.
+"""FAST late revolutions: once at most half a solve's facets are active, its
+sweep runs over the list of active facets (thread per facet, whole warps of
+active facets), and once the batch has at most 12 active facets per SM, one
+warp per active facet (k_conduction_warp).  All forms share their arithmetic,
+so temperatures, depth profiles and the per-revolution convergence counts are
+identical with the list forms on (the default) and off (ATPM_WARP_TAIL=0: one
+thread per facet over every facet block).  Each case is checked to have
+reached the warp form: some revolution from the 7th on started with at most
+12 active facets per SM over the batch's running solves.
 """
 import dataclasses
 import os
