@@ -131,7 +131,7 @@ struct Layout {
 
 enum {
     B_VERT, B_FAC, B_DPTR, B_DIDX, B_DVF, B_SHADOW, B_COS, B_EFM, B_E, B_S0, B_S1, B_TEMP, B_Q, B_W,
-    B_CONV, B_HOT, B_COUNTS, B_STATUS, B_CTL, B_DIAG, B_ACT, B_MEAN, B_N
+    B_CONV, B_HOT, B_COUNTS, B_STATUS, B_CTL, B_DIAG, B_ACT, B_MEAN, B_RBACT, B_N
 };
 
 Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
@@ -160,6 +160,7 @@ Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
     sz[B_DIAG] = 4 * 8;
     sz[B_ACT] = ((size_t)2 * nf + 4) * 4;
     sz[B_MEAN] = (size_t)nf * rs;
+    sz[B_RBACT] = (size_t)(nf + 127) / 128;
     Layout L;
     size_t o = 0;
     for (int i = 0; i < B_N; ++i) {
@@ -295,12 +296,28 @@ void tc_chunks(int ntau, int* n, int* nch) {
     *nch = c;
 }
 
+// work items of the tensor-core product {solve, row block, step chunk, 0}
 void build_tc_maps(int nf, int ntau, int solve, std::vector<int4>& q) {
     int n, nch;
     tc_chunks(ntau, &n, &nch);
     const int nmb = (nf + 127) / 128;
     for (int mb = 0; mb < nmb; ++mb)
         for (int c = 0; c < nch; ++c) q.push_back(make_int4(solve, mb, c, 0));
+}
+
+// device layout of a batch's tensor-core map: the nq items, then room for the
+// per-launch list of active items (nq), then the two work counters
+size_t tc_map_entries(size_t nq) { return nq ? 2 * nq + 1 : 0; }
+void tc_map_extend(std::vector<int4>& q) {
+    const size_t nq = q.size();
+    if (nq) q.resize(tc_map_entries(nq), make_int4(0, 0, 0, 0));
+}
+void set_tc_map(Batch& b, const int4* dev_map, size_t entries) {
+    b.qmap = dev_map;
+    b.nq = entries ? (int)((entries - 1) / 2) : 0;
+    int4* w = const_cast<int4*>(dev_map);
+    b.tc_list = b.nq ? w + b.nq : nullptr;
+    b.tc_work = b.nq ? reinterpret_cast<int*>(w + 2 * (size_t)b.nq) : nullptr;
 }
 
 // block-sparse BF16 tiles of the view-factor matrix (128 x 64, swizzled)
@@ -377,9 +394,10 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     d.tc_nkb = nkb;
     std::vector<int4> q;
     build_tc_maps(nf, ntau, 0, q);
+    tc_map_extend(q);
     CK(cudaMalloc(&s->qmap, q.size() * sizeof(int4)));
     CK(cudaMemcpy(s->qmap, q.data(), q.size() * sizeof(int4), cudaMemcpyHostToDevice));
-    s->nq = (int)q.size();
+    s->nq = (int)q.size();  // map entries (items, list, counters)
     return ATPM_OK;
 }
 
@@ -399,6 +417,8 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.pq = view(ctx->pq);
     b.qmap = nullptr;
     b.nq = 0;
+    b.tc_list = nullptr;
+    b.tc_work = nullptr;
     b.tc_nmax = 0;
     b.cond_variant = cond_variant();
     b.tc_stages = 0;
@@ -407,6 +427,7 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     // facet: about a dozen warps per SM, where one warp per facet still beats
     // the thread-per-facet sweep's latency-bound last warps
     b.tail_limit = 12 * ctx->sm_count;
+    b.sms = ctx->sm_count;
     return b;
 }
 
@@ -417,8 +438,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
     *tmp = nullptr;
     if (n == 1) {
         *out = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
-        out->qmap = s0->qmap;
-        out->nq = s0->nq;
+        set_tc_map(*out, s0->qmap, (size_t)s0->nq);
         out->tc_nmax = s0->ds.tc_n;
         return ATPM_OK;
     }
@@ -438,6 +458,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
     }
     const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
     const size_t bf = align256(fm.size() * sizeof(int2));
+    tc_map_extend(qm);
     const size_t bq = align256(std::max<size_t>(qm.size(), 1) * sizeof(int4));
     CK(cudaMalloc(tmp, bt + bw + bf + bq));
     char* t = static_cast<char*>(*tmp);
@@ -447,8 +468,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
     if (!qm.empty()) CK(cudaMemcpy(t + bt + bw + bf, qm.data(), qm.size() * sizeof(int4), cudaMemcpyHostToDevice));
     *out = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + bt), (int)wm.size(),
                       reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
-    out->qmap = reinterpret_cast<int4*>(t + bt + bw + bf);
-    out->nq = (int)qm.size();
+    set_tc_map(*out, reinterpret_cast<int4*>(t + bt + bw + bf), qm.size());
     out->tc_nmax = nmax;
     return ATPM_OK;
 }
@@ -547,7 +567,7 @@ atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64
     b.cond_variant = ch.cond_variant;
     b.tc_stages = ch.tc_stages;
     *done_revs = 3;
-    *launches += 3 * (b.nw > 0 || b.nq > 0 ? 5 : 3);
+    *launches += 3 * kernels_per_revolution(b);
     *tuned = 1;
     return ATPM_OK;
 }
@@ -625,6 +645,7 @@ void host_table(atpm_solve* const* solves, int n, HostTable& h) {
     h.bt = align256(n * sizeof(DevSolve));
     h.bw = align256(std::max<size_t>(h.wm.size(), 1) * sizeof(int4));
     h.bf = align256(h.fm.size() * sizeof(int2));
+    tc_map_extend(h.qm);
     h.bq = align256(std::max<size_t>(h.qm.size(), 1) * sizeof(int4));
 }
 }  // namespace
@@ -648,8 +669,7 @@ atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cud
     atpm_solve* s0 = solves[0];
     Batch b = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + h.bt), (int)h.wm.size(),
                          reinterpret_cast<int2*>(t + h.bt + h.bw), (int)h.fm.size(), s0->P.precision, s0->P.nx);
-    b.qmap = reinterpret_cast<int4*>(t + h.bt + h.bw + h.bf);
-    b.nq = (int)h.qm.size();
+    set_tc_map(b, reinterpret_cast<int4*>(t + h.bt + h.bw + h.bf), h.qm.size());
     b.tc_nmax = h.nmax;
     for (int r = 0; r < k; ++r)
         if (launch_revolution(b, st)) return fail(ATPM_E_CUDA, "batched revolution launch");
@@ -782,6 +802,7 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     d.diag = reinterpret_cast<double*>(a + L.off[B_DIAG]);
     d.act_list = reinterpret_cast<int*>(a + L.off[B_ACT]);
     d.act_cnt = d.act_list + (size_t)2 * s->nf;
+    d.rb_act = reinterpret_cast<uint8_t*>(a + L.off[B_RBACT]);
     set_scalars(s, 0.0f);
     s->vert_h.assign(sh->vertices, sh->vertices + 3 * (size_t)s->nv);
     s->fac_h.assign(sh->facets, sh->facets + 3 * (size_t)s->nf);
@@ -794,6 +815,8 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     UP(d.dep_vf, sh->dep_vf, (size_t)s->nnz * 4);
 #undef UP
     e = cudaMemsetAsync(a + L.off[B_CONV], 0, L.off[B_MEAN] - L.off[B_CONV], s->st);
+    if (e != cudaSuccess) goto cuda_fail;
+    e = cudaMemsetAsync(d.rb_act, 1, (size_t)(s->nf + 127) / 128, s->st);  // every row block active
     if (e != cudaSuccess) goto cuda_fail;
     e = cudaMalloc(&s->ds_dev, sizeof(DevSolve));
     if (e != cudaSuccess) goto cuda_fail;
@@ -963,6 +986,7 @@ ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
     Ctl c{0, 1, 0, 0};
     CK(cudaMemcpyAsync(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
     CK(cudaMemsetAsync(s->ds.conv, 0, s->nf, s->st));
+    CK(cudaMemsetAsync(s->ds.rb_act, 1, (size_t)(s->nf + 127) / 128, s->st));
     CK(cudaMemsetAsync(s->ds.hot, 0, s->nf, s->st));
     CK(cudaMemsetAsync(s->ds.counts, 0, (size_t)s->P.revcap * 4, s->st));
     CK(reset_active_lists(s));
@@ -1061,7 +1085,7 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     while (e == cudaSuccess && done_revs < maxcap) {
         const int k = std::min(chunk, maxcap - done_revs);
         for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaGraphLaunch(gx, s0->st);
-        launches += (int64_t)k * (b.nw > 0 ? 5 : 3);
+        launches += (int64_t)k * kernels_per_revolution(b);
         done_revs += k;
         if (e != cudaSuccess) break;
         e = cudaEventRecord(s0->ev1, s0->st);

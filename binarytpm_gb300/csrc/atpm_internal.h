@@ -95,6 +95,7 @@ struct DevSolve {
     // facets still active after each convergence test (FAST, freeze on),
     // double-buffered by revolution parity: k_converge of revolution r fills
     // list (r+1)&1, the conduction of r+1 reads it, k_advance of r+1 clears it
+    uint8_t* rb_act;         // [ceil(nf/128)] some facet of the 128-facet row block active (FAST)
     int* act_list;           // [2][nf]
     int* act_cnt;            // [4]: counts of the two lists, then the revolution each list is for
     int* counts;             // [revcap] numconverged after each revolution
@@ -177,16 +178,20 @@ struct Batch {
     PowTab pq;               // x^0.25 (built only when a REFERENCE solve has TI 0)
     const int4* qmap;        // tensor-core work items {solve, row block, step chunk, 0}
     int nq;
+    int4* tc_list;           // [nq] this launch's items whose row block has an active facet
+    int* tc_work;            // [2] list length, next ticket (zeroed before every launch)
     int tc_nmax;             // largest step chunk in the batch
     int cond_variant;        // FAST conduction register/occupancy variant (1, 2, 3)
     int tc_stages;           // tensor-core pipeline depth (0: deepest that fits)
     int warp_tail;           // 1: FAST revolutions with few active facets sweep the active list
                              // (thread per facet; warp per facet below tail_limit)
     int tail_limit;          // active facets of the batch up to which they do
+    int sms;                 // SMs of the device (persistent tensor-core grid)
 };
 // deepest tensor-core pipeline that fits shared memory for step chunk N
 int tc_max_stages(int N);
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
+int kernels_per_revolution(const Batch& b);          // kernels launch_revolution starts
 // BF16 view-factor tiles (and residual tiles) of a solve from its uploaded
 // lists: slot[mb * nkb + kb] = tile of (row block, column block), lo_of[t] =
 // residual tile of tile t or -1; tiles must be zeroed (atpm_spmm_tc.cu)

@@ -67,6 +67,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 // bounded wait: false after ~1 s
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const long long t0 = clock64();
@@ -215,48 +219,64 @@ __global__ void __launch_bounds__(256) k_w_bf16(Batch b) {
     }
 }
 
-__global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
-    extern __shared__ __align__(1024) unsigned char dyn[];
-    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], done;
-    __shared__ uint32_t tmem_base;
-    const int4 item = b.qmap[blockIdx.x];
-    const DevSolve& sv = b.tab[item.x];
-    if (!sv.ctl->active || !sv.tc_tiles) return;
-    const int mb = item.y, nc = item.z;
-    const int N = sv.tc_n, nch = sv.tc_nchunks;
-    const int nf = sv.nf, ntau = sv.ntau;
-    const int t0 = sv.tc_ptr[mb], T = sv.tc_ptr[mb + 1] - t0;
-    float* Q = static_cast<float*>(sv.Q);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int f = mb * TC_M + warp * 32 + lane;
-    const bool everyone = !sv.freeze || sv.ti == 0.0f;
-    if (!__syncthreads_or(f < nf && (everyone || !sv.conv[f]))) return;  // all frozen
-    if (T == 0) {
-        if (f < nf)
-            for (int n = 0; n < N; ++n) {
-                const int s = nc * N + n;
-                if (s < ntau) Q[(size_t)s * nf + f] = 0.0f;
-            }
-        return;
+// Work items whose row block has an active facet, compacted before every
+// launch (in map order within each warp), so tickets are spent on work only.
+__global__ void __launch_bounds__(128) k_tc_compact(Batch b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool use = false;
+    int4 it = make_int4(0, 0, 0, 0);
+    if (i < b.nq) {
+        it = b.qmap[i];
+        const DevSolve& sv = b.tab[it.x];
+        const bool everyone = !sv.freeze || sv.ti == 0.0f;
+        use = sv.ctl->active && sv.tc_tiles && (everyone || sv.rb_act[it.y]);
     }
-    // 1024-byte aligned stage ring (alignment of the shared-window address)
-    unsigned char* base = dyn + ((1024u - (smem_u32(dyn) & 1023u)) & 1023u);
+    const unsigned m = __ballot_sync(0xffffffffu, use);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&b.tc_work[0], __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (use) b.tc_list[base + __popc(m & ((1u << lane) - 1u))] = it;
+}
+
+// Persistent, warp-specialised: one CTA per SM.  Work items are handed out
+// dynamically: the producer takes the next ticket of the launch's counter
+// over the compacted list and queues the item in a small shared-memory queue
+// read by the other roles; a ticket past the end queues the stop item.
+//   warp 0, lane 0   producer: tickets, the item queue, and bulk copies of
+//                    each tile's V_hi (+ V_lo) and W chunk into the stage
+//                    ring, across item boundaries
+//   warp 1, lane 0   MMA issuer: per item, into TMEM accumulator buffer
+//                    (item & 1), then tcgen05.commit -> tfull[buffer]
+//   warps 2-5        epilogue: TMEM quadrant (warp & 3) -> Q, then arrive on
+//                    tempty[buffer]; the issuer's next-but-one item waits on it
+// Every item's products accumulate in the single-item order, so Q does not
+// depend on which CTA computed it.
+constexpr int TC_THREADS = 192;
+constexpr int TC_QUEUE = 4;  // queued work items
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
+    extern __shared__ __align__(1024) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t full[TC_STAGES], empty[TC_STAGES], tfull[2], tempty[2], fin;
+    __shared__ __align__(8) uint64_t qfull[TC_QUEUE], qempty[TC_QUEUE];
+    __shared__ int4 qitem[TC_QUEUE];
+    __shared__ uint32_t tmem_base;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // one stage layout for the launch, sized for the largest chunk of the batch
+    const int Nmax = b.tc_nmax;
     const uint32_t a_bytes = TC_M * TC_K * 2;
-    const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;  // hi + lo
-    const uint32_t stage_bytes = (2 * a_bytes + b_bytes + 1023) & ~1023u;
-    // ring depth: the requested one, never more than this chunk size allows
-    // nor than the launch's dynamic shared memory holds (solves of one batch
-    // may use different chunk sizes)
-    int S = (b.tc_stages > 0 && b.tc_stages < tc_stages(N)) ? b.tc_stages : tc_stages(N);
+    const uint32_t stage_bytes = (2 * a_bytes + (uint32_t)Nmax * TC_K * 2 * 2 + 1023) & ~1023u;
+    int S = (b.tc_stages > 0 && b.tc_stages < tc_stages(Nmax)) ? b.tc_stages : tc_stages(Nmax);
     {
         uint32_t dsz;
         asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsz));
         const int fit = (int)((dsz - 1024u) / stage_bytes);
         if (S > fit) S = fit;
     }
-    const uint32_t ncols = (N <= 32) ? 32 : (N <= 64) ? 64 : (N <= 128) ? 128 : 256;
+    unsigned char* base = dyn + ((1024u - (smem_u32(dyn) & 1023u)) & 1023u);
+    constexpr uint32_t kBufCols = 256;  // TMEM columns per accumulator buffer (N <= 256)
     if (warp == 0) {
-        tc_alloc(&tmem_base, ncols);
+        tc_alloc(&tmem_base, 2 * kBufCols);
         tc_relinquish();
     }
     if (threadIdx.x == 0) {
@@ -264,7 +284,15 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
             mbar_init(&full[i], 1);
             mbar_init(&empty[i], 1);
         }
-        mbar_init(&done, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&tfull[i], 1);
+            mbar_init(&tempty[i], 4);  // one arrival per epilogue warp
+        }
+        for (int i = 0; i < TC_QUEUE; ++i) {
+            mbar_init(&qfull[i], 1);
+            mbar_init(&qempty[i], 5);  // the issuer and the four epilogue warps
+        }
+        mbar_init(&fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -272,77 +300,158 @@ __global__ void __launch_bounds__(128, 1) k_spmm_tc(Batch b) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base;
-    const __nv_bfloat16* tiles = static_cast<const __nv_bfloat16*>(sv.tc_tiles);
-    const __nv_bfloat16* lo_tiles = static_cast<const __nv_bfloat16*>(sv.tc_lo_tiles);
-    const __nv_bfloat16* Wb = static_cast<const __nv_bfloat16*>(sv.Wb);
-    // warp 0 lane 0: producer (bulk copies into the stage ring);
-    // warp 1 lane 0: MMA issuer.  Stage st is refilled as soon as the MMAs
-    // that read it complete (tcgen05.commit -> empty[st]), while the issuer
-    // keeps feeding the tensor pipe from the stages already full.
+    int* status0 = b.tab[0].status;  // where a timeout is reported when no item is at hand
+
     if (threadIdx.x == 0) {
-        bool ok = true;
-        for (int i = 0; i < T; ++i) {
-            const int st = i % S;
-            if (i >= S && !mbar_wait(&empty[st], (uint32_t)((i / S) - 1) & 1u)) { ok = false; break; }
-            unsigned char* sa = base + (size_t)st * stage_bytes;
-            const int kb = sv.tc_col[t0 + i] & 0xffffff;
-            const int lo = sv.tc_lo[t0 + i];
-            mbar_expect_tx(&full[st], a_bytes + (lo >= 0 ? a_bytes : 0u) + b_bytes);
-            bulk_g2s(sa, tiles + (size_t)(t0 + i) * (TC_M * TC_K), a_bytes, &full[st]);
-            if (lo >= 0) bulk_g2s(sa + a_bytes, lo_tiles + (size_t)lo * (TC_M * TC_K), a_bytes, &full[st]);
-            bulk_g2s(sa + 2 * a_bytes, Wb + ((size_t)kb * nch + nc) * (size_t)2 * N * TC_K, b_bytes, &full[st]);
-        }
-        if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);
-    } else if (threadIdx.x == 32) {
-        const uint32_t idesc = idesc_bf16(N);
-        uint32_t acc = 0u;  // the first product issued overwrites the accumulator
-        bool ok = true;
-        for (int i = 0; i < T; ++i) {
-            const int st = i % S;
-            if (!mbar_wait(&full[st], (uint32_t)(i / S) & 1u)) { ok = false; break; }
-            tc_fence_after();
-            const uint32_t sa = smem_u32(base + (size_t)st * stage_bytes);
-            const uint64_t ad = sw128_desc(sa), al = sw128_desc(sa + a_bytes);
-            const uint64_t bh = sw128_desc(sa + 2 * a_bytes), bl = sw128_desc(sa + 2 * a_bytes + b_bytes / 2);
-            const bool has_lo = sv.tc_lo[t0 + i] >= 0;
-            // K slices without an entry are zero in both A tiles: their
-            // products would add exact zeros, so they are not issued
-            const uint32_t kmask = (uint32_t)sv.tc_col[t0 + i] >> 24;
+        // ------------------------------------------------------------ producer
+        uint32_t slot = 0, ph = 0, qs = 0, qph = 0;
+        int last_ph[TC_STAGES];  // parity of each stage's last fill (-1: never filled)
 #pragma unroll
-            for (int k = 0; k < TC_K / 16; ++k) {
-                if (!((kmask >> k) & 1u)) continue;
-                tc_mma(tmem, ad + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, acc);
-                tc_mma(tmem, ad + (uint64_t)(2 * k), bl + (uint64_t)(2 * k), idesc, 1u);
-                if (has_lo) tc_mma(tmem, al + (uint64_t)(2 * k), bh + (uint64_t)(2 * k), idesc, 1u);
-                acc = 1u;
-            }
-            tc_commit(&empty[st]);
-        }
-        tc_commit(&done);
-        if (!ok) atomicOr(sv.status, ST_TC_TIMEOUT);
-    }
-    __syncwarp();
-    const bool fin = __all_sync(0xffffffffu, mbar_wait(&done, 0));
-    tc_fence_after();
-    if (fin) {
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-            float v[16];
-            tc_ld16(tmem + lane_base + (uint32_t)c0, v);
-            if (f < nf) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int s = nc * N + c0 + j;
-                    if (c0 + j < N && s < ntau) Q[(size_t)s * nf + f] = v[j];
+        for (int i = 0; i < TC_STAGES; ++i) last_ph[i] = -1;
+        bool ok = true;
+        const int nlist = b.tc_work[0];
+        for (;;) {
+            const int g = atomicAdd(&b.tc_work[1], 1);
+            const bool stop = g >= nlist;
+            const int4 it = stop ? make_int4(-1, 0, 0, 0) : b.tc_list[g];
+            {
+                // queue the item (or the stop item)
+                if (!mbar_wait(&qempty[qs], qph ^ 1u)) { ok = false; break; }
+                qitem[qs] = it;
+                mbar_arrive(&qfull[qs]);
+                if (++qs == TC_QUEUE) { qs = 0; qph ^= 1u; }
+                if (stop) break;
+                const DevSolve& sv = b.tab[it.x];
+                const int N = sv.tc_n, c = it.z;
+                const int t0 = sv.tc_ptr[it.y], T = sv.tc_ptr[it.y + 1] - t0;
+                const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;
+                const __nv_bfloat16* tiles = static_cast<const __nv_bfloat16*>(sv.tc_tiles);
+                const __nv_bfloat16* lo_tiles = static_cast<const __nv_bfloat16*>(sv.tc_lo_tiles);
+                const __nv_bfloat16* Wb = static_cast<const __nv_bfloat16*>(sv.Wb);
+                for (int i = 0; i < T; ++i) {
+                    if (!mbar_wait(&empty[slot], ph ^ 1u)) { ok = false; break; }
+                    unsigned char* sa = base + (size_t)slot * stage_bytes;
+                    const int kb = sv.tc_col[t0 + i] & 0xffffff;
+                    const int lo = sv.tc_lo[t0 + i];
+                    mbar_expect_tx(&full[slot], a_bytes + (lo >= 0 ? a_bytes : 0u) + b_bytes);
+                    bulk_g2s(sa, tiles + (size_t)(t0 + i) * (TC_M * TC_K), a_bytes, &full[slot]);
+                    if (lo >= 0) bulk_g2s(sa + a_bytes, lo_tiles + (size_t)lo * (TC_M * TC_K), a_bytes, &full[slot]);
+                    bulk_g2s(sa + 2 * a_bytes, Wb + ((size_t)kb * sv.tc_nchunks + c) * (size_t)2 * N * TC_K, b_bytes,
+                             &full[slot]);
+                    last_ph[slot] = (int)ph;
+                    if (++slot == (uint32_t)S) { slot = 0; ph ^= 1u; }
                 }
             }
+            if (!ok) break;
         }
-    } else if (threadIdx.x == 0) {
-        atomicOr(sv.status, ST_TC_TIMEOUT);
+        if (!ok) atomicOr(status0, ST_TC_TIMEOUT);
+        // copies still in flight exist only after a timeout: let them land
+#pragma unroll
+        for (int i = 0; i < TC_STAGES; ++i)
+            if (last_ph[i] >= 0) mbar_wait(&full[i], (uint32_t)last_ph[i]);
+    } else if (threadIdx.x == 32) {
+        // ---------------------------------------------------------- MMA issuer
+        uint32_t slot = 0, ph = 0, qs = 0, qph = 0, item_no = 0;
+        bool ok = true;
+        for (;;) {
+            if (!mbar_wait(&qfull[qs], qph)) { ok = false; break; }
+            const int4 w = qitem[qs];
+            if (w.x < 0) break;
+            const DevSolve& sv = b.tab[w.x];
+            const int N = sv.tc_n;
+            const int t0 = sv.tc_ptr[w.y], T = sv.tc_ptr[w.y + 1] - t0;
+            const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;
+            const uint32_t ab = item_no & 1u, use_no = item_no >> 1;
+            if (!mbar_wait(&tempty[ab], (use_no & 1u) ^ 1u)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t d = tmem + ab * kBufCols;
+            const uint32_t idesc = idesc_bf16(N);
+            uint32_t acc = 0u;  // the first product issued overwrites the accumulator
+            for (int i = 0; i < T && ok; ++i) {
+                if (!mbar_wait(&full[slot], ph)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t sa = smem_u32(base + (size_t)slot * stage_bytes);
+                const uint64_t ad = sw128_desc(sa), al = sw128_desc(sa + a_bytes);
+                const uint64_t bh = sw128_desc(sa + 2 * a_bytes), bl = sw128_desc(sa + 2 * a_bytes + b_bytes / 2);
+                const bool has_lo = sv.tc_lo[t0 + i] >= 0;
+                // K slices without an entry are zero in both A tiles: their
+                // products would add exact zeros, so they are not issued
+                const uint32_t kmask = (uint32_t)sv.tc_col[t0 + i] >> 24;
+#pragma unroll
+                for (int kk = 0; kk < TC_K / 16; ++kk) {
+                    if (!((kmask >> kk) & 1u)) continue;
+                    tc_mma(d, ad + (uint64_t)(2 * kk), bh + (uint64_t)(2 * kk), idesc, acc);
+                    tc_mma(d, ad + (uint64_t)(2 * kk), bl + (uint64_t)(2 * kk), idesc, 1u);
+                    if (has_lo) tc_mma(d, al + (uint64_t)(2 * kk), bh + (uint64_t)(2 * kk), idesc, 1u);
+                    acc = 1u;
+                }
+                tc_commit(&empty[slot]);
+                if (++slot == (uint32_t)S) { slot = 0; ph ^= 1u; }
+            }
+            if (!ok) break;
+            tc_commit(&tfull[ab]);  // this item's products complete -> epilogue
+            mbar_arrive(&qempty[qs]);
+            if (++qs == TC_QUEUE) { qs = 0; qph ^= 1u; }
+            ++item_no;
+        }
+        if (!ok) atomicOr(status0, ST_TC_TIMEOUT);
+        tc_commit(&fin);  // every product issued by this thread has completed
+        mbar_wait(&fin, 0);
+    } else if (warp >= 2) {
+        // ------------------------------------------------------------ epilogue
+        const int q = warp & 3;  // TMEM lanes q * 32 .. q * 32 + 31
+        uint32_t qs = 0, qph = 0, item_no = 0;
+        for (;;) {
+            if (!__all_sync(0xffffffffu, mbar_wait(&qfull[qs], qph))) {
+                if (lane == 0) atomicOr(status0, ST_TC_TIMEOUT);
+                break;
+            }
+            const int4 w = qitem[qs];
+            if (w.x < 0) break;
+            const DevSolve& sv = b.tab[w.x];
+            const int N = sv.tc_n, nf = sv.nf, ntau = sv.ntau, nc = w.z;
+            const int T = sv.tc_ptr[w.y + 1] - sv.tc_ptr[w.y];
+            float* Q = static_cast<float*>(sv.Q);
+            const uint32_t ab = item_no & 1u, use_no = item_no >> 1;
+            if (!__all_sync(0xffffffffu, mbar_wait(&tfull[ab], use_no & 1u))) {
+                if (lane == 0) atomicOr(sv.status, ST_TC_TIMEOUT);
+                break;
+            }
+            tc_fence_after();
+            const int f = w.y * TC_M + q * 32 + lane;
+            if (T == 0) {  // no other facet seen by this row block
+                if (f < nf)
+                    for (int n = 0; n < N; ++n) {
+                        const int s = nc * N + n;
+                        if (s < ntau) Q[(size_t)s * nf + f] = 0.0f;
+                    }
+            } else {
+                const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + ab * kBufCols;
+                for (int c0 = 0; c0 < N; c0 += 16) {
+                    float v[16];
+                    tc_ld16(tbase + (uint32_t)c0, v);
+                    if (f < nf) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int s = nc * N + c0 + j;
+                            if (c0 + j < N && s < ntau) Q[(size_t)s * nf + f] = v[j];
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&tempty[ab]);
+                mbar_arrive(&qempty[qs]);
+            }
+            if (++qs == TC_QUEUE) { qs = 0; qph ^= 1u; }
+            ++item_no;
+        }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc_dealloc(tmem, ncols);
+    if (warp == 0) tc_dealloc(tmem, 2 * kBufCols);
 }
 
 size_t spmm_tc_smem_bytes(int N, int stages) {
@@ -367,7 +476,12 @@ int launch_spmm_tc(const Batch& b, stream_t stv) {
             return 2;
         attr_dev = dev;
     }
-    k_spmm_tc<<<b.nq, 128, smem, st>>>(b);
+    // the list length and the ticket counter start at zero for every launch
+    // (a memset node when the revolution is captured in a graph)
+    if (cudaMemsetAsync(b.tc_work, 0, 2 * sizeof(int), st) != cudaSuccess) return 2;
+    k_tc_compact<<<(b.nq + 127) / 128, 128, 0, st>>>(b);
+    const int grid = b.nq < b.sms ? b.nq : b.sms;  // one persistent CTA per SM
+    k_spmm_tc<<<grid, TC_THREADS, smem, st>>>(b);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

@@ -622,6 +622,10 @@ __global__ void __launch_bounds__(128) k_converge(Batch b) {
     }
     c = __syncthreads_count(c);
     if (threadIdx.x == 0 && c) atomicAdd(&sv.counts[rev], c);
+    // row-block activity read by the next revolution's tensor-core product
+    // (blocks of this kernel are the product's 128-facet row blocks)
+    const int any = __syncthreads_or(f < sv.nf && !sv.conv[f]);
+    if (threadIdx.x == 0) sv.rb_act[fb.y >> 7] = any ? 1 : 0;
     // list of the facets still active for the next revolution (FAST, freeze):
     // each block appends its active facets as one segment in facet order, so
     // a sweep over the list keeps runs of neighbouring facets together
@@ -799,6 +803,13 @@ int launch_revolution_part(const Batch& b, int part, stream_t stv) {
         case MODE_FAST: return launch_rev_part<MODE_FAST>(b, part, st);
     }
     return 1;
+}
+
+int kernels_per_revolution(const Batch& b) {
+    const bool tc = b.mode == MODE_FAST && b.nq > 0;
+    const int selfheat = tc ? 2 : (b.nw > 0 ? 2 : 0);  // k_tc_compact + k_spmm_tc, or W + Q
+    const int conduction = b.mode == MODE_FAST ? 2 : 1;  // + k_conduction_warp
+    return selfheat + conduction + 2;                    // + k_converge, k_advance
 }
 
 int launch_revolution(const Batch& b, stream_t st) {
