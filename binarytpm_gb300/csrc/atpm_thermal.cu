@@ -272,9 +272,12 @@ constexpr int kFastPrefetch = 8;  // steps of forcing / flux / previous temperat
 
 // One FTCS node update and one Newton step of the FAST sweep, shared by the
 // thread-per-facet and the warp-per-facet forms so both round alike.
+// (up + dn) - 2 t is formed as one fma: 2 t is exact, so this is the
+// rounding of the plain expression
 __device__ __forceinline__ float ftcs_node(float r, float up, float dn, float t) {
-    return fmaf(r, (up + dn) - 2.0f * t, t);
+    return fmaf(r, fmaf(-2.0f, t, up + dn), t);
 }
+
 __device__ __forceinline__ float newton_fast(float th, float Tref, float t1, float a, float m1, float es, float es4,
                                              float& DT) {
     const float TR = Tref + th;
