@@ -158,7 +158,7 @@ Layout layout(int nv, int nf, int nnz, const atpm_params& P) {
     sz[B_STATUS] = 4;
     sz[B_CTL] = sizeof(Ctl);
     sz[B_DIAG] = 4 * 8;
-    sz[B_ACT] = ((size_t)2 * nf + 4) * 4;
+    sz[B_ACT] = ((size_t)2 * nf + 5) * 4;
     sz[B_MEAN] = (size_t)nf * rs;
     sz[B_RBACT] = (size_t)(nf + 127) / 128;
     Layout L;

@@ -97,7 +97,8 @@ struct DevSolve {
     // list (r+1)&1, the conduction of r+1 reads it, k_advance of r+1 clears it
     uint8_t* rb_act;         // [ceil(nf/128)] some facet of the 128-facet row block active (FAST)
     int* act_list;           // [2][nf]
-    int* act_cnt;            // [4]: counts of the two lists, then the revolution each list is for
+    int* act_cnt;            // [5]: counts of the two lists, the revolution each list is for, and
+                             // (batch leader) whether this revolution runs warp per facet
     int* counts;             // [revcap] numconverged after each revolution
     int* status;             // ST_* bits
     Ctl* ctl;

@@ -423,6 +423,8 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
     int flags = 0;
     const int cap = sv.newton_cap;
     float th1 = 0.0f;
+    // nodes 0, 1, 2 held by every lane (lane 0 owns 0 and 1, lane 1 owns 2)
+    float th_u = __shfl_sync(FULL, Ta, 0), t1_u = __shfl_sync(FULL, Tb, 0), t2_u = __shfl_sync(FULL, Ta, 1);
     float ce = 0.0f, cq = 0.0f, co = 0.0f;
     if (lane < ntau) {
         const size_t o = (size_t)lane * nf + f;
@@ -440,18 +442,22 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
         }
         float ts = 0.0f;
         const int nstep = min(32, ntau - s0);
+        // unrolled so that the node updates of the next steps (independent of
+        // this step's boundary solve) overlap its dependency chain
+#pragma unroll 4
         for (int j = 0; j < nstep; ++j) {
             const float e = __shfl_sync(FULL, ce, j), q = __shfl_sync(FULL, cq, j), old = __shfl_sync(FULL, co, j);
             const float lft = __shfl_up_sync(FULL, Tb, 1);    // node na - 1
             const float rgt = __shfl_down_sync(FULL, Ta, 1);  // node nb + 1
-            const float th = __shfl_sync(FULL, Ta, 0);        // node 0 (old)
+            // nodes 2 .. NX-1 from old values, off the boundary's dependency chain
             float Ta_n = Ta, Tb_n = Tb;
-            if (na >= 1 && na <= NX - 1) Ta_n = ftcs_node(r, Tb, lft, Ta);
-            if (nb <= NX - 1) Tb_n = ftcs_node(r, rgt, Ta, Tb);
-            const float t1n = __shfl_sync(FULL, Tb_n, 0);     // node 1 (new)
+            if (na >= 2 && na <= NX - 1) Ta_n = ftcs_node(r, Tb, lft, Ta);
+            if (nb >= 2 && nb <= NX - 1) Tb_n = ftcs_node(r, rgt, Ta, Tb);
+            // node 1 and the boundary solve on every lane (uniform values)
+            const float t1n = ftcs_node(r, t2_u, th_u, t1_u);
             const float a = fmaf(oma, e, q);
             float DT;
-            th1 = newton_fast(th, Tref, t1n, a, m1, es, es4, DT);
+            th1 = newton_fast(th_u, Tref, t1n, a, m1, es, es4, DT);
             if (DT >= tacc10) th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
             int it = 2;
             while (DT >= tacc10) {
@@ -459,7 +465,10 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
                 th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
                 ++it;
             }
-            if (lane == 0) Ta_n = th1;
+            if (lane == 0) {
+                Ta_n = th1;
+                Tb_n = t1n;
+            }
             // bottom node: T[NX] = T[NX - 1] (new)
             const float bot = __shfl_sync(FULL, ((NX - 1) & 1) ? Tb_n : Ta_n, (NX - 1) >> 1);
             if (lane == (NX >> 1)) {
@@ -468,6 +477,9 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
             }
             Ta = Ta_n;
             Tb = Tb_n;
+            th_u = th1;
+            t1_u = t1n;
+            t2_u = __shfl_sync(FULL, Ta, 1);  // node 2 (new)
             const float Tsurf = Tref + th1;
             if (lane == j) ts = Tsurf;
             hot = hot || (fabsf(Tsurf - old) >= tacc);
@@ -503,30 +515,29 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
 // A revolution of the batch runs warp per facet when every active solve with
 // a depth sweep (TI > 0) freezes converged facets, fits a warp's nodes and
 // has the list of its active facets built for this revolution, and those
-// lists hold at most b.tail_limit facets together.  Both conduction kernels
-// evaluate the same rule on the same words, so exactly one of them advances
-// each facet.
+// lists hold at most b.tail_limit facets together.  k_tail_mode decides once
+// per revolution (one warp over the solves) and leaves the answer in the
+// batch's first solve (act_cnt[4]), where both conduction kernels read it:
+// exactly one of them advances each facet.
 constexpr int kSparseCtas = 128;  // CTAs (4 warps each) per solve
-__device__ __forceinline__ bool warp_tail_revolution(const Batch& b) {
-    if (!b.warp_tail) return false;
+
+__global__ void k_tail_mode(Batch b) {
+    const int lane = threadIdx.x;
+    bool ok = b.warp_tail != 0;
     int total = 0;
-    for (int i = 0; i < b.n; ++i) {
+    for (int i = lane; i < b.n; i += 32) {
         const DevSolve& s = b.tab[i];
         if (!s.ctl->active || s.ti == 0.0f) continue;
         const int rev = s.ctl->rev;
-        if (!s.freeze || s.nx + 1 > kWarpNodes || rev < 7 || s.act_cnt[2 + (rev & 1)] != rev) return false;
-        total += s.act_cnt[rev & 1];
+        if (!s.freeze || s.nx + 1 > kWarpNodes || rev < 7 || s.act_cnt[2 + (rev & 1)] != rev) ok = false;
+        else total += s.act_cnt[rev & 1];
     }
-    return total <= b.tail_limit;
+    ok = __all_sync(0xffffffffu, ok);
+    for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+    if (lane == 0) b.tab[0].act_cnt[4] = (ok && total <= b.tail_limit) ? 1 : 0;
 }
 
-// one thread decides for the CTA
-__device__ __forceinline__ bool cta_warp_tail(const Batch& b) {
-    __shared__ int flag;
-    if (threadIdx.x == 0) flag = warp_tail_revolution(b) ? 1 : 0;
-    __syncthreads();
-    return flag != 0;
-}
+__device__ __forceinline__ bool warp_tail_now(const Batch& b) { return b.tab[0].act_cnt[4] != 0; }
 
 template <int NX>
 __global__ void __launch_bounds__(128) k_conduction_warp(Batch b) {
@@ -536,7 +547,7 @@ __global__ void __launch_bounds__(128) k_conduction_warp(Batch b) {
     if (!sv.ctl->active || sv.ti == 0.0f) return;
     const int rev = sv.ctl->rev;
     if (rev < 7 || sv.act_cnt[2 + (rev & 1)] != rev || sv.act_cnt[rev & 1] == 0) return;
-    if (!cta_warp_tail(b)) return;
+    if (!warp_tail_now(b)) return;
     if constexpr (NX + 1 <= kWarpNodes) {
         const int n = sv.act_cnt[rev & 1];
         const int* list = sv.act_list + (size_t)(rev & 1) * sv.nf;
@@ -585,7 +596,7 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     if (!sv.ctl->active) return;
     if constexpr (MODE == MODE_FAST) {
         if (sv.ti != 0.0f) {
-            if (cta_warp_tail(b)) return;  // k_conduction_warp runs this revolution
+            if (warp_tail_now(b)) return;  // k_conduction_warp runs this revolution
             // at most half the facets active: the solve's blocks sweep its
             // list of active facets instead of its facet range, so active
             // facets fill whole warps and the remaining blocks exit
@@ -759,6 +770,7 @@ static int launch_rev_part(const Batch& b, int part, cudaStream_t st) {
         case 0: if (b.nw > 0) k_selfheat_w<MODE><<<b.nw, dim3(32, 8), 0, st>>>(b); break;
         case 1: if (b.nw > 0) k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b); break;
         case 2:
+            if (MODE == MODE_FAST) k_tail_mode<<<1, 32, 0, st>>>(b);
             if (MODE == MODE_FAST && b.cond_variant == 3) {
                 switch (b.nx) {
 #define NX_CASE(n) case n: k_conduction<MODE, n, 3><<<b.nfb, 128, 0, st>>>(b); break;
@@ -811,7 +823,7 @@ int launch_revolution_part(const Batch& b, int part, stream_t stv) {
 int kernels_per_revolution(const Batch& b) {
     const bool tc = b.mode == MODE_FAST && b.nq > 0;
     const int selfheat = tc ? 2 : (b.nw > 0 ? 2 : 0);  // k_tc_compact + k_spmm_tc, or W + Q
-    const int conduction = b.mode == MODE_FAST ? 2 : 1;  // + k_conduction_warp
+    const int conduction = b.mode == MODE_FAST ? 3 : 1;  // + k_tail_mode, k_conduction_warp
     return selfheat + conduction + 2;                    // + k_converge, k_advance
 }
 
