@@ -369,6 +369,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     char* m = nullptr;
     CK(cudaMalloc((void**)&m, b_tiles + b_ptr + b_col + b_w + b_lo + b_loi + b_slot));
     s->tc_mem = m;
+    s->tc_bytes = b_tiles + b_ptr + b_col + b_w + b_lo + b_loi + b_slot;
     char* p_lo = m + b_tiles + b_ptr + b_col + b_w;
     int* d_slot = reinterpret_cast<int*>(p_lo + b_lo + b_loi);
     CK(cudaMemsetAsync(m, 0, b_tiles, s->st));
@@ -749,6 +750,35 @@ ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* sh, const atpm_param
     return ATPM_OK;
 }
 
+// device pointers of a solve into its arena (layout L)
+void wire_arena(atpm_solve* s, const Layout& L) {
+    char* a = static_cast<char*>(s->arena);
+    DevSolve& d = s->ds;
+    d.vert = reinterpret_cast<double*>(a + L.off[B_VERT]);
+    d.fac = reinterpret_cast<int*>(a + L.off[B_FAC]);
+    d.dep_ptr = reinterpret_cast<int*>(a + L.off[B_DPTR]);
+    d.dep_idx = reinterpret_cast<int*>(a + L.off[B_DIDX]);
+    d.dep_vf = reinterpret_cast<float*>(a + L.off[B_DVF]);
+    d.shadow = reinterpret_cast<uint8_t*>(a + L.off[B_SHADOW]);
+    d.cosil = a + L.off[B_COS];
+    d.Efm = a + L.off[B_EFM];
+    d.E = a + L.off[B_E];
+    d.stemp0 = a + L.off[B_S0];
+    d.stemp1 = a + L.off[B_S1];
+    d.temp = a + L.off[B_TEMP];
+    d.Q = a + L.off[B_Q];
+    d.W = a + L.off[B_W];
+    d.conv = reinterpret_cast<uint8_t*>(a + L.off[B_CONV]);
+    d.hot = reinterpret_cast<uint8_t*>(a + L.off[B_HOT]);
+    d.counts = reinterpret_cast<int*>(a + L.off[B_COUNTS]);
+    d.status = reinterpret_cast<int*>(a + L.off[B_STATUS]);
+    d.ctl = reinterpret_cast<Ctl*>(a + L.off[B_CTL]);
+    d.diag = reinterpret_cast<double*>(a + L.off[B_DIAG]);
+    d.act_list = reinterpret_cast<int*>(a + L.off[B_ACT]);
+    d.act_cnt = d.act_list + (size_t)2 * s->nf;
+    d.rb_act = reinterpret_cast<uint8_t*>(a + L.off[B_RBACT]);
+}
+
 ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, const atpm_params* P,
                                        atpm_solve** out) {
     if (!ctx || !out) return fail(ATPM_E_INVALID, "null context or out");
@@ -780,29 +810,7 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     DevSolve& d = s->ds;
     d.nf = s->nf; d.nv = s->nv; d.ntau = P->ntau; d.nx = P->nx; d.revcap = P->revcap;
     d.mode = P->precision; d.nnz = s->nnz; d.freeze = P->freeze ? 1 : 0;
-    d.vert = reinterpret_cast<double*>(a + L.off[B_VERT]);
-    d.fac = reinterpret_cast<int*>(a + L.off[B_FAC]);
-    d.dep_ptr = reinterpret_cast<int*>(a + L.off[B_DPTR]);
-    d.dep_idx = reinterpret_cast<int*>(a + L.off[B_DIDX]);
-    d.dep_vf = reinterpret_cast<float*>(a + L.off[B_DVF]);
-    d.shadow = reinterpret_cast<uint8_t*>(a + L.off[B_SHADOW]);
-    d.cosil = a + L.off[B_COS];
-    d.Efm = a + L.off[B_EFM];
-    d.E = a + L.off[B_E];
-    d.stemp0 = a + L.off[B_S0];
-    d.stemp1 = a + L.off[B_S1];
-    d.temp = a + L.off[B_TEMP];
-    d.Q = a + L.off[B_Q];
-    d.W = a + L.off[B_W];
-    d.conv = reinterpret_cast<uint8_t*>(a + L.off[B_CONV]);
-    d.hot = reinterpret_cast<uint8_t*>(a + L.off[B_HOT]);
-    d.counts = reinterpret_cast<int*>(a + L.off[B_COUNTS]);
-    d.status = reinterpret_cast<int*>(a + L.off[B_STATUS]);
-    d.ctl = reinterpret_cast<Ctl*>(a + L.off[B_CTL]);
-    d.diag = reinterpret_cast<double*>(a + L.off[B_DIAG]);
-    d.act_list = reinterpret_cast<int*>(a + L.off[B_ACT]);
-    d.act_cnt = d.act_list + (size_t)2 * s->nf;
-    d.rb_act = reinterpret_cast<uint8_t*>(a + L.off[B_RBACT]);
+    wire_arena(s, L);
     set_scalars(s, 0.0f);
     s->vert_h.assign(sh->vertices, sh->vertices + 3 * (size_t)s->nv);
     s->fac_h.assign(sh->facets, sh->facets + 3 * (size_t)s->nf);
@@ -868,6 +876,81 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->arena) cudaFree(s->arena);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
+    return ATPM_OK;
+}
+
+// the address at the same offset from `to` as p is from `from`
+static void* rebase_ptr(const void* p, const void* from, void* to) {
+    if (!p) return nullptr;
+    return static_cast<char*>(to) + (static_cast<const char*>(p) - static_cast<const char*>(from));
+}
+
+ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
+    if (!src || !out) return fail(ATPM_E_INVALID, "null solve or out");
+    CK(cudaSetDevice(src->ctx->device));
+    CK(cudaStreamSynchronize(src->st));  // the source's state is complete
+    auto* s = new atpm_solve();
+    s->ctx = src->ctx;
+    s->P = src->P;
+    s->nf = src->nf; s->nv = src->nv; s->nnz = src->nnz; s->rs = src->rs;
+    s->nw = src->nw; s->nfb = src->nfb; s->nq = src->nq;
+    s->vert_h = src->vert_h;
+    s->fac_h = src->fac_h;
+    s->have_forcing = src->have_forcing; s->have_temps = src->have_temps;
+    s->has_position = src->has_position;
+    std::memcpy(s->position, src->position, sizeof s->position);
+    s->sec_vertex = src->sec_vertex; s->sec_facet = src->sec_facet;
+    s->revs_p = src->revs_p; s->revs_s = src->revs_s;
+    s->ir_abs = src->ir_abs;
+    s->ti = src->ti;
+    s->ds = src->ds;  // scalars; device pointers rebased below
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
+    e = cudaMalloc(&s->arena, src->arena_bytes);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s->st);
+        delete s;
+        return fail(ATPM_E_NOMEM, "cudaMalloc(%zu): %s", src->arena_bytes, cudaGetErrorString(e));
+    }
+    s->arena_bytes = src->arena_bytes;
+    wire_arena(s, layout(s->nv, s->nf, s->nnz, s->P));
+    e = cudaMemcpyAsync(s->arena, src->arena, s->arena_bytes, cudaMemcpyDeviceToDevice, s->st);
+    if (e == cudaSuccess) e = cudaMalloc(&s->ds_dev, sizeof(DevSolve));
+    if (e == cudaSuccess) e = cudaMalloc(&s->wmap, std::max<size_t>((size_t)s->nw, 1) * sizeof(int4));
+    if (e == cudaSuccess) e = cudaMalloc(&s->fmap, (size_t)s->nfb * sizeof(int2));
+    if (e == cudaSuccess && s->nw)
+        e = cudaMemcpyAsync(s->wmap, src->wmap, (size_t)s->nw * sizeof(int4), cudaMemcpyDeviceToDevice, s->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->fmap, src->fmap, (size_t)s->nfb * sizeof(int2), cudaMemcpyDeviceToDevice, s->st);
+    if (e == cudaSuccess && src->tc_mem) {
+        e = cudaMalloc(&s->tc_mem, src->tc_bytes);
+        if (e == cudaSuccess) {
+            s->tc_bytes = src->tc_bytes;
+            e = cudaMemcpyAsync(s->tc_mem, src->tc_mem, s->tc_bytes, cudaMemcpyDeviceToDevice, s->st);
+            DevSolve& d = s->ds;
+            d.tc_ptr = static_cast<const int*>(rebase_ptr(d.tc_ptr, src->tc_mem, s->tc_mem));
+            d.tc_col = static_cast<const int*>(rebase_ptr(d.tc_col, src->tc_mem, s->tc_mem));
+            d.tc_tiles = rebase_ptr(d.tc_tiles, src->tc_mem, s->tc_mem);
+            d.tc_lo = static_cast<const int*>(rebase_ptr(d.tc_lo, src->tc_mem, s->tc_mem));
+            d.tc_lo_tiles = rebase_ptr(d.tc_lo_tiles, src->tc_mem, s->tc_mem);
+            d.Wb = rebase_ptr(d.Wb, src->tc_mem, s->tc_mem);
+        }
+    }
+    if (e == cudaSuccess && src->qmap) {
+        e = cudaMalloc(&s->qmap, (size_t)s->nq * sizeof(int4));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->qmap, src->qmap, (size_t)s->nq * sizeof(int4), cudaMemcpyDeviceToDevice, s->st);
+    }
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+    if (e != cudaSuccess) {
+        atpm_solve_destroy(s);
+        return fail(ATPM_E_CUDA, "solve clone: %s", cudaGetErrorString(e));
+    }
+    atpm_status r = upload_table(s);
+    if (r) { atpm_solve_destroy(s); return r; }
+    *out = s;
     return ATPM_OK;
 }
 

@@ -43,6 +43,7 @@ struct atpm_solve {
     int2* fmap = nullptr;
     int nw = 0, nfb = 0;
     void* tc_mem = nullptr;   // tensor-core tiles + W tiles (FAST)
+    size_t tc_bytes = 0;
     int4* qmap = nullptr;
     int nq = 0;
     cudaGraphExec_t graph = nullptr;

@@ -49,6 +49,7 @@ _SIGS = {
     "atpm_context_destroy": (C.c_int, [C.c_void_p]),
     "atpm_solve_create": (C.c_int, [C.c_void_p, C.POINTER(Shape), C.POINTER(Params), C.POINTER(C.c_void_p)]),
     "atpm_solve_destroy": (C.c_int, [C.c_void_p]),
+    "atpm_solve_clone": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "atpm_solve_footprint": (C.c_int, [C.POINTER(Shape), C.POINTER(Params), C.POINTER(C.c_uint64)]),
     "atpm_geometry_shadow": (C.c_int, [C.c_void_p]),
     "atpm_scattering": (C.c_int, [C.c_void_p]),
@@ -202,6 +203,17 @@ class Solve:
         _ck(lib.atpm_solve_create(ctx.h, C.byref(sh), C.byref(self.params), C.byref(h)))
         self.h = h
         self.nf, self.ntau, self.nx = len(f), problem.ntau, problem.nx
+
+    def clone(self) -> "Solve":
+        """A new solve with this one's shape, parameters and device state
+        (forcing, temperatures, tiles), copied on the device
+        (atpm_solve_clone): a thermal-inertia sweep prepares the shape once."""
+        h = C.c_void_p()
+        _ck(load().atpm_solve_clone(self.h, C.byref(h)))
+        c = Solve.__new__(Solve)
+        c.__dict__.update({k: v for k, v in self.__dict__.items() if k != "h"})
+        c.h = h
+        return c
 
     def close(self):
         if getattr(self, "h", None):

@@ -104,6 +104,13 @@ ATPM_API atpm_status atpm_context_destroy(atpm_context* ctx);
 ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* shape,
                                        const atpm_params* params, atpm_solve** out);
 ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s);
+/* A new solve with the same shape, parameters and device state as `src`
+ * (forcing, temperatures, convergence, tensor-core tiles), copied on the
+ * device: the thermal-inertia loop of the reference's driver
+ * (3905/Thermal/NominalPole/main.cpp:2481-2495) reruns one shape and forcing
+ * for every thermal inertia, so a sweep uploads and prepares the shape once
+ * and clones it per inertia.  No counterpart function in the reference. */
+ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out);
 /* Device bytes held by a solve with this shape and params (HBM admission). */
 ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* shape, const atpm_params* params,
                                           uint64_t* bytes);

@@ -120,3 +120,34 @@ def test_fast_scattering_within_accuracy(gpu_ctx, name):
     assert np.array_equal(s.shadow(), ref["shadow"])
     d = np.abs(e - ref["illumination"])
     assert np.max(d) <= 2 * 1e-4 / prob.albedo + 1e-6 * np.max(np.abs(ref["illumination"])), np.max(d)
+
+
+@pytest.mark.parametrize("precision", ["FAST", "REFERENCE"])
+def test_clone_matches_a_solve_set_up_from_host_arrays(gpu_ctx, precision):
+    """atpm_solve_clone copies shape, forcing and tiles on the device: each
+    clone, given its own thermal inertia, ends bit-identical to a solve
+    created from the same host arrays with the forcing uploaded."""
+    from binarytpm_gb300 import lib
+
+    prec = getattr(lib, precision)
+    prob, _ = golden("binary_s3s1")
+    s0 = lib.Solve(gpu_ctx, prob, precision=prec, revcap=80)
+    s0.geometry_shadow()
+    s0.scattering()
+    sh, il = s0.shadow(), s0.illumination()
+    for ti in (50.0, 400.0):
+        c = s0.clone()
+        h = lib.Solve(gpu_ctx, prob, precision=prec, revcap=80)
+        h.set_forcing(sh, il)
+        for s in (c, h):
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+        nc, nh = lib.batch_run([c]), lib.batch_run([h])
+        assert np.array_equal(nc[0], nh[0])
+        (a1, a0), (b1, b0) = c.surface_temperature(), h.surface_temperature()
+        assert np.array_equal(a1.view(np.uint32), b1.view(np.uint32))
+        assert np.array_equal(a0.view(np.uint32), b0.view(np.uint32))
+        assert np.array_equal(c.depth_temperature().view(np.uint32), h.depth_temperature().view(np.uint32))
+        c.close()
+        h.close()
+
