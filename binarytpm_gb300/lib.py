@@ -135,6 +135,23 @@ def exported_symbols():
     return list(_SIGS)
 
 
+def _host_out(shape, dtype) -> np.ndarray:
+    """Output array for a device read-back: page-locked host memory (torch's
+    cached pinned allocator) when torch sees a CUDA device, so the copy runs
+    as direct DMA; plain numpy otherwise.  Every element is written by the
+    call that fills it."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+                   np.dtype(np.int32): torch.int32}[np.dtype(dtype)]
+            return torch.empty(shape, dtype=tdt, pin_memory=True).numpy()
+    except (ImportError, KeyError, RuntimeError):
+        pass
+    return np.empty(shape, dtype)
+
+
 def _ck(rc: int):
     if rc != 0:
         lib = load()
@@ -265,34 +282,34 @@ class Solve:
 
     # getters ------------------------------------------------------------
     def shadow(self):
-        out = np.zeros((self.nf, self.ntau), np.int32)
+        out = _host_out((self.nf, self.ntau), np.int32)
         _ck(load().atpm_get_shadow(self.h, _p(out)))
         return out
 
     def illumination(self):
-        out = np.zeros((self.nf, self.ntau), np.float32)
+        out = _host_out((self.nf, self.ntau), np.float32)
         _ck(load().atpm_get_illumination(self.h, _p(out)))
         return out
 
     def cosillum(self):
-        out = np.zeros((self.nf, self.ntau), np.float32)
+        out = _host_out((self.nf, self.ntau), np.float32)
         _ck(load().atpm_get_cosillum(self.h, _p(out)))
         return out
 
     def selfheating_flux(self):
         """Q [ntau][nf] for the current temperatures."""
-        out = np.zeros((self.ntau, self.nf), np.float32)
+        out = _host_out((self.ntau, self.nf), np.float32)
         _ck(load().atpm_selfheating_flux(self.h, _p(out)))
         return out
 
     def surface_temperature(self):
-        s1 = np.zeros((self.nf, self.ntau), np.float32)
-        s0 = np.zeros((self.nf, self.ntau), np.float32)
+        s1 = _host_out((self.nf, self.ntau), np.float32)
+        s0 = _host_out((self.nf, self.ntau), np.float32)
         _ck(load().atpm_get_surface_temperature(self.h, _p(s1), _p(s0)))
         return s1, s0
 
     def surface_temperature64(self):
-        s1 = np.zeros((self.nf, self.ntau), np.float64)
+        s1 = _host_out((self.nf, self.ntau), np.float64)
         _ck(load().atpm_get_surface_temperature64(self.h, _p(s1)))
         return s1
 
