@@ -263,10 +263,8 @@ def main():
     s0 = lib.Solve(ctx, prob, precision=lib.FAST)
     s0.geometry_shadow()
     s0.scattering()
-    shadow, illum = s0.shadow(), s0.illumination()
-    solves = [s0] + [lib.Solve(ctx, prob, precision=lib.FAST) for _ in tis[1:]]
-    for s in solves[1:]:
-        s.set_forcing(shadow, illum)
+    # the other inertias: device clones of the prepared solve (shared tiles)
+    solves = [s0] + [s0.clone() for _ in tis[1:]]
     setup_s = time.perf_counter() - t_setup
 
     def step():
@@ -312,6 +310,7 @@ def main():
     fp64 = None
     err = None
     if not args.no_fp64:
+        shadow, illum = s0.shadow(), s0.illumination()
         p = lib.Solve(ctx, prob, precision=lib.FP64)
         p.set_forcing(shadow, illum)
         f64_ms, f64_fs = 0.0, 0

@@ -297,12 +297,20 @@ void tc_chunks(int ntau, int* n, int* nch) {
 }
 
 // work items of the tensor-core product {solve, row block, step chunk, 0}
-void build_tc_maps(int nf, int ntau, int solve, std::vector<int4>& q) {
-    int n, nch;
-    tc_chunks(ntau, &n, &nch);
-    const int nmb = (nf + 127) / 128;
-    for (int mb = 0; mb < nmb; ++mb)
-        for (int c = 0; c < nch; ++c) q.push_back(make_int4(solve, mb, c, 0));
+// for the solves of a batch that have tiles, solve by solve and row block by
+// row block: one solve's W tiles stay in L2 while its items run, and
+// neighbouring row blocks read largely the same W column blocks.  (Putting
+// the same row block of all solves together, to share V tiles in L2, made
+// the batch's W working set exceed L2: 25 % slower.)
+void build_tc_items(atpm_solve* const* solves, int n, std::vector<int4>& q) {
+    for (int i = 0; i < n; ++i) {
+        const atpm_solve* s = solves[i];
+        if (!s->tc) continue;
+        int N, nch;
+        tc_chunks(s->P.ntau, &N, &nch);
+        for (int mb = 0; mb < (int)s->tc->rb_tiles.size(); ++mb)
+            for (int c = 0; c < nch; ++c) q.push_back(make_int4(i, mb, c, 0));
+    }
 }
 
 // device layout of a batch's tensor-core map: the nq items, then room for the
@@ -366,16 +374,21 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     const size_t b_w = align256((size_t)nkb * nch * N * 64 * 2 * 2);
     const size_t b_lo = align256((size_t)std::max(nlo, 1) * tile_el * 2), b_loi = align256(lo_of.size() * 4);
     const size_t b_slot = align256(ncell * 4);
-    char* m = nullptr;
-    CK(cudaMalloc((void**)&m, b_tiles + b_ptr + b_col + b_w + b_lo + b_loi + b_slot));
-    s->tc_mem = m;
-    s->tc_bytes = b_tiles + b_ptr + b_col + b_w + b_lo + b_loi + b_slot;
-    char* p_lo = m + b_tiles + b_ptr + b_col + b_w;
+    auto* tc = new TcShared();
+    s->tc = tc;
+    tc->bytes = b_tiles + b_ptr + b_col + b_lo + b_loi + b_slot;
+    tc->rb_tiles.resize(nmb);
+    for (int mb = 0; mb < nmb; ++mb) tc->rb_tiles[mb] = tptr[mb + 1] - tptr[mb];
+    CK(cudaMalloc(&tc->mem, tc->bytes));
+    CK(cudaMalloc(&s->wb_mem, b_w));
+    s->wb_bytes = b_w;
+    char* m = static_cast<char*>(tc->mem);
+    char* p_lo = m + b_tiles + b_ptr + b_col;
     int* d_slot = reinterpret_cast<int*>(p_lo + b_lo + b_loi);
     CK(cudaMemsetAsync(m, 0, b_tiles, s->st));
     CK(cudaMemcpyAsync(m + b_tiles, tptr.data(), (nmb + 1) * 4, cudaMemcpyHostToDevice, s->st));
     if (ntiles) CK(cudaMemcpyAsync(m + b_tiles + b_ptr, tcol.data(), ntiles * 4, cudaMemcpyHostToDevice, s->st));
-    CK(cudaMemsetAsync(m + b_tiles + b_ptr + b_col, 0, b_w, s->st));
+    CK(cudaMemsetAsync(s->wb_mem, 0, b_w, s->st));
     CK(cudaMemsetAsync(p_lo, 0, b_lo, s->st));
     CK(cudaMemcpyAsync(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(d_slot, slot.data(), ncell * 4, cudaMemcpyHostToDevice, s->st));
@@ -386,7 +399,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     d.tc_tiles = m;
     d.tc_ptr = reinterpret_cast<const int*>(m + b_tiles);
     d.tc_col = reinterpret_cast<const int*>(m + b_tiles + b_ptr);
-    d.Wb = m + b_tiles + b_ptr + b_col;
+    d.Wb = s->wb_mem;
     d.tc_lo_tiles = p_lo;
     d.tc_lo = reinterpret_cast<const int*>(p_lo + b_lo);
     d.tc_n = N;
@@ -394,7 +407,8 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     d.tc_nmb = nmb;
     d.tc_nkb = nkb;
     std::vector<int4> q;
-    build_tc_maps(nf, ntau, 0, q);
+    atpm_solve* one[1] = {s};
+    build_tc_items(one, 1, q);
     tc_map_extend(q);
     CK(cudaMalloc(&s->qmap, q.size() * sizeof(int4)));
     CK(cudaMemcpy(s->qmap, q.data(), q.size() * sizeof(int4), cudaMemcpyHostToDevice));
@@ -452,11 +466,9 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
         std::vector<int4> w1;
         build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, fm);
         if (solves[i]->nnz > 0) wm.insert(wm.end(), w1.begin(), w1.end());
-        if (solves[i]->nq > 0) {
-            build_tc_maps(solves[i]->nf, solves[i]->P.ntau, i, qm);
-            nmax = std::max(nmax, solves[i]->ds.tc_n);
-        }
+        if (solves[i]->nq > 0) nmax = std::max(nmax, solves[i]->ds.tc_n);
     }
+    build_tc_items(solves, n, qm);
     const size_t bt = align256(n * sizeof(DevSolve)), bw = align256(std::max<size_t>(wm.size(), 1) * sizeof(int4));
     const size_t bf = align256(fm.size() * sizeof(int2));
     tc_map_extend(qm);
@@ -638,11 +650,9 @@ void host_table(atpm_solve* const* solves, int n, HostTable& h) {
         std::vector<int4> w1;
         build_maps(solves[i]->nf, solves[i]->P.ntau, i, w1, h.fm);
         if (solves[i]->nnz > 0) h.wm.insert(h.wm.end(), w1.begin(), w1.end());
-        if (solves[i]->nq > 0) {
-            build_tc_maps(solves[i]->nf, solves[i]->P.ntau, i, h.qm);
-            h.nmax = std::max(h.nmax, solves[i]->ds.tc_n);
-        }
+        if (solves[i]->nq > 0) h.nmax = std::max(h.nmax, solves[i]->ds.tc_n);
     }
+    build_tc_items(solves, n, h.qm);
     h.bt = align256(n * sizeof(DevSolve));
     h.bw = align256(std::max<size_t>(h.wm.size(), 1) * sizeof(int4));
     h.bf = align256(h.fm.size() * sizeof(int2));
@@ -677,17 +687,6 @@ atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cud
     return ATPM_OK;
 }
 
-atpm_status copy_forcing(atpm_solve* from, atpm_solve* to, cudaStream_t st) {
-    if (from->nf != to->nf || from->P.ntau != to->P.ntau || from->rs != to->rs)
-        return fail(ATPM_E_INVALID, "copy_forcing: solves differ in size or precision");
-    const size_t nt = (size_t)from->nf * from->P.ntau;
-    CK(cudaMemcpyAsync(to->ds.shadow, from->ds.shadow, nt, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(to->ds.cosil, from->ds.cosil, nt * from->rs, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(to->ds.Efm, from->ds.Efm, nt * from->rs, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(to->ds.E, from->ds.E, nt * from->rs, cudaMemcpyDeviceToDevice, st));
-    to->have_forcing = true;
-    return ATPM_OK;
-}
 }  // namespace atpm
 
 // =================================================================== C ABI
@@ -746,7 +745,15 @@ ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* sh, const atpm_param
     // transient peak: geometry (hp, hm, nrm, dist) or scattering work
     const size_t geo = (size_t)sh->nv * P->ntau * 24 + nt * 56 + (size_t)P->ntau * 16;
     const size_t sct = 3 * nt * rs;
-    *bytes = (uint64_t)(L.total + std::max(geo, sct) + 64 * 1024);
+    // FAST with self-heating: this solve's BF16 W tiles (hi + lo; the view-
+    // factor tiles are shared with the solve it is cloned from)
+    size_t wb = 0;
+    if (P->precision == ATPM_FAST && sh->dep_ptr[sh->nf] > 0 && tc_enabled()) {
+        int N, nch;
+        tc_chunks(P->ntau, &N, &nch);
+        wb = align256((size_t)((sh->nf + 63) / 64) * nch * N * 64 * 2 * 2);
+    }
+    *bytes = (uint64_t)(L.total + wb + std::max(geo, sct) + 64 * 1024);
     return ATPM_OK;
 }
 
@@ -871,18 +878,16 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->wmap) cudaFree(s->wmap);
     if (s->fmap) cudaFree(s->fmap);
     if (s->ds_dev) cudaFree(s->ds_dev);
-    if (s->tc_mem) cudaFree(s->tc_mem);
+    if (s->tc && --s->tc->refs == 0) {
+        cudaFree(s->tc->mem);
+        delete s->tc;
+    }
+    if (s->wb_mem) cudaFree(s->wb_mem);
     if (s->qmap) cudaFree(s->qmap);
     if (s->arena) cudaFree(s->arena);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return ATPM_OK;
-}
-
-// the address at the same offset from `to` as p is from `from`
-static void* rebase_ptr(const void* p, const void* from, void* to) {
-    if (!p) return nullptr;
-    return static_cast<char*>(to) + (static_cast<const char*>(p) - static_cast<const char*>(from));
 }
 
 ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
@@ -922,18 +927,15 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
         e = cudaMemcpyAsync(s->wmap, src->wmap, (size_t)s->nw * sizeof(int4), cudaMemcpyDeviceToDevice, s->st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->fmap, src->fmap, (size_t)s->nfb * sizeof(int2), cudaMemcpyDeviceToDevice, s->st);
-    if (e == cudaSuccess && src->tc_mem) {
-        e = cudaMalloc(&s->tc_mem, src->tc_bytes);
+    if (e == cudaSuccess && src->tc) {
+        // the tiles are read-only: shared; W is this solve's own
+        s->tc = src->tc;
+        ++s->tc->refs;
+        e = cudaMalloc(&s->wb_mem, src->wb_bytes);
         if (e == cudaSuccess) {
-            s->tc_bytes = src->tc_bytes;
-            e = cudaMemcpyAsync(s->tc_mem, src->tc_mem, s->tc_bytes, cudaMemcpyDeviceToDevice, s->st);
-            DevSolve& d = s->ds;
-            d.tc_ptr = static_cast<const int*>(rebase_ptr(d.tc_ptr, src->tc_mem, s->tc_mem));
-            d.tc_col = static_cast<const int*>(rebase_ptr(d.tc_col, src->tc_mem, s->tc_mem));
-            d.tc_tiles = rebase_ptr(d.tc_tiles, src->tc_mem, s->tc_mem);
-            d.tc_lo = static_cast<const int*>(rebase_ptr(d.tc_lo, src->tc_mem, s->tc_mem));
-            d.tc_lo_tiles = rebase_ptr(d.tc_lo_tiles, src->tc_mem, s->tc_mem);
-            d.Wb = rebase_ptr(d.Wb, src->tc_mem, s->tc_mem);
+            s->wb_bytes = src->wb_bytes;
+            e = cudaMemcpyAsync(s->wb_mem, src->wb_mem, s->wb_bytes, cudaMemcpyDeviceToDevice, s->st);
+            s->ds.Wb = s->wb_mem;
         }
     }
     if (e == cudaSuccess && src->qmap) {

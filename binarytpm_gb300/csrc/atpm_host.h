@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -29,6 +30,16 @@ struct atpm_context {
     std::map<uint64_t, atpm_tune_choice> tune;  // by batch kind
 };
 
+// Read-only tensor-core view-factor tiles of one shape (FAST), shared by a
+// solve and its clones: tiles | row-block tile ranges | column blocks |
+// residual tiles | residual index | (row block, column block) slot table.
+struct TcShared {
+    std::atomic<int> refs{1};
+    void* mem = nullptr;
+    size_t bytes = 0;
+    std::vector<int> rb_tiles;  // tiles per 128-facet row block (work ordering)
+};
+
 struct atpm_solve {
     atpm_context* ctx = nullptr;
     atpm_params P{};
@@ -42,8 +53,9 @@ struct atpm_solve {
     int4* wmap = nullptr;
     int2* fmap = nullptr;
     int nw = 0, nfb = 0;
-    void* tc_mem = nullptr;   // tensor-core tiles + W tiles (FAST)
-    size_t tc_bytes = 0;
+    TcShared* tc = nullptr;   // tensor-core tiles (FAST), shared with clones
+    void* wb_mem = nullptr;   // this solve's BF16 W tiles
+    size_t wb_bytes = 0;
     int4* qmap = nullptr;
     int nq = 0;
     cudaGraphExec_t graph = nullptr;
@@ -72,7 +84,5 @@ namespace atpm {
 // device buffer of at least batch_table_bytes(solves, n) bytes
 size_t batch_table_bytes(atpm_solve* const* solves, int n);
 atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st);
-// copy the forcing (shadow, Sun angle, illumination) of `from` into `to`
-atpm_status copy_forcing(atpm_solve* from, atpm_solve* to, cudaStream_t st);
 atpm_status fail_status(atpm_status s, const char* msg);
 }  // namespace atpm

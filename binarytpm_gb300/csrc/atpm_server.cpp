@@ -8,10 +8,11 @@
 //     shadowing and scattered sunlight are computed on the device and kept as
 //     a prototype solve, so each request only carries its thermal inertia;
 //   * a request is admitted when a batch slot is free and its device
-//     footprint fits the HBM budget left by the resident solves; its forcing
-//     is copied device-to-device from the prototype and its temperatures are
-//     initialised on a setup stream, so admission overlaps the revolutions of
-//     the solves already running;
+//     footprint fits the HBM budget left by the resident solves; it is a
+//     device copy of the prototype (atpm_solve_clone: forcing, and the
+//     prototype's tensor-core tiles shared) with its own temperatures, so
+//     admission does no host work on the shape and overlaps the revolutions
+//     of the solves already running;
 //   * every scheduler tick advances all resident solves by K revolutions in
 //     shared launches (one batch table, the tensor-core and conduction
 //     kernels span every solve) and retires the ones that converged or hit
@@ -101,11 +102,10 @@ namespace {
 atpm_status admit(atpm_server* S, Request* r) {
     ShapeEntry& sh = *S->shapes[r->shape];
     atpm_solve* s = nullptr;
-    atpm_status st = atpm_solve_create(S->ctx, &sh.shape, &sh.params, &s);
+    // a device copy of the prototype: forcing and (shared) tensor-core tiles
+    // come along, no host work on the shape
+    atpm_status st = atpm_solve_clone(sh.proto, &s);
     if (st) return st;
-    st = atpm::copy_forcing(sh.proto, s, S->setup_st);
-    if (!st && cudaStreamSynchronize(S->setup_st) != cudaSuccess)
-        st = atpm::fail_status(ATPM_E_CUDA, "server: forcing copy failed");
     if (!st) st = atpm_set_thermal_inertia(s, r->ti);
     if (!st && r->ti != 0.0f) st = atpm_initialise_temperatures(s);
     if (st) {
