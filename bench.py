@@ -327,7 +327,7 @@ def main():
         err = accuracy(ctx, prob, tis, shadow, illum)
 
     # end to end through the C ABI from host buffers
-    e2e = e2e_run(ctx, prob, tis, max(1, min(args.steps, 2)))
+    e2e = e2e_run(ctx, prob, tis, max(1, min(args.steps, 3)))  # median: the first pins read-back buffers
 
     serve = serving(ctx, args.serve_requests, args.serve_rate) if args.serve_requests > 0 else None
 

@@ -330,26 +330,39 @@ void set_tc_map(Batch& b, const int4* dev_map, size_t entries) {
 
 // block-sparse BF16 tiles of the view-factor matrix (128 x 64, swizzled)
 atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
-    // tile structure on the host (one pass over the lists): which 64-facet
-    // column blocks each 128-facet row block touches, the largest view factor
-    // of each tile; the BF16 values are filled on the device (k_tc_fill) from
-    // the lists already uploaded
+    // tile structure: which 64-facet column blocks each 128-facet row block
+    // touches, the largest view factor and K-slice mask of each tile (one
+    // device pass over the uploaded lists, k_tc_cells); the tile tables are
+    // laid out on the host from those cells, the BF16 values filled on the
+    // device (k_tc_fill)
     const int nf = s->nf, ntau = s->P.ntau;
     const int nmb = (nf + 127) / 128, nkb = (nf + 63) / 64;
     int N, nch;
     tc_chunks(ntau, &N, &nch);
     const size_t ncell = (size_t)nmb * nkb;
     if (nkb >= (1 << 24)) return fail(ATPM_E_UNSUPPORTED, "tensor-core tiles: %d facets exceed the column-block index", nf);
+    (void)sh;
     std::vector<float> vm(ncell, -1.0f);
     std::vector<uint8_t> km(ncell, 0);  // which 16-wide K slices of the tile hold an entry
-    for (int f = 0; f < nf; ++f) {
-        float* row = vm.data() + (size_t)(f / 128) * nkb;
-        uint8_t* mrow = km.data() + (size_t)(f / 128) * nkb;
-        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
-            const int g = sh->dep_idx[k];
-            float& c = row[g / 64];
-            c = std::max(c, std::fabs(sh->dep_vf[k]));
-            mrow[g / 64] |= (uint8_t)(1u << ((g % 64) / 16));
+    {
+        std::vector<unsigned> cmax(ncell), cmask(ncell);
+        unsigned* dc = nullptr;
+        CK(cudaMalloc((void**)&dc, ncell * 2 * sizeof(unsigned)));
+        cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 2 * sizeof(unsigned), s->st);
+        if (e == cudaSuccess && launch_tc_cells(s->ds, nkb, dc, dc + ncell, s->st)) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cmax.data(), dc, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(cmask.data(), dc + ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        cudaFree(dc);
+        if (e != cudaSuccess) return fail(ATPM_E_CUDA, "tile structure: %s", cudaGetErrorString(e));
+        for (size_t c = 0; c < ncell; ++c) {
+            if (!cmax[c]) continue;
+            uint32_t bits = cmax[c] - 1u;
+            float v;
+            std::memcpy(&v, &bits, 4);
+            vm[c] = v;
+            km[c] = (uint8_t)cmask[c];
         }
     }
     std::vector<int> tptr(nmb + 1, 0), tcol, slot(ncell, -1), lo_of;

@@ -196,6 +196,10 @@ int kernels_per_revolution(const Batch& b);          // kernels launch_revolutio
 // BF16 view-factor tiles (and residual tiles) of a solve from its uploaded
 // lists: slot[mb * nkb + kb] = tile of (row block, column block), lo_of[t] =
 // residual tile of tile t or -1; tiles must be zeroed (atpm_spmm_tc.cu)
+// per (row block, column block) cell of the view-factor lists: largest
+// |value| as float bits + 1 (0: no entry) and the mask of 16-wide K slices
+// with an entry; cmax and cmask zeroed by the caller (atpm_spmm_tc.cu)
+int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, stream_t st);
 int launch_tc_fill(const DevSolve& s, int nkb, const int* slot, const int* lo_of, void* tiles, void* lo_tiles,
                    stream_t st);
 // part 0 W, 1 Q, 2 conduction, 3 convergence, 4 advance

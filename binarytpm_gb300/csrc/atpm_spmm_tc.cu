@@ -166,6 +166,31 @@ __device__ __forceinline__ uint16_t bf16_rne(float x) {
     return (uint16_t)(u >> 16);
 }
 
+// tile structure from the uploaded lists, one warp per facet row: for every
+// (128-facet row block, 64-facet column block) cell the largest |view
+// factor| (its float bits + 1, so 0 marks an empty cell: max and or do not
+// depend on the order the entries arrive in) and the mask of 16-wide K
+// slices holding an entry
+__global__ void __launch_bounds__(256) k_tc_cells(DevSolve s, int nkb, unsigned* cmax, unsigned* cmask) {
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (f >= s.nf) return;
+    const size_t row = (size_t)(f >> 7) * nkb;
+    for (int k = s.dep_ptr[f] + lane; k < s.dep_ptr[f + 1]; k += 32) {
+        const int g = s.dep_idx[k];
+        const size_t cell = row + (size_t)(g >> 6);
+        atomicMax(&cmax[cell], __float_as_uint(fabsf(s.dep_vf[k])) + 1u);
+        atomicOr(&cmask[cell], 1u << ((g & 63) >> 4));
+    }
+}
+
+int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t threads = (size_t)s.nf * 32;
+    k_tc_cells<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, cmax, cmask);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 // one warp per facet row: every list entry goes to its swizzled slot of its
 // (row block, column block) tile, plus the BF16 residual where the tile has one
 __global__ void __launch_bounds__(256) k_tc_fill(DevSolve s, int nkb, const int* slot, const int* lo_of,
