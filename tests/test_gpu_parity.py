@@ -151,3 +151,33 @@ def test_clone_matches_a_solve_set_up_from_host_arrays(gpu_ctx, precision):
         c.close()
         h.close()
 
+
+def test_clone_outlives_its_source(gpu_ctx):
+    """A clone shares the source's view-factor tiles (reference-counted): it
+    keeps working after the source is destroyed, and several clones of one
+    solve advance together in a batch like independently created solves."""
+    from binarytpm_gb300 import lib
+
+    prob, _ = golden("binary_s3s1")
+    s0 = lib.Solve(gpu_ctx, prob, precision=lib.FAST, revcap=60)
+    s0.geometry_shadow()
+    s0.scattering()
+    sh, il = s0.shadow(), s0.illumination()
+    clones = [s0.clone() for _ in range(3)]
+    s0.close()
+    fresh = []
+    for ti in (50.0, 200.0, 800.0):
+        h = lib.Solve(gpu_ctx, prob, precision=lib.FAST, revcap=60)
+        h.set_forcing(sh, il)
+        fresh.append(h)
+    for group in (clones, fresh):
+        for s, ti in zip(group, (50.0, 200.0, 800.0)):
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+    nc, nf = lib.batch_run(clones), lib.batch_run(fresh)
+    for c, h, a, b in zip(clones, fresh, nc, nf):
+        assert np.array_equal(a, b)
+        assert np.array_equal(c.surface_temperature()[0].view(np.uint32), h.surface_temperature()[0].view(np.uint32))
+    for s in clones + fresh:
+        s.close()
+
