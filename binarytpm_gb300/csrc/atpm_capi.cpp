@@ -20,6 +20,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/atpm.h"
@@ -1140,6 +1141,68 @@ ATPM_API atpm_status atpm_run(atpm_solve* s, int32_t* nrev, int32_t* counts) {
     return atpm_batch_run(one, 1, nrev, counts);
 }
 
+// Solves of one atpm_batch_run are advanced in two groups (even / odd
+// positions), each with its own stream and revolution graph: one group's
+// small late-revolution kernels and kernel tails overlap the other's work.
+// ATPM_BATCH_STREAMS=1 keeps one group.  Each solve's arithmetic does not
+// depend on the group it runs in.
+int batch_streams() {
+    const char* e = std::getenv("ATPM_BATCH_STREAMS");
+    return (e && e[0] == '1' && e[1] == 0) ? 1 : 2;
+}
+
+namespace {
+struct LoopOut {
+    atpm_status st = ATPM_OK;
+    std::string err;
+    int64_t launches = 0;
+};
+
+// the revolution loop of one group on its leader's stream: the graph of one
+// revolution, replayed in chunks that double up to 32 revolutions, the
+// solves' control words read back after each chunk
+LoopOut revolution_loop(atpm_solve* const* solves, int n, const Batch& b, int maxcap, int done_revs,
+                        std::vector<Ctl>& ctl) {
+    LoopOut o;
+    atpm_solve* lead = solves[0];
+    if (cudaSetDevice(lead->ctx->device) != cudaSuccess) {
+        o.st = fail(ATPM_E_CUDA, "cudaSetDevice");
+        o.err = g_err;
+        return o;
+    }
+    cudaGraphExec_t gx = nullptr;
+    atpm_status r = capture_graph(lead, b, &gx);
+    if (r) {
+        o.st = r;
+        o.err = g_err;
+        return o;
+    }
+    cudaError_t e = cudaSuccess;
+    int chunk = 4;
+    while (e == cudaSuccess && done_revs < maxcap) {
+        const int k = std::min(chunk, maxcap - done_revs);
+        for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaGraphLaunch(gx, lead->st);
+        o.launches += (int64_t)k * kernels_per_revolution(b);
+        done_revs += k;
+        if (e != cudaSuccess) break;
+        e = cudaEventRecord(lead->ev1, lead->st);
+        bool any = false;
+        for (int i = 0; i < n && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(&ctl[i], solves[i]->ds.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, lead->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(lead->st);
+        for (int i = 0; i < n; ++i) any = any || ctl[i].active;
+        if (!any) break;
+        chunk = std::min(chunk * 2, 32);
+    }
+    cudaGraphExecDestroy(gx);
+    if (e != cudaSuccess) {
+        o.st = fail(ATPM_E_CUDA, "revolution loop: %s", cudaGetErrorString(e));
+        o.err = g_err;
+    }
+    return o;
+}
+}  // namespace
+
 ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_t* nrev, int32_t* counts) {
     if (!solves || n < 1) return fail(ATPM_E_INVALID, "empty batch");
     atpm_solve* s0 = solves[0];
@@ -1152,72 +1215,96 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
             return fail(ATPM_E_STATE, "solve %d: forcing and initial temperatures required", i);
     }
     CK(cudaSetDevice(s0->ctx->device));
-    // all solves must be ready before s0's stream runs the batch
+    // all solves must be ready before their group's stream runs them
     for (int i = 1; i < n; ++i) CK(cudaStreamSynchronize(solves[i]->st));
-    Batch b;
-    void* tmp = nullptr;
-    atpm_status rb = make_batch_for(solves, n, &b, &tmp);
-    if (rb) return rb;
-    int maxcap = 0;
-    for (int i = 0; i < n; ++i) maxcap = std::max(maxcap, solves[i]->P.revcap);
-    std::vector<Ctl> ctl(n);
-    int done_revs = 0;
-    int chunk = 4;
+    const int ng = (n >= 2 && batch_streams() >= 2) ? 2 : 1;
+    std::vector<std::vector<atpm_solve*>> gs(ng);
+    std::vector<std::vector<int>> gi(ng);
+    for (int i = 0; i < n; ++i) {
+        gs[i % ng].push_back(solves[i]);
+        gi[i % ng].push_back(i);
+    }
+    std::vector<Batch> bs(ng);
+    std::vector<void*> tmps(ng, nullptr);
+    auto free_tmps = [&]() {
+        for (void* t : tmps)
+            if (t) cudaFree(t);
+    };
+    for (int g = 0; g < ng; ++g) {
+        atpm_status rb = make_batch_for(gs[g].data(), (int)gs[g].size(), &bs[g], &tmps[g]);
+        if (rb) { free_tmps(); return rb; }
+    }
+    std::vector<int> maxcap(ng, 0);
+    int maxcap_all = 0;
+    for (int g = 0; g < ng; ++g)
+        for (atpm_solve* s : gs[g]) maxcap[g] = std::max(maxcap[g], s->P.revcap);
+    for (int g = 0; g < ng; ++g) maxcap_all = std::max(maxcap_all, maxcap[g]);
     int64_t launches = 0;
-    // the timed region starts before any revolution, tuning ones included
-    cudaError_t e = cudaEventRecord(s0->ev0, s0->st);
     int tuned = 0;
-    if (e == cudaSuccess && b.mode == MODE_FAST) {
-        const bool ok = autotune_enabled();
-        if (!ok) {
-            b.cond_variant = cond_variant();
-            b.tc_stages = 0;
+    std::vector<int> done(ng, 0);
+    // the timed region starts before any revolution, tuning ones included,
+    // on every group's stream
+    cudaError_t e = cudaEventRecord(s0->ev0, s0->st);
+    for (int g = 1; g < ng && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(gs[g][0]->st, s0->ev0, 0);
+    if (e != cudaSuccess) { free_tmps(); return fail(ATPM_E_CUDA, "batch start: %s", cudaGetErrorString(e)); }
+    if (bs[0].mode == MODE_FAST) {
+        if (!autotune_enabled()) {
+            bs[0].cond_variant = cond_variant();
+            bs[0].tc_stages = 0;
         } else {
-            atpm_status rt = autotune(s0, b, maxcap, &done_revs, &launches, &tuned);
-            if (rt) { if (tmp) cudaFree(tmp); return rt; }
+            // group 0 tunes (if this kind of batch has not been), the others take its choice
+            atpm_status rt = autotune(s0, bs[0], maxcap[0], &done[0], &launches, &tuned);
+            if (rt) { free_tmps(); return rt; }
+        }
+        for (int g = 1; g < ng; ++g) {
+            bs[g].cond_variant = bs[0].cond_variant;
+            bs[g].tc_stages = bs[0].tc_stages;
         }
     }
-    cudaGraphExec_t gx = nullptr;
-    atpm_status r = capture_graph(s0, b, &gx);
-    if (r) { if (tmp) cudaFree(tmp); return r; }
-    while (e == cudaSuccess && done_revs < maxcap) {
-        const int k = std::min(chunk, maxcap - done_revs);
-        for (int j = 0; j < k && e == cudaSuccess; ++j) e = cudaGraphLaunch(gx, s0->st);
-        launches += (int64_t)k * kernels_per_revolution(b);
-        done_revs += k;
-        if (e != cudaSuccess) break;
-        e = cudaEventRecord(s0->ev1, s0->st);
-        bool any = false;
-        for (int i = 0; i < n && e == cudaSuccess; ++i)
-            e = cudaMemcpyAsync(&ctl[i], solves[i]->ds.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s0->st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s0->st);
-        for (int i = 0; i < n; ++i) any = any || ctl[i].active;
-        if (!any) break;
-        chunk = std::min(chunk * 2, 32);
+    std::vector<std::vector<Ctl>> ctl(ng);
+    for (int g = 0; g < ng; ++g) ctl[g].resize(gs[g].size());
+    std::vector<LoopOut> outs(ng);
+    {
+        std::vector<std::thread> workers;
+        for (int g = 1; g < ng; ++g)
+            workers.emplace_back([&, g]() {
+                outs[g] = revolution_loop(gs[g].data(), (int)gs[g].size(), bs[g], maxcap[g], done[g], ctl[g]);
+            });
+        outs[0] = revolution_loop(gs[0].data(), (int)gs[0].size(), bs[0], maxcap[0], done[0], ctl[0]);
+        for (auto& w : workers) w.join();
     }
-    cudaGraphExecDestroy(gx);
-    if (tmp) cudaFree(tmp);
-    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "revolution loop: %s", cudaGetErrorString(e));
+    free_tmps();
+    for (int g = 0; g < ng; ++g) {
+        launches += outs[g].launches;
+        if (outs[g].st) return fail(outs[g].st, "%s", outs[g].err.c_str());
+    }
     float ms = 0.0f;
-    CK(cudaEventElapsedTime(&ms, s0->ev0, s0->ev1));
+    for (int g = 0; g < ng; ++g) {
+        float m = 0.0f;
+        CK(cudaEventElapsedTime(&m, s0->ev0, gs[g][0]->ev1));
+        ms = std::max(ms, m);
+    }
     int64_t fsteps_total = 0;
     atpm_status worst = ATPM_OK;
-    for (int i = 0; i < n; ++i) {
-        atpm_solve* s = solves[i];
-        std::vector<int32_t> cnt(s->P.revcap);
-        int st = 0;
-        CK(cudaMemcpy(cnt.data(), s->ds.counts, (size_t)s->P.revcap * 4, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(&st, s->ds.status, 4, cudaMemcpyDeviceToHost));
-        const int nr = ctl[i].rev;
-        if (nrev) nrev[i] = nr;
-        if (counts) std::memcpy(counts + (size_t)i * maxcap, cnt.data(), (size_t)s->P.revcap * 4);
-        const int64_t fs = facet_steps_from_counts(cnt.data(), nr, s->nf, s->P.ntau, s->ti == 0.0f || !s->P.freeze);
-        s->last_nrev = nr;
-        s->last_facet_steps = fs;
-        fsteps_total += fs;
-        atpm_status r2 = check_status(s, st);
-        if (r2 && !worst) worst = r2;
-    }
+    for (int g = 0; g < ng; ++g)
+        for (size_t j = 0; j < gs[g].size(); ++j) {
+            atpm_solve* s = gs[g][j];
+            const int i = gi[g][j];
+            std::vector<int32_t> cnt(s->P.revcap);
+            int st = 0;
+            CK(cudaMemcpy(cnt.data(), s->ds.counts, (size_t)s->P.revcap * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(&st, s->ds.status, 4, cudaMemcpyDeviceToHost));
+            const int nr = ctl[g][j].rev;
+            if (nrev) nrev[i] = nr;
+            if (counts) std::memcpy(counts + (size_t)i * maxcap_all, cnt.data(), (size_t)s->P.revcap * 4);
+            const int64_t fs = facet_steps_from_counts(cnt.data(), nr, s->nf, s->P.ntau, s->ti == 0.0f || !s->P.freeze);
+            s->last_nrev = nr;
+            s->last_facet_steps = fs;
+            fsteps_total += fs;
+            atpm_status r2 = check_status(s, st);
+            if (r2 && !worst) worst = r2;
+        }
+    const Batch& b = bs[0];
     s0->last_ms = ms;
     s0->last_launches = launches;
     s0->last_facet_steps = fsteps_total;
