@@ -230,11 +230,9 @@ struct FluxArgs {
 size_t flux_partial_bytes(const DevSolve& s, int nwl);
 int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t st);
 // tensor-core self-heating (atpm_spmm_tc.cu)
-int launch_w_bf16(const Batch& b, stream_t st);
 int launch_w_bf16_one(const DevSolve& s, stream_t st);
 int launch_spmm_tc(const Batch& b, stream_t st);
 size_t spmm_tc_smem_bytes(int N, int stages = 0);  // 0: deepest ring that fits
-uint32_t tc_swizzle_offset(uint32_t row, uint32_t k);
 int tc_max_chunk();  // largest step chunk N of the tensor-core product
 bool conduction_nx_supported(int nx);
 

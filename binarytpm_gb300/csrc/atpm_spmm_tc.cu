@@ -15,17 +15,22 @@
 // are skipped: their flux is not read.
 //
 // V is stored as 128 x 64 BF16 tiles (block-sparse rows: every 128-facet row
-// block keeps the 64-facet column blocks it touches) and W as 64-facet x N-step
-// tiles.  Both are laid out in HBM already in the 128-byte-swizzled K-major
-// form the tensor core reads, so each tile moves with one bulk copy
-// (cp.async.bulk) into a 4-stage shared-memory ring.  One elected thread
-// issues tcgen05.mma (M = 128, N = step chunk, K = 16) into a TMEM
-// accumulator; the four warps then drain TMEM with tcgen05.ld and write Q
-// coalesced along facets.
+// block keeps the 64-facet column blocks it touches; one set per shape,
+// shared by clones) and W as 64-facet x N-step tiles (per solve, written by
+// the conduction sweep).  Both are laid out in HBM already in the
+// 128-byte-swizzled K-major form the tensor core reads, so each tile moves
+// with one bulk copy (cp.async.bulk) into a shared-memory stage ring.  The
+// product kernel is persistent (one CTA per SM) and warp-specialised: a
+// producer warp takes work items (row block x step chunk) by ticket from the
+// list k_tc_compact builds before each launch and streams their tiles, an MMA
+// warp issues tcgen05.mma (M = 128, N = step chunk, K = 16) into one of two
+// TMEM accumulators, and four epilogue warps drain the other with
+// tcgen05.ld and write Q coalesced along facets.  All-zero 16-wide K slices
+// of a tile are not issued.
 //
 // Every mbarrier wait is bounded (about one second of clock cycles); a
-// timeout sets ST_TC_TIMEOUT in the solve's status word and the block drains
-// and frees its TMEM instead of spinning.
+// timeout sets ST_TC_TIMEOUT in the solve's status word and the roles stop,
+// let their copies and products land and free TMEM instead of spinning.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -155,7 +160,6 @@ __host__ __device__ inline int tc_stages(int N) {
 
 }  // namespace
 
-uint32_t tc_swizzle_offset(uint32_t row, uint32_t k) { return swz(row, k); }
 int tc_max_chunk() { return 160; }
 
 // float -> BF16, round to nearest even (quiet NaN for NaN), as the host's f2bf
@@ -219,29 +223,6 @@ int launch_tc_fill(const DevSolve& s, int nkb, const int* slot, const int* lo_of
     k_tc_fill<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, lo_of, static_cast<uint16_t*>(tiles),
                                                                    static_cast<uint16_t*>(lo_tiles));
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
-}
-
-// W = eps sigma T^4 in BF16, written as (column block, step chunk) tiles
-__global__ void __launch_bounds__(256) k_w_bf16(Batch b) {
-    const int4 t = b.wmap[blockIdx.x];
-    const DevSolve& sv = b.tab[t.x];
-    if (!sv.ctl->active || !sv.tc_tiles) return;
-    const int nf = sv.nf, ntau = sv.ntau, N = sv.tc_n, nch = sv.tc_nchunks;
-    const float* T = static_cast<const float*>(sv.stemp1);
-    __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
-    const float es = sv.es_w;
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const int s = t.z + j, f = t.y + threadIdx.x;
-        if (s >= ntau || f >= nf) continue;
-        const float x = T[(size_t)s * nf + f];
-        const float x2 = x * x;
-        const float w = es * (x2 * x2);
-        const int kb = f / TC_K, k = f % TC_K, nc = s / N, n = s % N;
-        const size_t base = ((size_t)kb * nch + nc) * (size_t)2 * N * TC_K;
-        const __nv_bfloat16 hi = __float2bfloat16_rn(w);
-        W[base + swz(n, k)] = hi;
-        W[base + (size_t)N * TC_K + swz(n, k)] = __float2bfloat16_rn(w - __bfloat162float(hi));
-    }
 }
 
 // Work items whose row block has an active facet, compacted before every
@@ -530,13 +511,6 @@ int launch_w_bf16_one(const DevSolve& s, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const size_t n = (size_t)s.nf * s.ntau;
     k_w_bf16_one<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s);
-    return cudaGetLastError() == cudaSuccess ? 0 : 2;
-}
-
-int launch_w_bf16(const Batch& b, stream_t stv) {
-    cudaStream_t st = static_cast<cudaStream_t>(stv);
-    if (b.nw == 0) return 0;
-    k_w_bf16<<<b.nw, dim3(32, 8), 0, st>>>(b);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
