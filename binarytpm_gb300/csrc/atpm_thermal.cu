@@ -8,11 +8,17 @@
 //
 //   k_selfheat_w   W[f][s] = eps*sigma*T_{r-1}[s][f]^4          (transpose)
 //   k_selfheat_q   Q[s][f] = sum_k W[g_k][s] * vf_k  (list order)  -- A6
+//                  (FAST: the tensor-core product of atpm_spmm_tc.cu)
 //   k_conduction   depth column in registers, NTAU steps, Newton BC -- A1
+//                  (FAST: over the active-facet list once at most half a
+//                  solve is active)
+//   k_tail_mode, k_conduction_warp   FAST late revolutions: one warp per
+//                  active facet once the batch has few of them
 //   k_converge     shape_converged (main.cpp:1876-1909)             -- A4
+//                  (+ the active-facet lists and row-block activity)
 //   k_advance      revolution counter / stop rule (main.cpp:2522-2539)
 //
-// All five read the per-solve control word and return at once for solves
+// All of them read the per-solve control word and return at once for solves
 // that have stopped, so the same launch sequence (or a captured graph of it)
 // can be replayed until every solve in the batch is done.
 #include <cuda_runtime.h>
