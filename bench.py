@@ -198,6 +198,29 @@ def profile_case(nsolves: int = 2):
     print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz, "tiles": tiles, "lo_tiles": lo}))
 
 
+def precision_stress(p_subdiv: int):
+    """The precision-stress configuration: concave 81,920-facet primary +
+    5,120-facet secondary (workloads.stress_problem), view factors on the
+    GPU, FAST vs plain FP64 on the same schedule at two thermal inertias."""
+    from binarytpm_gb300 import lib, workloads
+
+    ctx = lib.Context(0)
+    t0 = time.perf_counter()
+    prob = workloads.stress_problem(ctx, p_subdiv=p_subdiv)
+    vf_s = time.perf_counter() - t0
+    s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    s0.geometry_shadow()
+    s0.scattering()
+    shadow, illum = s0.shadow(), s0.illumination()
+    s0.close()
+    tiles, lo = _tile_stats(prob)
+    t1 = time.perf_counter()
+    err = workloads.fast_vs_fp64(ctx, prob, [50.0, 800.0], ACC_REVS, shadow, illum)
+    print(json.dumps({"precision_stress": err, "workload": prob.name, "nf": prob.nf, "nnz": int(prob.nnz),
+                      "mean_list_length": prob.nnz / prob.nf, "tiles": tiles, "lo_tiles": lo,
+                      "viewfactor_s": vf_s, "comparison_s": time.perf_counter() - t1}), flush=True)
+
+
 def run_reference_arm(args, world, rank):
     if rank != 0:
         return
@@ -236,11 +259,16 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving run (1/s)")
     ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
+    ap.add_argument("--precision-stress", type=int, default=0, metavar="SUBDIV",
+                    help="run the precision-stress configuration with this primary subdivision (6: 81,920 facets)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: binary 5120+1280 facets, 2 solves, 3 instrumented revolutions")
     args = ap.parse_args()
     if args.prepare:
         print(prepare())
+        return
+    if args.precision_stress:
+        precision_stress(args.precision_stress)
         return
     if args.profile_case:
         profile_case(args.profile_solves)
@@ -422,54 +450,24 @@ ACC_REVS = 40
 
 
 def accuracy(ctx, prob, tis, shadow, illum):
-    """FAST (batched) vs plain FP64 after the same ACC_REVS revolutions with
-    every facet advancing every revolution (freeze off), so both runs follow
-    the same schedule: max |T_fast - T_fp64| over facets, steps and thermal
-    inertias, and the relative error of the disk-integrated 12 um flux seen
-    from the Sun, reduced in FP64 on the GPU (atpm_disk_flux)."""
-    from binarytpm_gb300 import lib
+    """FAST vs plain FP64 on the same schedule (workloads.fast_vs_fp64)."""
+    from binarytpm_gb300 import workloads
 
-    fast = [lib.Solve(ctx, prob, precision=lib.FAST, revcap=ACC_REVS, freeze=False) for _ in tis]
-    for s, ti in zip(fast, tis):
-        s.set_forcing(shadow, illum)
-        s.set_thermal_inertia(ti)
-        s.initialise_temperatures()
-    lib.batch_run(fast)
-    ref = lib.Solve(ctx, prob, precision=lib.FP64, revcap=ACC_REVS, freeze=False)
-    ref.set_forcing(shadow, illum)
-    errs, ferrs = {}, {}
-    for s, ti in zip(fast, tis):
-        ref.set_thermal_inertia(ti)
-        ref.initialise_temperatures()
-        ref.run()
-        t64 = ref.surface_temperature64()
-        t32 = s.surface_temperature64()
-        errs[str(ti)] = float(np.max(np.abs(t32 - t64)))
-        F64 = ref.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
-        F32 = s.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
-        ferrs[str(ti)] = float(np.max(np.abs(F32 - F64) / np.abs(F64)))
-        s.close()
-    ref.close()
-    return {"max_temperature_error_K": max(errs.values()), "max_rel_flux_error_12um": max(ferrs.values()),
-            "per_ti_max_K": errs, "per_ti_rel_flux": ferrs,
-            "schedule": f"{ACC_REVS} revolutions, every facet advancing (freeze off), same forcing"}
+    return workloads.fast_vs_fp64(ctx, prob, tis, ACC_REVS, shadow, illum)
 
 
 def _tile_stats(prob, slices=False):
     """Tile structure of the FAST tensor-core product: 128x64 tiles touched,
-    how many of them carry the residual (a view factor >= 1e-4), and with
-    ``slices`` the 128x16 K slices holding an entry (all tiles; residual
+    how many of them carry the residual (workloads.tc_tile_structure), and
+    with ``slices`` the 128x16 K slices holding an entry (all tiles; residual
     tiles): the products the kernel issues."""
-    rows = np.repeat(np.arange(prob.nf), np.diff(prob.dep_ptr))
-    key = (rows // 128).astype(np.int64) * ((prob.nf + 63) // 64) + prob.dep_idx // 64
-    u, inv = np.unique(key, return_inverse=True)
-    vmax = np.zeros(len(u), np.float32)
-    np.maximum.at(vmax, inv, np.abs(prob.dep_vf))
-    has_lo = vmax >= 1e-4
+    from binarytpm_gb300 import workloads
+
+    tiles, inv, sl, has_lo = workloads.tc_tile_structure(prob.nf, prob.dep_ptr, prob.dep_idx, prob.dep_vf)
     if not slices:
-        return len(u), int(has_lo.sum())
-    sk = np.unique(inv.astype(np.int64) * 4 + (prob.dep_idx % 64) // 16)
-    return len(u), int(has_lo.sum()), len(sk), int(has_lo[sk // 4].sum())
+        return len(tiles), int(has_lo.sum())
+    sk = np.unique(inv.astype(np.int64) * 4 + sl)
+    return len(tiles), int(has_lo.sum()), len(sk), int(has_lo[sk // 4].sum())
 
 
 def _roofline(kern, solves, prob, hbm, bf16, kind):

@@ -345,15 +345,19 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     (void)sh;
     std::vector<float> vm(ncell, -1.0f);
     std::vector<uint8_t> km(ncell, 0);  // which 16-wide K slices of the tile hold an entry
+    std::vector<unsigned> need(ncell, 0);  // the tile needs its residual for some row's flux
     {
         std::vector<unsigned> cmax(ncell), cmask(ncell);
         unsigned* dc = nullptr;
-        CK(cudaMalloc((void**)&dc, ncell * 2 * sizeof(unsigned)));
-        cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 2 * sizeof(unsigned), s->st);
+        CK(cudaMalloc((void**)&dc, ncell * 3 * sizeof(unsigned)));
+        cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 3 * sizeof(unsigned), s->st);
         if (e == cudaSuccess && launch_tc_cells(s->ds, nkb, dc, dc + ncell, s->st)) e = cudaGetLastError();
+        if (e == cudaSuccess && launch_tc_rowneed(s->ds, nkb, dc + 2 * ncell, s->st) == 2) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(cmax.data(), dc, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(cmask.data(), dc + ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(need.data(), dc + 2 * ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
         cudaFree(dc);
         if (e != cudaSuccess) return fail(ATPM_E_CUDA, "tile structure: %s", cudaGetErrorString(e));
@@ -376,7 +380,8 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
             // column block in the low 24 bits, K-slice mask in bits 24-27
             tcol.push_back(kb | ((int)km[(size_t)mb * nkb + kb] << 24));
             // residual tile V - bf16(V) where the tile holds a view factor >= 1e-4
-            lo_of.push_back(v >= 1e-4f ? nlo++ : -1);
+            // or carries a noticeable share of some row's mass (k_tc_rowneed)
+            lo_of.push_back(v >= 1e-4f || need[(size_t)mb * nkb + kb] ? nlo++ : -1);
         }
         tptr[mb + 1] = (int)tcol.size();
     }

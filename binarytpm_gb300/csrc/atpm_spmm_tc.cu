@@ -34,6 +34,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "atpm_internal.h"
@@ -195,6 +196,59 @@ int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask,
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+// Which tiles need the residual V_lo for the rows they serve.  BF16 rounding
+// of V is correlated between neighbouring entries of a smooth surface, so in
+// a row's flux its error can approach 2^-9 of the mass it applies to.  A warp
+// per facet row sums the row's |view factor| per 64-facet column block in
+// shared memory (fixed point, 2^-36 units, plus one unit per entry so a
+// touched block is never zero: the sums do not depend on the order of the
+// additions); a block holding at least 1 % of the row's mean per touched
+// block marks its tile.  The blocks left unmarked hold less than 1 % of the
+// row's view-factor mass between them.
+__global__ void k_tc_rowneed(DevSolve s, int nkb, unsigned* need) {
+    extern __shared__ unsigned long long mass_sm[];
+    const int warps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < warps * nkb; i += blockDim.x) mass_sm[i] = 0ull;
+    __syncthreads();
+    const int f = blockIdx.x * warps + warp;
+    if (f >= s.nf) return;  // warp-uniform; no block barrier follows
+    unsigned long long* m = mass_sm + (size_t)warp * nkb;
+    const int k0 = s.dep_ptr[f], k1 = s.dep_ptr[f + 1];
+    unsigned long long tot = 0;
+    unsigned touched = 0;
+    for (int k = k0 + lane; k < k1; k += 32) {
+        const unsigned long long q = __double2ull_rn((double)fabsf(s.dep_vf[k]) * 68719476736.0) + 1ull;
+        if (atomicAdd(&m[s.dep_idx[k] >> 6], q) == 0ull) ++touched;
+        tot += q;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        touched += __shfl_xor_sync(0xffffffffu, touched, o);
+    }
+    __syncwarp();
+    unsigned* row = need + (size_t)(f >> 7) * nkb;
+    for (int k = k0 + lane; k < k1; k += 32) {
+        const int kb = s.dep_idx[k] >> 6;
+        if (100ull * touched * m[kb] >= tot) atomicOr(&row[kb], 1u);
+    }
+}
+
+// 0: launched; 1: the row maps do not fit shared memory (very large shapes:
+// the caller keeps the absolute rule alone); 2: launch error
+int launch_tc_rowneed(const DevSolve& s, int nkb, unsigned* need, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t per_warp = (size_t)nkb * 8;
+    constexpr size_t kMax = 200 * 1024;
+    if (per_warp > kMax) return 1;
+    int warps = (int)std::min<size_t>(8, kMax / per_warp);
+    const size_t smem = per_warp * warps;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_tc_rowneed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 2;
+    k_tc_rowneed<<<(unsigned)((s.nf + warps - 1) / warps), warps * 32, smem, st>>>(s, nkb, need);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 // one warp per facet row: every list entry goes to its swizzled slot of its
 // (row block, column block) tile, plus the BF16 residual where the tile has one
 __global__ void __launch_bounds__(256) k_tc_fill(DevSolve s, int nkb, const int* slot, const int* lo_of,
@@ -260,6 +314,13 @@ __global__ void __launch_bounds__(128) k_tc_compact(Batch b) {
 // depend on which CTA computed it.
 constexpr int TC_THREADS = 192;
 constexpr int TC_QUEUE = 4;  // queued work items
+// Tiles accumulated in TMEM before the partial sum goes to Q: the tensor
+// core's FP32 accumulation of long runs of positive products drifts low
+// (measured -1.9e-5 relative on rows of ~3,700 entries summed in one
+// accumulator, -1.0e-5 with 64-tile segments, -4.4e-6 with 32), so a work
+// item is summed in segments of this many tiles, each a fresh accumulator,
+// and the epilogue adds the segments into Q in order with round-to-nearest.
+constexpr int TC_SEG = 64;
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
     extern __shared__ __align__(1024) unsigned char dyn[];
@@ -320,16 +381,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
             const int g = atomicAdd(&b.tc_work[1], 1);
             const bool stop = g >= nlist;
             const int4 it = stop ? make_int4(-1, 0, 0, 0) : b.tc_list[g];
-            {
-                // queue the item (or the stop item)
+            const int tall = stop ? 0 : b.tab[it.x].tc_ptr[it.y + 1] - b.tab[it.x].tc_ptr[it.y];
+            const int nseg = stop ? 1 : max(1, (tall + TC_SEG - 1) / TC_SEG);
+            for (int seg = 0; seg < nseg && ok; ++seg) {
+                // queue the item's segment (or the stop item)
                 if (!mbar_wait(&qempty[qs], qph ^ 1u)) { ok = false; break; }
-                qitem[qs] = it;
+                qitem[qs] = make_int4(it.x, it.y, it.z, seg);
                 mbar_arrive(&qfull[qs]);
                 if (++qs == TC_QUEUE) { qs = 0; qph ^= 1u; }
                 if (stop) break;
                 const DevSolve& sv = b.tab[it.x];
                 const int N = sv.tc_n, c = it.z;
-                const int t0 = sv.tc_ptr[it.y], T = sv.tc_ptr[it.y + 1] - t0;
+                const int t0 = sv.tc_ptr[it.y] + seg * TC_SEG, T = min(TC_SEG, tall - seg * TC_SEG);
                 const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;
                 const __nv_bfloat16* tiles = static_cast<const __nv_bfloat16*>(sv.tc_tiles);
                 const __nv_bfloat16* lo_tiles = static_cast<const __nv_bfloat16*>(sv.tc_lo_tiles);
@@ -348,7 +411,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
                     if (++slot == (uint32_t)S) { slot = 0; ph ^= 1u; }
                 }
             }
-            if (!ok) break;
+            if (!ok || stop) break;
         }
         if (!ok) atomicOr(status0, ST_TC_TIMEOUT);
         // copies still in flight exist only after a timeout: let them land
@@ -365,7 +428,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
             if (w.x < 0) break;
             const DevSolve& sv = b.tab[w.x];
             const int N = sv.tc_n;
-            const int t0 = sv.tc_ptr[w.y], T = sv.tc_ptr[w.y + 1] - t0;
+            const int tall = sv.tc_ptr[w.y + 1] - sv.tc_ptr[w.y];
+            const int t0 = sv.tc_ptr[w.y] + w.w * TC_SEG, T = max(0, min(TC_SEG, tall - w.w * TC_SEG));
             const uint32_t b_bytes = (uint32_t)N * TC_K * 2 * 2;
             const uint32_t ab = item_no & 1u, use_no = item_no >> 1;
             if (!mbar_wait(&tempty[ab], (use_no & 1u) ^ 1u)) { ok = false; break; }
@@ -432,15 +496,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
                         if (s < ntau) Q[(size_t)s * nf + f] = 0.0f;
                     }
             } else {
+                // the first segment stores, later ones add to Q in order
+                // (round to nearest); a batch's 16 loads all issue before
+                // its stores
                 const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + ab * kBufCols;
                 for (int c0 = 0; c0 < N; c0 += 16) {
                     float v[16];
                     tc_ld16(tbase + (uint32_t)c0, v);
                     if (f < nf) {
+                        float prev[16];
 #pragma unroll
                         for (int j = 0; j < 16; ++j) {
                             const int s = nc * N + c0 + j;
-                            if (c0 + j < N && s < ntau) Q[(size_t)s * nf + f] = v[j];
+                            prev[j] = (w.w > 0 && c0 + j < N && s < ntau) ? __ldcg(&Q[(size_t)s * nf + f]) : 0.0f;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const int s = nc * N + c0 + j;
+                            if (c0 + j < N && s < ntau) Q[(size_t)s * nf + f] = w.w == 0 ? v[j] : prev[j] + v[j];
                         }
                     }
                 }

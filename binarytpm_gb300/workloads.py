@@ -40,6 +40,58 @@ def binary_problem(ctx, p_subdiv=5, s_subdiv=3, ntau=720, nx=56, seed=2) -> P.Pr
                      thermal_inertia=200.0, tacc=0.005, name=f"binary_s{p_subdiv}s{s_subdiv}")
 
 
+def stress_problem(ctx, p_subdiv=6, s_subdiv=4, ntau=720, nx=56, seed=3) -> P.Problem:
+    """Precision stress: a concave primary (icosphere subdivision 6 = 81,920
+    facets, r = 0.39 km, seeded Gaussian-random-field radii, sigma 15 %,
+    correlation 0.3 rad) + a 5,120-facet secondary (subdivision 4, r = 0.08
+    km, +-8 %), merged 1.19 km apart like the binary; view factors from
+    mutual visibility on the GPU."""
+    from . import mesh
+
+    prim = mesh.grf_body(p_subdiv, 0.39, 0.15, 0.3, seed)
+    sec = mesh.perturbed_body(s_subdiv, 0.08, 0.08, seed + 1000)
+    v, f = mesh.binary_system(prim, sec, 1.19)
+    ptr, idx, vf = _lists(ctx, v, f)
+    return P.Problem(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf,
+                     ntau=ntau, nx=nx, polar=(1.0, 0.0, 0.0), pole=P.BINARY_POLE,
+                     rotation_period_s=11.9 * 3600.0, albedo=0.02, emissivity=0.9,
+                     thermal_inertia=200.0, tacc=0.005, name=f"stress_s{p_subdiv}s{s_subdiv}")
+
+
+def fast_vs_fp64(ctx, prob, tis, revs, shadow, illum):
+    """FAST (batched) vs plain FP64 after the same ``revs`` revolutions with
+    every facet advancing every revolution (freeze off), so both runs follow
+    the same schedule: max |T_fast - T_fp64| over facets, steps and thermal
+    inertias, and the relative error of the disk-integrated 12 um flux seen
+    from the Sun, reduced in FP64 on the GPU (atpm_disk_flux)."""
+    from . import lib
+
+    fast = [lib.Solve(ctx, prob, precision=lib.FAST, revcap=revs, freeze=False) for _ in tis]
+    for s, ti in zip(fast, tis):
+        s.set_forcing(shadow, illum)
+        s.set_thermal_inertia(ti)
+        s.initialise_temperatures()
+    lib.batch_run(fast)
+    ref = lib.Solve(ctx, prob, precision=lib.FP64, revcap=revs, freeze=False)
+    ref.set_forcing(shadow, illum)
+    errs, ferrs = {}, {}
+    for s, ti in zip(fast, tis):
+        ref.set_thermal_inertia(ti)
+        ref.initialise_temperatures()
+        ref.run()
+        t64 = ref.surface_temperature64()
+        t32 = s.surface_temperature64()
+        errs[str(ti)] = float(np.max(np.abs(t32 - t64)))
+        F64 = ref.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
+        F32 = s.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
+        ferrs[str(ti)] = float(np.max(np.abs(F32 - F64) / np.abs(F64)))
+        s.close()
+    ref.close()
+    return {"max_temperature_error_K": max(errs.values()), "max_rel_flux_error_12um": max(ferrs.values()),
+            "per_ti_max_K": errs, "per_ti_rel_flux": ferrs,
+            "schedule": f"{revs} revolutions, every facet advancing (freeze off), same forcing"}
+
+
 def single_problem(ctx, subdiv=3, ntau=720, nx=56, seed=1) -> P.Problem:
     v, f = P.single_body_mesh(subdiv, 0.39, 0.05, seed)
     ptr, idx, vf = _lists(ctx, v, f)
@@ -47,6 +99,34 @@ def single_problem(ctx, subdiv=3, ntau=720, nx=56, seed=1) -> P.Problem:
                      ntau=ntau, nx=nx, polar=(1.0, 0.0, 0.0), pole=(math.pi / 2, 0.0),
                      rotation_period_s=2.26 * 3600.0, albedo=0.02, emissivity=0.9,
                      thermal_inertia=200.0, tacc=0.005, name=f"single_s{subdiv}")
+
+
+def tc_tile_structure(nf, dep_ptr, dep_idx, dep_vf):
+    """The FAST tensor-core tiling of a view-factor list, restated in numpy:
+    the 128 x 64 tiles touched (keys row block * nkb + column block, sorted),
+    the tile of every list entry, the entries' 16-wide K slices, and which
+    tiles carry the residual V - bf16(V): a view factor >= 1e-4, or, for
+    some facet row, at least 1 % of that row's mean |view factor| per
+    64-facet column block it touches (the rule of build_tc/k_tc_rowneed)."""
+    nkb = (nf + 63) // 64
+    rows = np.repeat(np.arange(nf), np.diff(dep_ptr))
+    av = np.abs(np.asarray(dep_vf, np.float32))
+    key = (rows // 128).astype(np.int64) * nkb + np.asarray(dep_idx) // 64
+    tiles, inv = np.unique(key, return_inverse=True)
+    vmax = np.zeros(len(tiles), np.float32)
+    np.maximum.at(vmax, inv, av)
+    has_lo = vmax >= np.float32(1e-4)
+    rk = rows.astype(np.int64) * nkb + np.asarray(dep_idx) // 64
+    u, rinv = np.unique(rk, return_inverse=True)
+    m = np.bincount(rinv, weights=av.astype(np.float64))
+    r = u // nkb
+    M = np.bincount(r, weights=m, minlength=nf)
+    n = np.bincount(r, minlength=nf)
+    need = 100.0 * n[r] * m >= M[r]
+    need_keys = np.unique((r[need] // 128) * nkb + u[need] % nkb)
+    has_lo |= np.isin(tiles, need_keys)
+    slices = np.asarray(dep_idx) % 64 // 16
+    return tiles, inv, slices, has_lo
 
 
 def facet_areas(problem) -> np.ndarray:

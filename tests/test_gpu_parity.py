@@ -181,3 +181,22 @@ def test_clone_outlives_its_source(gpu_ctx):
     for s in clones + fresh:
         s.close()
 
+
+
+def test_precision_stress_concave_binary_small(gpu_ctx):
+    """The precision-stress configuration at a test size: a concave primary
+    (Gaussian-random-field radii, sigma 15 %, correlation 0.3 rad; 5,120
+    facets) + a 1,280-facet secondary, view factors from mutual visibility.
+    FAST stays within 0.01 K and 1e-5 relative 12 um flux of plain FP64 on the
+    same 40-revolution schedule."""
+    from binarytpm_gb300 import lib, workloads
+
+    prob = workloads.stress_problem(gpu_ctx, p_subdiv=4, s_subdiv=3)
+    s0 = lib.Solve(gpu_ctx, prob, precision=lib.FAST)
+    s0.geometry_shadow()
+    s0.scattering()
+    sh, il = s0.shadow(), s0.illumination()
+    s0.close()
+    err = workloads.fast_vs_fp64(gpu_ctx, prob, [50.0, 800.0], 40, sh, il)
+    assert err["max_temperature_error_K"] < 0.01, err
+    assert err["max_rel_flux_error_12um"] < 1e-5, err

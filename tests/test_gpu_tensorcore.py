@@ -31,14 +31,13 @@ def _host_q(prob, T, rounded):
         hi = _bf16(W)
         lo = _bf16((W - hi.astype(np.float32)).astype(np.float32))
         W = hi + lo
-        # V_hi everywhere; V_lo added in 128x64 tiles holding a value >= 1e-4
-        key = (rows // 128) * ((prob.nf + 63) // 64) + prob.dep_idx // 64
-        u, inv = np.unique(key, return_inverse=True)
-        vmax = np.zeros(len(u), np.float32)
-        np.maximum.at(vmax, inv, np.abs(vf))
+        # V_hi everywhere; V_lo added in the tiles that carry the residual
+        from binarytpm_gb300 import workloads
+
+        _, inv, _, has_lo = workloads.tc_tile_structure(prob.nf, prob.dep_ptr, prob.dep_idx, vf)
         vhi = _bf16(vf)
         vlo = _bf16((vf - vhi.astype(np.float32)).astype(np.float32))
-        vf = vhi + np.where(vmax[inv] >= np.float32(1e-4), vlo, 0.0)
+        vf = vhi + np.where(has_lo[inv], vlo, 0.0)
     Q = np.zeros((prob.nf, T.shape[1]))
     np.add.at(Q, rows, vf[:, None] * W[prob.dep_idx].astype(np.float64))
     return Q.T
