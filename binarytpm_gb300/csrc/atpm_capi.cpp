@@ -281,6 +281,14 @@ bool warp_tail_enabled() {
     return !(e && e[0] == '0');
 }
 
+// active facets per SM up to which a revolution runs warp per facet
+// (ATPM_WARP_TAIL_PER_SM, 1..64; both forms give identical results)
+int warp_tail_per_sm() {
+    const char* e = std::getenv("ATPM_WARP_TAIL_PER_SM");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 64 ? v : 12;
+}
+
 bool tc_enabled() {
     const char* e = std::getenv("ATPM_TC");
     return !(e && e[0] == '0');
@@ -460,7 +468,7 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     // active facets of the whole batch up to which a revolution runs warp per
     // facet: about a dozen warps per SM, where one warp per facet still beats
     // the thread-per-facet sweep's latency-bound last warps
-    b.tail_limit = 12 * ctx->sm_count;
+    b.tail_limit = warp_tail_per_sm() * ctx->sm_count;
     b.sms = ctx->sm_count;
     return b;
 }

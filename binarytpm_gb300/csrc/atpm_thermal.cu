@@ -396,9 +396,12 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
 }
 
 // FAST, late revolutions: one warp per active facet.  Lane l holds depth
-// nodes 2l and 2l+1 (theta offsets, as above); each step exchanges the two
-// neighbours by shuffles, and every lane runs the same Newton boundary solve
-// on the broadcast node 1, so the arithmetic is that of
+// nodes 2l and 2l+1 (theta offsets, as above), and every lane also carries
+// nodes 0..3, so a step's boundary chain (node 1, then the Newton solve)
+// waits on no shuffle: the new node 3 and the next step's absorbed flux are
+// shuffled while the Newton solve runs.  The bottom node is a copy of node
+// NX-1 after every step, so node NX-1 reads its own old value for it and the
+// bottom is written once, after the revolution.  The arithmetic is that of
 // column_revolution_fast step for step.  Forcing, flux and the previous
 // temperature come in blocks of 32 steps (lane j holds step s0 + j, the next
 // block loading while this one runs); the step's outputs collect in the lane
@@ -408,6 +411,7 @@ constexpr int kWarpNodes = 64;  // nodes 0..NX a warp can hold
 template <int NX>
 __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f) {
     static_assert(NX + 1 <= kWarpNodes, "two nodes per lane");
+    static_assert(NX >= 4, "nodes 0..3 above the bottom node");
     constexpr unsigned FULL = 0xffffffffu;
     const int nf = sv.nf, ntau = sv.ntau;
     const int lane = threadIdx.x & 31;
@@ -428,14 +432,14 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
     bool hot = false;
     int flags = 0;
     const int cap = sv.newton_cap;
-    float th1 = 0.0f;
-    // nodes 0, 1, 2 held by every lane (lane 0 owns 0 and 1, lane 1 owns 2)
-    float th_u = __shfl_sync(FULL, Ta, 0), t1_u = __shfl_sync(FULL, Tb, 0), t2_u = __shfl_sync(FULL, Ta, 1);
-    float ce = 0.0f, cq = 0.0f, co = 0.0f;
+    // nodes 0..3 on every lane (lane 0 owns 0 and 1, lane 1 owns 2 and 3)
+    float th_u = __shfl_sync(FULL, Ta, 0), t1_u = __shfl_sync(FULL, Tb, 0);
+    float t2_u = __shfl_sync(FULL, Ta, 1), t3_u = __shfl_sync(FULL, Tb, 1);
+    // lane j: (1 - A) E + Q and the previous surface temperature of step s0 + j
+    float ca = 0.0f, co = 0.0f;
     if (lane < ntau) {
         const size_t o = (size_t)lane * nf + f;
-        ce = E[o];
-        cq = Q[o];
+        ca = fmaf(oma, E[o], Q[o]);
         co = S1[o];
     }
     for (int s0 = 0; s0 < ntau; s0 += 32) {
@@ -448,22 +452,26 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
         }
         float ts = 0.0f;
         const int nstep = min(32, ntau - s0);
-        // unrolled so that the node updates of the next steps (independent of
-        // this step's boundary solve) overlap its dependency chain
+        float a = __shfl_sync(FULL, ca, 0);
 #pragma unroll 4
         for (int j = 0; j < nstep; ++j) {
-            const float e = __shfl_sync(FULL, ce, j), q = __shfl_sync(FULL, cq, j), old = __shfl_sync(FULL, co, j);
+            const float old = __shfl_sync(FULL, co, j);
+            const float a_next = __shfl_sync(FULL, ca, (j + 1) & 31);  // unused after the block's last step
             const float lft = __shfl_up_sync(FULL, Tb, 1);    // node na - 1
             const float rgt = __shfl_down_sync(FULL, Ta, 1);  // node nb + 1
-            // nodes 2 .. NX-1 from old values, off the boundary's dependency chain
+            // nodes 2 .. NX-1 from old values; node NX-1 reads itself for the bottom
             float Ta_n = Ta, Tb_n = Tb;
             if (na >= 2 && na <= NX - 1) Ta_n = ftcs_node(r, Tb, lft, Ta);
-            if (nb >= 2 && nb <= NX - 1) Tb_n = ftcs_node(r, rgt, Ta, Tb);
-            // node 1 and the boundary solve on every lane (uniform values)
+            if (nb >= 2 && nb <= NX - 1) Tb_n = ftcs_node(r, nb == NX - 1 ? Tb : rgt, Ta, Tb);
+            if (nb == NX) Tb_n = Ta_n;  // odd NX: the bottom copy beside node NX-1
+            // nodes 1 and 2 on every lane (uniform values)
             const float t1n = ftcs_node(r, t2_u, th_u, t1_u);
-            const float a = fmaf(oma, e, q);
+            const float t2n = ftcs_node(r, t3_u, t1_u, t2_u);
+            if (lane == 0) Tb_n = t1n;  // node 1, read by lane 1 next step
+            const float t3n = __shfl_sync(FULL, Tb_n, 1);
+            // the boundary solve on every lane
             float DT;
-            th1 = newton_fast(th_u, Tref, t1n, a, m1, es, es4, DT);
+            float th1 = newton_fast(th_u, Tref, t1n, a, m1, es, es4, DT);
             if (DT >= tacc10) th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
             int it = 2;
             while (DT >= tacc10) {
@@ -471,21 +479,13 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
                 th1 = newton_fast(th1, Tref, t1n, a, m1, es, es4, DT);
                 ++it;
             }
-            if (lane == 0) {
-                Ta_n = th1;
-                Tb_n = t1n;
-            }
-            // bottom node: T[NX] = T[NX - 1] (new)
-            const float bot = __shfl_sync(FULL, ((NX - 1) & 1) ? Tb_n : Ta_n, (NX - 1) >> 1);
-            if (lane == (NX >> 1)) {
-                if (NX & 1) Tb_n = bot;
-                else Ta_n = bot;
-            }
             Ta = Ta_n;
             Tb = Tb_n;
             th_u = th1;
             t1_u = t1n;
-            t2_u = __shfl_sync(FULL, Ta, 1);  // node 2 (new)
+            t2_u = t2n;
+            t3_u = t3n;
+            a = a_next;
             const float Tsurf = Tref + th1;
             if (lane == j) ts = Tsurf;
             hot = hot || (fabsf(Tsurf - old) >= tacc);
@@ -505,11 +505,15 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
                 Wb[base + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
             }
         }
-        ce = ne;
-        cq = nq;
+        ca = fmaf(oma, ne, nq);
         co = no;
     }
-    if (!isfinite(th1 + Tref)) flags |= ST_NONFINITE;
+    if (!isfinite(th_u + Tref)) flags |= ST_NONFINITE;
+    if (lane == 0) Ta = th_u;  // node 0 lives in the uniform copy during the sweep
+    if constexpr ((NX & 1) == 0) {
+        const float bot = __shfl_sync(FULL, Tb, (NX - 1) >> 1);  // node NX-1
+        if (lane == (NX >> 1)) Ta = bot;
+    }
     if (na <= NX) temp[(size_t)na * nf + f] = Tref + Ta;
     if (nb <= NX) temp[(size_t)nb * nf + f] = Tref + Tb;
     if (lane == 0) {

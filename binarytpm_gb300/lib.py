@@ -135,11 +135,13 @@ def exported_symbols():
     return list(_SIGS)
 
 
-def _host_out(shape, dtype) -> np.ndarray:
-    """Output array for a device read-back: page-locked host memory (torch's
-    cached pinned allocator) when torch sees a CUDA device, so the copy runs
-    as direct DMA; plain numpy otherwise.  Every element is written by the
-    call that fills it."""
+def host_buffer(shape, dtype) -> np.ndarray:
+    """Uninitialised host array in page-locked memory (torch's cached pinned
+    allocator) when torch sees a CUDA device, so copies to and from it run
+    as direct DMA; plain numpy otherwise.  For inputs a caller uploads every
+    job and for read-back buffers it reuses (``Solve.surface_temperature(out=)``):
+    the allocator hands a block back only once its array is freed, so a
+    caller that keeps its previous results page-locks fresh memory per call."""
     try:
         import torch
 
@@ -150,6 +152,23 @@ def _host_out(shape, dtype) -> np.ndarray:
     except (ImportError, KeyError, RuntimeError):
         pass
     return np.empty(shape, dtype)
+
+
+def pinned_copy(a: np.ndarray) -> np.ndarray:
+    """``a`` copied into a page-locked host array of the same shape and dtype."""
+    out = host_buffer(a.shape, a.dtype)
+    out[...] = a
+    return out
+
+
+_host_out = host_buffer
+
+
+def _out_arg(a, shape, dtype, name) -> np.ndarray:
+    if not isinstance(a, np.ndarray) or a.shape != shape or a.dtype != np.dtype(dtype) or not a.flags.c_contiguous \
+            or not a.flags.writeable:
+        raise ValueError(f"{name}: expected a writable C-contiguous {np.dtype(dtype).name} array of shape {shape}")
+    return a
 
 
 def _ck(rc: int):
@@ -302,9 +321,15 @@ class Solve:
         _ck(load().atpm_selfheating_flux(self.h, _p(out)))
         return out
 
-    def surface_temperature(self):
-        s1 = _host_out((self.nf, self.ntau), np.float32)
-        s0 = _host_out((self.nf, self.ntau), np.float32)
+    def surface_temperature(self, out=None):
+        """(stemp1, stemp0) as [nf][ntau] FP32.  ``out``: an (stemp1, stemp0)
+        pair of arrays to fill instead of new ones (see ``host_buffer``)."""
+        shp = (self.nf, self.ntau)
+        if out is None:
+            s1, s0 = _host_out(shp, np.float32), _host_out(shp, np.float32)
+        else:
+            s1 = _out_arg(out[0], shp, np.float32, "out[0]")
+            s0 = _out_arg(out[1], shp, np.float32, "out[1]")
         _ck(load().atpm_get_surface_temperature(self.h, _p(s1), _p(s0)))
         return s1, s0
 

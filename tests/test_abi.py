@@ -3,6 +3,7 @@ import re
 import subprocess
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -69,3 +70,23 @@ def test_reference_gpu_module_shim_defines_every_symbol(tmp_path, header, shim, 
     out = subprocess.run(["nm", "--defined-only", str(obj)], capture_output=True, text=True, check=True).stdout
     defined = set(re.findall(r"\s[Tt]\s+(\w+)$", out, re.M))
     assert declared <= defined, declared - defined
+
+
+def test_read_back_buffers_are_checked():
+    """Caller-owned read-back buffers (Solve.surface_temperature(out=)) are
+    checked for shape, dtype, layout and writability before any C call."""
+    from binarytpm_gb300 import lib
+
+    a = lib.host_buffer((3, 5), np.float32)
+    assert a.shape == (3, 5) and a.dtype == np.float32
+    assert lib._out_arg(a, (3, 5), np.float32, "out") is a
+    for bad in (np.empty((5, 3), np.float32), np.empty((3, 5), np.float64), np.empty((5, 3), np.float32).T):
+        with pytest.raises(ValueError):
+            lib._out_arg(bad, (3, 5), np.float32, "out")
+    ro = np.empty((3, 5), np.float32)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        lib._out_arg(ro, (3, 5), np.float32, "out")
+    src = np.arange(6, dtype=np.int32).reshape(2, 3)
+    c = lib.pinned_copy(src)
+    assert c.dtype == src.dtype and np.array_equal(c, src)

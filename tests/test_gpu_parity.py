@@ -33,6 +33,11 @@ def test_reference_mode_bit_exact(gpu_ctx, name):
     bad = np.flatnonzero(s1.view(np.uint32) != ref["stemp1"].view(np.uint32))
     assert bad.size == 0, f"{bad.size} temperatures differ, max {np.abs(s1 - ref['stemp1']).max()} K"
     assert np.array_equal(s0.view(np.uint32), ref["stemp0"].view(np.uint32))
+    # the same read into caller-owned page-locked buffers
+    out = (lib.host_buffer(s1.shape, np.float32), lib.host_buffer(s1.shape, np.float32))
+    r1, r0 = s.surface_temperature(out=out)
+    assert r1 is out[0] and r0 is out[1]
+    assert np.array_equal(r1.view(np.uint32), s1.view(np.uint32)) and np.array_equal(r0.view(np.uint32), s0.view(np.uint32))
     assert np.array_equal(s.depth_temperature().view(np.uint32), ref["temp"].view(np.uint32))
     for got, want in zip(counts, ref["counts_list"]):
         assert np.array_equal(got, want)
