@@ -100,11 +100,17 @@ struct atpm_server {
 namespace {
 
 atpm_status admit(atpm_server* S, Request* r) {
-    ShapeEntry& sh = *S->shapes[r->shape];
+    ShapeEntry* sh;
+    {
+        // add_shape may grow the table on another thread: read it locked (the
+        // entries themselves never move)
+        std::lock_guard<std::mutex> lk(S->mu);
+        sh = S->shapes[r->shape].get();
+    }
     atpm_solve* s = nullptr;
     // a device copy of the prototype: forcing and (shared) tensor-core tiles
     // come along, no host work on the shape
-    atpm_status st = atpm_solve_clone(sh.proto, &s);
+    atpm_status st = atpm_solve_clone(sh->proto, &s);
     if (st) return st;
     if (!st) st = atpm_set_thermal_inertia(s, r->ti);
     if (!st && r->ti != 0.0f) st = atpm_initialise_temperatures(s);
