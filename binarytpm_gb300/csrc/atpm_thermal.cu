@@ -529,7 +529,11 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
 // per revolution (one warp over the solves) and leaves the answer in the
 // batch's first solve (act_cnt[4]), where both conduction kernels read it:
 // exactly one of them advances each facet.
-constexpr int kSparseCtas = 128;  // CTAs (4 warps each) per solve
+// CTAs (4 warps each) per solve: in the late revolutions most active facets
+// belong to the one or two solves of highest thermal inertia, so one solve
+// may hold nearly the whole batch's b.tail_limit facets; 384 x 4 warps give
+// each of them its own warp, and the CTAs beyond a solve's list exit at once
+constexpr int kSparseCtas = 384;
 
 __global__ void k_tail_mode(Batch b) {
     const int lane = threadIdx.x;
@@ -552,12 +556,12 @@ __device__ __forceinline__ bool warp_tail_now(const Batch& b) { return b.tab[0].
 template <int NX>
 __global__ void __launch_bounds__(128) k_conduction_warp(Batch b) {
     const int si = blockIdx.x / kSparseCtas;
-    if (si >= b.n || !b.warp_tail) return;
+    // the batch-wide decision first: one load, and most revolutions stop here
+    if (si >= b.n || !b.warp_tail || !warp_tail_now(b)) return;
     const DevSolve& sv = b.tab[si];
     if (!sv.ctl->active || sv.ti == 0.0f) return;
     const int rev = sv.ctl->rev;
     if (rev < 7 || sv.act_cnt[2 + (rev & 1)] != rev || sv.act_cnt[rev & 1] == 0) return;
-    if (!warp_tail_now(b)) return;
     if constexpr (NX + 1 <= kWarpNodes) {
         const int n = sv.act_cnt[rev & 1];
         const int* list = sv.act_list + (size_t)(rev & 1) * sv.nf;
