@@ -529,12 +529,6 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
 // per revolution (one warp over the solves) and leaves the answer in the
 // batch's first solve (act_cnt[4]), where both conduction kernels read it:
 // exactly one of them advances each facet.
-// CTAs (4 warps each) per solve: in the late revolutions most active facets
-// belong to the one or two solves of highest thermal inertia, so one solve
-// may hold nearly the whole batch's b.tail_limit facets; 384 x 4 warps give
-// each of them its own warp, and the CTAs beyond a solve's list exit at once
-constexpr int kSparseCtas = 384;
-
 __global__ void k_tail_mode(Batch b) {
     const int lane = threadIdx.x;
     bool ok = b.warp_tail != 0;
@@ -552,6 +546,13 @@ __global__ void k_tail_mode(Batch b) {
 }
 
 __device__ __forceinline__ bool warp_tail_now(const Batch& b) { return b.tab[0].act_cnt[4] != 0; }
+
+// CTAs (4 warps each) per solve: in the late revolutions most active facets
+// belong to the one or two solves of highest thermal inertia, so one solve
+// may hold most of the batch's b.tail_limit facets (12 per SM, 1,824 on 152
+// SMs); 384 x 4 = 1,536 warps give nearly every one of them its own warp, and
+// the CTAs beyond a solve's list exit at once
+constexpr int kSparseCtas = 384;
 
 template <int NX>
 __global__ void __launch_bounds__(128) k_conduction_warp(Batch b) {
