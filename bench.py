@@ -171,6 +171,36 @@ def prepare():
     return refbuild.thermal_source(_ref_cfg(prob, 200.0, 1, 3))
 
 
+def activity(caps=(10, 25, 50, 75, 100, 150, 200, 250, 300)):
+    """Active facets per solve late in the batch: the bench's 8-inertia binary
+    is run to each revolution cap in turn (freeze on, fresh solves each time)
+    and the facets not yet converged are counted per solve.  One JSON line:
+    per cap, the counts in thermal-inertia order."""
+    from binarytpm_gb300 import lib, workloads
+
+    ctx = lib.Context(0)
+    prob = workloads.binary_problem(ctx)
+    tis = workloads.BATCH_TI
+    s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    s0.geometry_shadow()
+    s0.scattering()
+    shadow, illum = s0.shadow(), s0.illumination()
+    s0.close()
+    out = {}
+    for cap in caps:
+        solves = [lib.Solve(ctx, prob, precision=lib.FAST, revcap=cap) for _ in tis]
+        for s, ti in zip(solves, tis):
+            s.set_forcing(shadow, illum)
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+        lib.batch_run(solves)
+        out[str(cap)] = [int(prob.nf - s.converged().sum()) for s in solves]
+        for s in solves:
+            s.close()
+    ctx.close()
+    print(json.dumps({"active_facets_per_solve": out, "thermal_inertia": tis, "nf": prob.nf}), flush=True)
+
+
 def profile_case(nsolves: int = 2):
     """A small, fast case of the same kernels for ncu --set full captures:
     the binary with a subdivision-4 primary (5,120 + 1,280 facets, NX = 56,
@@ -262,6 +292,8 @@ def main():
     ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
     ap.add_argument("--precision-stress", type=int, default=0, metavar="SUBDIV",
                     help="run the precision-stress configuration with this primary subdivision (6: 81,920 facets)")
+    ap.add_argument("--activity", action="store_true",
+                    help="active facets per solve of the 8-inertia binary at revolution caps 10 ... 300")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: binary 5120+1280 facets, 2 solves, 3 instrumented revolutions")
     args = ap.parse_args()
@@ -273,6 +305,9 @@ def main():
         return
     if args.profile_case:
         profile_case(args.profile_solves)
+        return
+    if args.activity:
+        activity()
         return
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":
