@@ -346,6 +346,7 @@ int launch_set_forcing(const DevSolve& s, const int32_t* shadow_d, const float* 
 namespace {
 constexpr size_t kNoAllocMaxCells = size_t(1) << 20;
 constexpr size_t kNoAllocStatusSlot = 3 * kNoAllocMaxCells;  // one int after the three arrays
+constexpr int kNoAllocMaxFacets = 8 * 65535;  // grid.y of the single-scattering launch is nf / 8
 static __device__ __align__(256) float g_noalloc_scratch[3 * kNoAllocMaxCells + 64];
 
 std::mutex g_noalloc_mu;
@@ -388,9 +389,21 @@ extern "C" ATPM_API atpm_status atpm_scattering_noalloc(
     int32_t multiple, float* illumination, int32_t* status, void* stream) {
     using namespace atpm;
     char err[256];
-    if (nf < 1 || ntau < 1 || !dep_ptr || !cosillum || !shadow || !illumination) {
-        set_last_error("scattering_noalloc: bad arguments");
+    if (nf < 1 || ntau < 1 || !dep_ptr || !dep_idx || !dep_vf || !cosillum || !shadow || !illumination) {
+        set_last_error("scattering_noalloc: bad arguments (every array, dep_idx and dep_vf included, must be a "
+                       "device pointer)");
         return ATPM_E_INVALID;
+    }
+    if (multiple && !status) {
+        set_last_error("scattering_noalloc: multiple scattering needs a status word (the Gauss-Seidel cap is "
+                       "reported there)");
+        return ATPM_E_INVALID;
+    }
+    if (nf > kNoAllocMaxFacets) {
+        std::snprintf(err, sizeof err, "scattering_noalloc: nf = %d exceeds %d facets (launch grid limit)", nf,
+                      kNoAllocMaxFacets);
+        set_last_error(err);
+        return ATPM_E_UNSUPPORTED;
     }
     if ((size_t)nf * (size_t)ntau > kNoAllocMaxCells) {
         std::snprintf(err, sizeof err,

@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "atpm_internal.h"
@@ -545,15 +546,18 @@ int launch_spmm_tc(const Batch& b, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     if (b.nq == 0) return 0;
     const size_t smem = spmm_tc_smem_bytes(b.tc_nmax, b.tc_stages);
-    static int attr_dev = -1;
+    // the shared-memory attribute is set once per device; the two batch
+    // groups launch from their own threads, so the record is atomic
+    static std::atomic<uint64_t> attr_set{0};
     int dev = 0;
     cudaGetDevice(&dev);
-    if (attr_dev != dev) {
+    const uint64_t bit = dev < 64 ? uint64_t(1) << dev : 0;
+    if (!bit || !(attr_set.load(std::memory_order_acquire) & bit)) {
         size_t most = 0;  // largest ring over every admissible chunk size
         for (int n = 16; n <= tc_max_chunk(); n += 16) most = spmm_tc_smem_bytes(n) > most ? spmm_tc_smem_bytes(n) : most;
         if (cudaFuncSetAttribute(k_spmm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) != cudaSuccess)
             return 2;
-        attr_dev = dev;
+        attr_set.fetch_or(bit, std::memory_order_release);
     }
     // the list length and the ticket counter start at zero for every launch
     // (a memset node when the revolution is captured in a graph)

@@ -333,11 +333,15 @@ ATPM_API atpm_status atpm_server_destroy(atpm_server* s);
  * Gauss-Seidel work arrays live in one fixed file-scope device array of
  * 2^20 cells x 3 floats (12 MiB), reserved on every GPU that loads the
  * library until exit.  No counterpart in the reference.
- *   nf * ntau must be <= 2^20, otherwise ATPM_E_UNSUPPORTED.
- *   dep_ptr/idx/vf: CSR lists; cosillum [nf][ntau] float; shadow [nf][ntau]
- *   bytes 0/1; illumination [nf][ntau] float output.  status: optional
- *   device int the kernels OR ST_* bits into (8 = scattering cap reached);
- *   the caller zeroes it.  Work is enqueued on `stream` (a cudaStream_t,
+ *   nf * ntau must be <= 2^20 and nf <= 524,280, otherwise
+ *   ATPM_E_UNSUPPORTED.
+ *   dep_ptr/idx/vf: CSR lists, all three device pointers (never NULL, even
+ *   for empty lists); cosillum [nf][ntau] float; shadow [nf][ntau] bytes
+ *   0/1; illumination [nf][ntau] float output.  status: device int the
+ *   kernels OR ST_* bits into (8 = scattering cap reached: Gauss-Seidel
+ *   stopped at 1,000 sweeps); the caller zeroes it.  It is required when
+ *   multiple != 0 (ATPM_E_INVALID otherwise) and may be NULL for single
+ *   scattering only.  Work is enqueued on `stream` (a cudaStream_t,
  *   NULL = default stream); the call returns without waiting for it.
  *   The first call on a device looks up the array's address
  *   (cudaGetSymbolAddress) with that device current: make it before any

@@ -33,7 +33,9 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("ATPM_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: ATPM_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's root
+REF_ROOT = Path(os.environ.get("ATPM_REFERENCE_ROOT", str(HERE.parent.parent / "reference")))
 OUT_ROOT = HERE / "_ref"
 
 THERMAL_SRC = "3905/Thermal/NominalPole/main.cpp"

@@ -90,3 +90,24 @@ def test_read_back_buffers_are_checked():
     src = np.arange(6, dtype=np.int32).reshape(2, 3)
     c = lib.pinned_copy(src)
     assert c.dtype == src.dtype and np.array_equal(c, src)
+
+
+def test_noalloc_entry_point_rejects_bad_arguments_before_any_device_work():
+    """atpm_scattering_noalloc checks its arguments on the host before it
+    touches the GPU: a NULL list pointer, multiple scattering without a
+    status word, and more facets than its launch grid covers are errors
+    (no kernel is launched, so this runs without a GPU)."""
+    from binarytpm_gb300 import build, lib
+
+    build.build()
+    L = lib.load()
+    p = 4096  # never dereferenced: every call below is rejected first
+    args = dict(solar=1367.0, albedo=0.1, acc=1e-4)
+    call = lambda nf, ntau, idx, vf, multiple, status: L.atpm_scattering_noalloc(
+        nf, ntau, p, idx, vf, p, p, args["solar"], args["albedo"], args["acc"], multiple, p, status, None)
+    assert call(16, 8, None, p, 0, p) == 1          # ATPM_E_INVALID: dep_idx NULL
+    assert call(16, 8, p, None, 0, p) == 1          # ATPM_E_INVALID: dep_vf NULL
+    assert call(16, 8, p, p, 1, None) == 1          # ATPM_E_INVALID: no status word for the Gauss-Seidel cap
+    assert b"status" in L.atpm_last_error()
+    assert call(600_000, 1, p, p, 0, p) == 4        # ATPM_E_UNSUPPORTED: nf beyond the launch grid
+    assert call(2048, 1024, p, p, 0, p) == 4        # ATPM_E_UNSUPPORTED: nf * ntau beyond the scratch

@@ -59,6 +59,6 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_ctx):
     L = lib.load()
     buf = torch.zeros(16, dtype=torch.float32, device="cuda:0")
     p = buf.data_ptr()
-    rc = L.atpm_scattering_noalloc(2048, 1024, p, p, p, p, p, 1367.0, 0.1, 1e-4, 1, p, None, None)
+    rc = L.atpm_scattering_noalloc(2048, 1024, p, p, p, p, p, 1367.0, 0.1, 1e-4, 1, p, p, None)
     assert rc == 4  # ATPM_E_UNSUPPORTED
     assert b"exceeds" in L.atpm_last_error()
