@@ -3,13 +3,23 @@
 FP64 GPU path on the binary-asteroid workload, with the reference's own
 OpenMP CPU code timed on this host beside it.
 
-Workload (one "step"): the synchronous binary (20,480 + 1,280 = 21,760
-facets, NX = 56, NTAU = 720, shadowing + self-heating on, TACC = 0.005 K)
-solved to convergence for a batch of 8 thermal inertias at once, starting
-from the reference's initial temperatures.  facet-steps = active facets x
-NTAU summed over the revolutions actually executed.
+Workload (one "step", the same in both arms): the synchronous binary
+(20,480 + 1,280 = 21,760 facets, NX = 56, NTAU = 720, shadowing +
+self-heating on, TACC = 0.005 K) for 8 thermal inertias (25 ... 2,000 SI),
+each run from the reference's initial temperatures for revolutions 0-5 of
+the reference's protocol.  The protocol tests convergence only after
+revolution 5, so every facet advances in every one of these revolutions.
+facet-steps = facets x NTAU x revolutions.  The same binary solved to
+convergence under the freeze protocol is reported beside it
+("converged_batch").
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+--impl reference times the reference's own Thermal program (compiled from a
+scratch copy, OpenMP on every host core) on the same mesh, with view-factor
+lists written by the reference's own Shape_Selfheating program; it loads no
+part of this repository's library.  Each of its steps is one revolution of
+one thermal inertia.
 
 Under torchrun (N > 1) every rank runs an independent replica (the solves do
 not shard); value = facet-steps of all ranks / max time over ranks.
@@ -35,6 +45,19 @@ sys.path.insert(0, str(ROOT))
 METRIC = "facet-steps/s, batched FP32 vs plain FP64 GPU at <=0.01 K; p50/p99 solve latency"
 UNIT = "facet-steps/s"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
+CACHE = ROOT / "_cache"
+
+# the timed workload, identical in both arms
+HEADLINE_REVS = 6
+BATCH_TI = [25.0, 50.0, 100.0, 200.0, 400.0, 800.0, 1400.0, 2000.0]
+WORKLOAD = ("binary asteroid 20480+1280 facets, NX=56, NTAU=720, TACC=0.005 K, shadowing + self-heating on; "
+            "8 thermal inertias 25-2000 SI, each run for revolutions 0-5 of the reference protocol from its "
+            "initial temperatures (convergence is tested only after revolution 5: every facet advances)")
+
+
+def headline_config() -> dict:
+    return {"workload": WORKLOAD, "facets": 21760, "nx": 56, "ntau": 720, "thermal_inertia": BATCH_TI,
+            "revolutions_per_solve": HEADLINE_REVS, "parallelism": "replicas"}
 
 
 def _peaks():
@@ -126,49 +149,71 @@ def _barrier(dist):
 
 
 # ----------------------------------------------------------------------------------------
-def reference_cpu(problem, ti: float, revs: int, threads: int):
-    """Time the reference's own Thermal program (compiled from a scratch copy by
-    oracle/refbuild.py) on this host: per-revolution wall time of its
-    revolution loop.  Returns (facet-steps/s, seconds, revolutions, threads)."""
-    from binarytpm_gb300 import formats, mesh
+def reference_revolutions(inputs: Path, dims: dict, ti: float, revs: int, threads: int):
+    """Run the reference's own Thermal program (scratch copy compiled by
+    oracle/refbuild.py, OpenMP on ``threads`` host cores) on the stage files
+    in ``inputs`` (mesh, view-factor lists, vector list, photon vectors) for
+    ``revs`` revolutions at one thermal inertia.  Returns one row per
+    revolution: (revolution, active facet-steps, seconds of its revolution
+    loop, facets converged after it)."""
+    import shutil
+
     from oracle import refbuild
 
-    cfg = _ref_cfg(problem, ti, threads, revs)
-    exe = refbuild.build_thermal(cfg)
+    exe = refbuild.build_thermal(_ref_cfg(dims, ti, threads, revs))
     with tempfile.TemporaryDirectory() as td:
         wd = Path(td)
-        mesh.write_shape(wd / "shape.txt", problem.vertices, problem.facets)
-        formats.write_selfheating_list(wd / "shape_selfheating_list.txt", problem.dep_ptr, problem.dep_idx,
-                                       problem.dep_vf)
-        (wd / "shape_selfheating_vector_list.txt").write_text("")
-        (wd / "shape_photovectors.txt").write_text("0 0 0\n" * problem.nf)
+        for name in ("shape.txt",) + tuple("shape" + x for x in refbuild.SELFHEATING_OUTPUTS):
+            os.symlink(Path(inputs).resolve() / name, wd / name)
         refbuild.run(exe, wd, env_threads=threads)
-        revs_tab = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)
-    secs = float(revs_tab[:, 3].sum())
-    fs = 0
-    for r in range(len(revs_tab)):
-        active = problem.nf if r - 1 <= 5 else problem.nf - int(revs_tab[r - 1, 2])
-        fs += active * problem.ntau
-    return fs / secs, secs, len(revs_tab), threads
+        tab = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)
+    rows, prev = [], 0
+    for r in range(len(tab)):
+        # facets frozen after revolution r-1 are skipped in revolution r (the
+        # convergence test runs only after revolution 5)
+        active = dims["nf"] - (prev if r > 6 else 0)
+        rows.append((int(tab[r, 1]), active * dims["ntau"], float(tab[r, 3]), int(tab[r, 2])))
+        prev = int(tab[r, 2])
+    return rows
 
 
-def _ref_cfg(problem, ti, threads, revs):
-    return dict(nv=problem.nv, nf=problem.nf, ntau=problem.ntau, nx=problem.nx, polar=list(problem.polar),
-                rot=list(problem.pole), rotation_period_s=problem.rotation_period_s, albedo=problem.albedo,
-                tacc=problem.tacc, ti_min=ti, ti_max=ti, threads=threads, revcap=revs)
+def _ref_cfg(dims, ti, threads, revs):
+    return dict(nv=dims["nv"], nf=dims["nf"], ntau=dims["ntau"], nx=dims["nx"], polar=list(dims["polar"]),
+                rot=list(dims["pole"]), rotation_period_s=dims["rotation_period_s"], albedo=dims["albedo"],
+                tacc=dims["tacc"], ti_min=ti, ti_max=ti, threads=threads, revcap=revs)
+
+
+def binary_dims():
+    """The headline binary's mesh and the constants the reference program
+    takes for it (the same seeded synthetic mesh as the GPU arm)."""
+    from binarytpm_gb300 import problem as P
+
+    v, f = P.binary_mesh(5, 3, 2)
+    return v, f, dict(nv=len(v), nf=len(f), ntau=720, nx=56, polar=(1.0, 0.0, 0.0), pole=P.BINARY_POLE,
+                      rotation_period_s=11.9 * 3600.0, albedo=0.02, tacc=0.005)
+
+
+def reference_inputs(threads: int):
+    """Stage files of the headline binary made by the reference's own
+    Shape_Selfheating program (cached under _cache/)."""
+    from oracle import refbuild
+
+    v, f, dims = binary_dims()
+    return refbuild.selfheating_inputs(v, f, threads, CACHE), dims
 
 
 def prepare():
-    """Write the reference scratch copy for this workload (needs the reference
-    checkout; the GPU host then compiles the copy it receives)."""
-    from binarytpm_gb300 import problem as P
+    """Write the reference scratch copies this bench compiles (needs the
+    reference checkout; the GPU host then compiles the copies it receives):
+    the Thermal driver for each revolution count it runs and the
+    Shape_Selfheating program for the binary."""
     from oracle import refbuild
 
-    v, f = P.binary_mesh(5, 3, 2)
-    prob = P.Problem(vertices=v, facets=f, dep_ptr=None, dep_idx=None, dep_vf=None, ntau=720, nx=56,
-                     polar=(1.0, 0.0, 0.0), pole=P.BINARY_POLE, rotation_period_s=11.9 * 3600.0,
-                     albedo=0.02, tacc=0.005)
-    return refbuild.thermal_source(_ref_cfg(prob, 200.0, 1, 3))
+    v, f, dims = binary_dims()
+    out = [refbuild.thermal_source(_ref_cfg(dims, ti, 1, HEADLINE_REVS)) for ti in BATCH_TI]
+    out.append(refbuild.thermal_source(_ref_cfg(dims, 200.0, 1, 2)))
+    sh = refbuild.selfheating_source(len(v), len(f), "shape")
+    return "\n".join(str(p) for p in out + [sh])
 
 
 def activity(caps=(10, 25, 50, 75, 100, 150, 200, 250, 300)):
@@ -253,28 +298,53 @@ def precision_stress(p_subdiv: int):
 
 
 def run_reference_arm(args, world, rank):
+    """The reference's own CPU implementation of the timed workload on this
+    host's cores.  Nothing of this repository's library is loaded: the
+    view-factor lists come from the reference's Shape_Selfheating program
+    and the revolutions from its Thermal program.  Each step is one
+    revolution of one thermal inertia; the thermal inertias are taken in the
+    headline order, 6 revolutions each (revolutions 0-5, every facet
+    active), until W + K revolutions are done; the first W are warm-up."""
     if rank != 0:
         return
-    from binarytpm_gb300 import lib, workloads
-
-    ctx = lib.Context(0)
-    prob = workloads.binary_problem(ctx)
-    ctx.close()
     threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.steps):
-        v, secs, nrev, _ = reference_cpu(prob, 200.0, 3, threads)
-        vals.append(v)
-    value = statistics.median(vals)
+    t0 = time.perf_counter()
+    inputs, dims = reference_inputs(threads)
+    inputs_s = time.perf_counter() - t0
+    need = args.warmup + args.steps
+    samples = []
+    k = 0
+    while len(samples) < need:
+        ti = BATCH_TI[k % len(BATCH_TI)]
+        n = min(HEADLINE_REVS, need - len(samples))
+        samples += [(ti,) + r for r in reference_revolutions(inputs, dims, ti, n, threads)]
+        k += 1
+    timed = samples[args.warmup:need]
+    fs = sum(r[2] for r in timed)
+    secs = sum(r[3] for r in timed)
+    value = fs / secs
+    sample = (f"{len(timed)} timed revolutions (after {args.warmup} warm-up) of the reference Thermal program's "
+              f"revolution loop, thermal inertias {sorted({r[0] for r in timed})}, revolutions 0-5 of each "
+              f"(every facet active), {threads} OpenMP threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "binary 20480+1280 facets, NX=56, NTAU=720, TI=200, reference OpenMP CPU",
-                       "sample": "3 revolutions per step (all facets active)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference",
-                             "sample": "reference Thermal revolution loop, 3 revolutions of the binary at TI=200"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(timed),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": headline_config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_inputs": {"viewfactor_lists": "the reference's Shape_Selfheating program on the same mesh",
+                                 "seconds": inputs_s, "nnz": _count_list_entries(inputs)},
+            "per_revolution_s": [r[3] for r in timed]}
     print(json.dumps(line), flush=True)
+
+
+def _count_list_entries(inputs: Path) -> int:
+    n = 0
+    with open(Path(inputs) / "shape_selfheating_list.txt") as fh:
+        for line in fh:
+            t = line.split(None, 1)
+            n += int(t[0]) if t else 0
+    return n
 
 
 # ----------------------------------------------------------------------------------------
@@ -323,24 +393,24 @@ def main():
     ctx = lib.Context(local)
     t_setup = time.perf_counter()
     prob = workloads.binary_problem(ctx)
-    tis = workloads.BATCH_TI
-    s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    tis = BATCH_TI
+    s0 = lib.Solve(ctx, prob, precision=lib.FAST, revcap=HEADLINE_REVS)
     s0.geometry_shadow()
     s0.scattering()
     # the other inertias: device clones of the prepared solve (shared tiles)
     solves = [s0] + [s0.clone() for _ in tis[1:]]
     setup_s = time.perf_counter() - t_setup
 
-    def step():
-        for s, ti in zip(solves, tis):
+    def step(batch):
+        for s, ti in zip(batch, tis):
             s.set_thermal_inertia(ti)
             s.initialise_temperatures()
-        counts = lib.batch_run(solves)
-        ms, launches, fs = s0.last_run_stats()
-        return ms, launches + 2 * len(solves), fs, counts
+        counts = lib.batch_run(batch)
+        ms, launches, fs = batch[0].last_run_stats()
+        return ms, launches + 2 * len(batch), fs, counts
 
     for _ in range(args.warmup):
-        step()
+        step(solves)
     torch.cuda.synchronize()
     _barrier(dist)
     clk = Clocks(local)
@@ -348,7 +418,7 @@ def main():
     t0 = time.perf_counter()
     dev_ms, launches, fsteps, nrevs = 0.0, 0, 0, []
     for _ in range(args.steps):
-        ms, la, fs, counts = step()
+        ms, la, fs, counts = step(solves)
         dev_ms += ms
         launches += la
         fsteps += fs
@@ -361,34 +431,34 @@ def main():
     fsteps_all = _sum_over_ranks(float(fsteps), dist, dev)
     value = fsteps_all / (dev_ms_max / 1e3)
     wall_value = fsteps_all / _max_over_ranks(wall, dist, dev)
+    # the state the timed schedule ends in: FP64 energy balance and the error
+    # against plain FP64 on exactly this schedule
+    energy = energy_balance(solves, tis)
+    shadow, illum = s0.shadow(), s0.illumination()
+    timed_err = None if args.no_fp64 else workloads.fp64_errors(ctx, prob, solves, tis, HEADLINE_REVS, shadow,
+                                                                illum, freeze=True)
 
     cond_v, tc_depth, _ = s0.last_run_config()
     launch_config = {"conduction_variant": cond_v, "tc_pipeline_depth": tc_depth,
                      "chosen_by": "autotuner: the first batch of this kind (a warm-up step) timed the candidates "
                                   "on its first 3 revolutions; results do not depend on the choice"}
 
-    # per-kernel durations of one instrumented revolution of the same batch
+    # per-kernel durations of one instrumented (all-active) revolution
     kern = lib.profile_revolution(solves)
+    for s in solves:
+        s.close()
 
-    # plain FP64 GPU path: one solve at a time under the same protocol
+    # the same binary solved to convergence under the freeze protocol
+    conv = converged_batch(ctx, prob, tis, shadow, illum, step, args)
+
+    # plain FP64 GPU path: one solve at a time on the timed workload
     fp64 = None
-    err = None
+    conv_err = None
+    rev40 = None
     if not args.no_fp64:
-        shadow, illum = s0.shadow(), s0.illumination()
-        p = lib.Solve(ctx, prob, precision=lib.FP64)
-        p.set_forcing(shadow, illum)
-        f64_ms, f64_fs = 0.0, 0
-        for ti in FP64_TI:
-            p.set_thermal_inertia(ti)
-            p.initialise_temperatures()
-            p.run()
-            ms, _, fs = p.last_run_stats()
-            f64_ms += ms
-            f64_fs += fs
-        p.close()
-        fp64 = {"value": f64_fs / (f64_ms / 1e3), "unit": UNIT, "device_ms": f64_ms, "facet_steps": f64_fs,
-                "thermal_inertia": FP64_TI, "mode": "plain FP64, one solve at a time, reference protocol"}
-        err = accuracy(ctx, prob, tis, shadow, illum)
+        fp64 = fp64_plain(ctx, prob, shadow, illum)
+        conv_err = converged_errors(ctx, prob, shadow, illum)
+        rev40 = workloads.fast_vs_fp64(ctx, prob, [25.0, 200.0, 2000.0], ACC_REVS, shadow, illum)
 
     # end to end through the C ABI from host buffers
     e2e = e2e_run(ctx, prob, tis, max(1, min(args.steps, 3)))  # median of up to 3 jobs
@@ -397,49 +467,159 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        try:
-            v, secs, nrev, th = reference_cpu(prob, 200.0, 3, os.cpu_count() or 1)
-            cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "reference",
-                   "sample": f"reference Thermal revolution loop, {nrev} revolutions of the binary at TI=200 "
-                             f"({secs:.1f} s)"}
-        except Exception as ex:  # the checker must not hide the GPU result
-            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
-                   "sample": f"failed: {ex}"}
+        cpu = cpu_baseline(prob)
 
     hbm, bf16, kind = _peaks()
-    roof = _roofline(kern, solves, prob, hbm, bf16, kind)
+    roof = _roofline(kern, len(tis), prob, hbm, bf16, kind)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "binary asteroid 20480+1280 facets, NX=56, NTAU=720, batch of 8 thermal inertias "
-                               "solved to convergence (TACC=0.005 K)",
-                   "thermal_inertia": tis, "precision": "FAST (batched FP32)", "parallelism": "replicas",
-                   "l2": "state per step 8 x 250 MB > L2 (inputs larger than L2)",
-                   "revolutions_per_solve": nrevs[-1], "nnz_viewfactors": int(prob.nnz)},
-        "wall_clock_value": wall_value, "setup_s": setup_s,
+        "config": headline_config(),
+        "precision": "FAST (batched FP32 state, BF16 view factors on the tensor cores, FP32 accumulation)",
+        "l2": "state per step 8 x 250 MB > L2 (inputs larger than L2)",
         "fp64_plain": fp64,
         "speedup_vs_fp64_plain": (value / fp64["value"]) if fp64 else None,
-        "errors_vs_fp64": err,
-        "latency_ms": ({"p50": serve["p50_ms"], "p99": serve["p99_ms"],
-                        "what": f"serving: submit to result, Poisson arrivals {serve['arrival_rate_per_s']}/s, "
-                                f"{serve['requests']} requests"} if serve else None),
-        "serving": serve,
-        "roofline": roof,
-        "kernels_ms": kern,
-        "launch_config": launch_config,
+        "errors_vs_fp64": {"timed_schedule": timed_err, "converged_freeze_on": conv_err,
+                           "freeze_off_40_revolutions": rev40},
+        "converged_batch": conv,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,
+        "roofline": roof,
+        "latency_ms": ({"p50": serve["p50_ms"], "p99": serve["p99_ms"],
+                        "what": f"serving: submit to result, Poisson arrivals {serve['arrival_rate_per_s']}/s, "
+                                f"{serve['requests']} requests"} if serve else None),
+        "serving": serve,
+        "energy_balance_fp64": energy,
+        "kernels_ms": kern,
+        "launch_config": launch_config,
+        "wall_clock_value": wall_value, "setup_s": setup_s, "nnz_viewfactors": int(prob.nnz),
+        "revolutions_per_solve": nrevs[-1],
     }
-    for s in solves:
-        s.close()
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def energy_balance(solves, tis):
+    """FP64 per-revolution energy balance of each solve's last revolution
+    (atpm_energy_balance): absorbed (1-A)E + Q and emitted eps sigma T^4,
+    summed over facets and steps, and their relative difference."""
+    out = {}
+    for s, ti in zip(solves, tis):
+        ab, em, tm = s.energy_balance()
+        out[str(ti)] = {"absorbed": ab, "emitted": em, "mean_temperature_K": tm,
+                        "rel_imbalance": (ab - em) / ab if ab else None}
+    return out
+
+
+def converged_batch(ctx, prob, tis, shadow, illum, step, args, steps: int = 2):
+    """The 8-inertia batch solved to convergence (freeze protocol, revolution
+    cap 301): facet-steps/s over the revolutions actually executed, counting
+    a frozen facet only while it is active."""
+    import torch
+
+    from binarytpm_gb300 import lib
+
+    c0 = lib.Solve(ctx, prob, precision=lib.FAST)
+    c0.set_forcing(shadow, illum)
+    batch = [c0] + [c0.clone() for _ in tis[1:]]
+    step(batch)  # warm-up: the autotuner times this kind's candidates here
+    torch.cuda.synchronize()
+    ms_all, fs_all, nrev = 0.0, 0, None
+    for _ in range(steps):
+        ms, _, fs, counts = step(batch)
+        ms_all += ms
+        fs_all += fs
+        nrev = [len(c) for c in counts]
+    energy = energy_balance(batch, tis)
+    for s in batch:
+        s.close()
+    return {"value": fs_all / (ms_all / 1e3), "unit": UNIT, "ms_per_step": ms_all / steps, "steps": steps,
+            "revolutions_per_solve": nrev, "energy_balance_fp64": energy,
+            "workload": "the same binary and 8 thermal inertias solved to convergence (TACC = 0.005 K, "
+                        "freeze protocol, revolution cap 301)"}
+
+
+def fp64_plain(ctx, prob, shadow, illum):
+    """Plain FP64 GPU path, one solve at a time, on the timed workload."""
+    from binarytpm_gb300 import lib
+
+    p = lib.Solve(ctx, prob, precision=lib.FP64, revcap=HEADLINE_REVS)
+    p.set_forcing(shadow, illum)
+    f64_ms, f64_fs = 0.0, 0
+    for ti in FP64_TI:
+        p.set_thermal_inertia(ti)
+        p.initialise_temperatures()
+        p.run()
+        ms, _, fs = p.last_run_stats()
+        f64_ms += ms
+        f64_fs += fs
+    p.close()
+    return {"value": f64_fs / (f64_ms / 1e3), "unit": UNIT, "device_ms": f64_ms, "facet_steps": f64_fs,
+            "thermal_inertia": FP64_TI, "mode": "plain FP64, one solve at a time, revolutions 0-5"}
+
+
+def converged_errors(ctx, prob, shadow, illum):
+    """Final-state error after convergence under the freeze protocol, FAST
+    and REFERENCE precision each against plain FP64 run the same way.  The
+    three precisions freeze some facets in different revolutions, so these
+    errors include the protocol's own schedule sensitivity (the bit-exact
+    REFERENCE replica shows it too)."""
+    from binarytpm_gb300 import lib, workloads
+
+    out = {}
+    for name, prec in (("fast", lib.FAST), ("reference", lib.REFERENCE)):
+        batch = [lib.Solve(ctx, prob, precision=prec) for _ in CONV_ERR_TI]
+        out[name] = workloads.fp64_errors(ctx, prob, batch, CONV_ERR_TI, 301, shadow, illum, freeze=True,
+                                          run=True)
+        for s in batch:
+            s.close()
+    return out
+
+
+def cpu_baseline(prob):
+    """The reference's own Thermal program on this host's cores, a bounded
+    sample of the timed workload: 2 revolutions at TI 200 (every facet
+    active).  Its view-factor lists are the reference Shape_Selfheating
+    program's when the reference arm has cached them on this host, else
+    this library's (identical index lists, values written at the
+    reference's 6 significant digits)."""
+    from binarytpm_gb300 import formats, mesh
+
+    threads = os.cpu_count() or 1
+    v, f, dims = binary_dims()
+    try:
+        digest_dir = CACHE / f"refinputs_{_mesh_digest(v, f)}"
+        src = "reference Shape_Selfheating (cached)"
+        if not (digest_dir / "done").exists():
+            digest_dir = Path(tempfile.mkdtemp(prefix="atpm_cpu_inputs_"))
+            mesh.write_shape(digest_dir / "shape.txt", prob.vertices, prob.facets)
+            formats.write_selfheating_list(digest_dir / "shape_selfheating_list.txt", prob.dep_ptr, prob.dep_idx,
+                                           prob.dep_vf)
+            (digest_dir / "shape_selfheating_vector_list.txt").write_text("")
+            (digest_dir / "shape_photovectors.txt").write_text("0 0 0\n" * prob.nf)
+            src = "this library's view factors in the reference's list format"
+        rows = reference_revolutions(digest_dir, dims, 200.0, 2, threads)
+        fs = sum(r[1] for r in rows)
+        secs = sum(r[2] for r in rows)
+        return {"value": fs / secs, "unit": UNIT, "cores": threads, "kind": "reference",
+                "sample": f"reference Thermal revolution loop, {len(rows)} revolutions of the binary at TI=200 "
+                          f"(every facet active, {secs:.1f} s); view-factor lists: {src}"}
+    except Exception as ex:  # the checker must not hide the GPU result
+        return {"value": None, "unit": UNIT, "cores": threads, "kind": "reference", "sample": f"failed: {ex}"}
+
+
+def _mesh_digest(v, f) -> str:
+    import hashlib
+
+    v = np.ascontiguousarray(v, np.float64)
+    f = np.ascontiguousarray(f, np.int32)
+    return hashlib.sha1(v.tobytes() + f.tobytes()).hexdigest()[:16]
 
 
 def serving(ctx, n_requests: int, rate: float, seed: int = 5):
@@ -482,14 +662,11 @@ def serving(ctx, n_requests: int, rate: float, seed: int = 5):
 
 
 FP64_TI = [200.0, 2000.0]
+CONV_ERR_TI = [200.0, 2000.0]
+# executed instructions per facet-step of k_conduction<FAST,56> (ncu,
+# profiles/conduction_and_spmm_binary_s4s3_fast.md)
+COND_INSTR_PER_FACET_STEP = 327
 ACC_REVS = 40
-
-
-def accuracy(ctx, prob, tis, shadow, illum):
-    """FAST vs plain FP64 on the same schedule (workloads.fast_vs_fp64)."""
-    from binarytpm_gb300 import workloads
-
-    return workloads.fast_vs_fp64(ctx, prob, tis, ACC_REVS, shadow, illum)
 
 
 def _tile_stats(prob, slices=False):
@@ -506,7 +683,7 @@ def _tile_stats(prob, slices=False):
     return len(tiles), int(has_lo.sum()), len(sk), int(has_lo[sk // 4].sum())
 
 
-def _roofline(kern, solves, prob, hbm, bf16, kind):
+def _roofline(kern, n, prob, hbm, bf16, kind):
     """Dominant kernel of the revolution loop: the tensor-core self-heating
     product (k_spmm_tc).  Algorithmic FLOP per solve-revolution =
     2 * nnz * NTAU (the list sum); executed = every issued 128x16 K slice x
@@ -514,7 +691,6 @@ def _roofline(kern, solves, prob, hbm, bf16, kind):
     is reported beside it: 20 B algorithmic HBM per facet-step."""
     out = {}
     k = kern.get("selfheat_q")
-    n = len(solves)
     if k and k["ms"]:
         flops = 2.0 * prob.nnz * prob.ntau * n
         tiles, lo, sl, sl_lo = _tile_stats(prob, slices=True)
@@ -534,18 +710,26 @@ def _roofline(kern, solves, prob, hbm, bf16, kind):
                        "residual) and the hi/lo products"}
     c = kern.get("conduction")
     if c and c["ms"]:
-        nx = solves[0].nx
+        nx = prob.nx
         bytes_ = c["facet_steps"] * 20 + c["active_facets"] * 2 * (nx + 1) * 4
         gbs = bytes_ / (c["ms"] / 1e3) / 1e9
         traffic = None
         tf = ROOT / "profiles" / "conduction_fast_nx56_traffic.json"
         if tf.exists():
             traffic = json.loads(tf.read_text())["dram_bytes_per_facet_step"] * c["facet_steps"]
-        flops = c["facet_steps"] * (5 * (nx - 1) + 20 * 2)
-        out["conduction"] = {"kernel": "k_conduction<FAST,56,3>", "bound": "hbm", "achieved": gbs, "peak": hbm,
-                             "unit": "GB/s", "frac": gbs / hbm, "traffic": traffic, "algorithmic_bytes": bytes_,
-                             "fp32_tflops": flops / (c["ms"] / 1e3) / 1e12,
-                             "note": "FP32-issue bound (about 230 instructions per facet-step at minimum)"}
+        # FP32 issue: one warp instruction per SM sub-partition per clock
+        issue_peak = 152 * 4 * 32 * 2.07e9
+        instr = COND_INSTR_PER_FACET_STEP * c["facet_steps"]
+        out["conduction"] = {"kernel": "k_conduction<FAST,56>", "bound": "fp32_issue",
+                             "achieved": instr / (c["ms"] / 1e3) / 1e12, "peak": issue_peak / 1e12,
+                             "unit": "T thread-instructions/s",
+                             "frac": instr / (c["ms"] / 1e3) / issue_peak,
+                             "instructions_per_facet_step": COND_INSTR_PER_FACET_STEP,
+                             "minimum_instructions_per_facet_step": 230,
+                             "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                     "algorithmic_bytes": bytes_, "traffic": traffic},
+                             "note": "issue peak = 152 SMs x 4 sub-partitions x 32 lanes x 2.07 GHz (nominal); "
+                                     "instructions per facet-step from the ncu capture of this kernel"}
     return out
 
 
@@ -567,7 +751,7 @@ def e2e_run(ctx, prob, tis, steps):
     for _ in range(steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s0 = lib.Solve(ctx, prob, precision=lib.FAST)
+        s0 = lib.Solve(ctx, prob, precision=lib.FAST, revcap=HEADLINE_REVS)
         s0.geometry_shadow()
         s0.scattering()
         # one prepared shape, cloned on the device for the other inertias
@@ -589,7 +773,8 @@ def e2e_run(ctx, prob, tis, steps):
     return {"value": statistics.median(vals), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h),
             "what": "C-ABI job from host arrays: solve create (H2D), geometry+shadowing+scattering, "
-                    "device clones for the other inertias, batched revolution loop, temperatures D2H; "
+                    "device clones for the other inertias, the timed workload's batched revolutions, "
+                    "temperatures D2H; "
                     "inputs and read-back buffers page-locked, allocated once before the timed jobs"}
 
 

@@ -192,10 +192,22 @@ atpm_status check_shape(const atpm_shape* sh, const atpm_params* P) {
     for (int i = 0; i < 3 * sh->nf; ++i)
         if (sh->facets[i] < 0 || sh->facets[i] >= sh->nv)
             return fail(ATPM_E_INVALID, "facet vertex index %d out of range", sh->facets[i]);
+    for (int i = 0; i < 3 * sh->nv; ++i)
+        if (!std::isfinite(sh->vertices[i])) return fail(ATPM_E_NONFINITE, "vertex coordinate %d is not finite", i);
+    for (int k = 0; k < nnz; ++k)
+        if (!std::isfinite(sh->dep_vf[k])) return fail(ATPM_E_NONFINITE, "view factor %d is not finite", k);
+    const double scal[] = {P->polar[0], P->polar[1], P->polar[2], P->pole[0], P->pole[1], P->rotation_period_s,
+                           P->albedo, P->emissivity, P->tacc, P->scattering_accuracy};
+    for (double x : scal)
+        if (!std::isfinite(x)) return fail(ATPM_E_INVALID, "a parameter is not finite");
+    if (!(P->rotation_period_s > 0.0f) || !(P->tacc > 0.0f))
+        return fail(ATPM_E_INVALID, "rotation period and TACC must be positive");
     return ATPM_OK;
 }
 
 // Scalars of the reference in its float operand order (main.cpp:1477-1541).
+int newton_cap();
+
 void set_scalars(atpm_solve* s, float ti) {
     const atpm_params& P = s->P;
     DevSolve& d = s->ds;
@@ -243,7 +255,7 @@ void set_scalars(atpm_solve* s, float ti) {
     d.alb_d = (double)P.albedo;
     d.solar_d = (double)d.solar;
     d.sacc_d = (double)P.scattering_accuracy;
-    d.newton_cap = 200;
+    d.newton_cap = newton_cap();
 }
 
 atpm_status upload_table(atpm_solve* s) {
@@ -264,6 +276,15 @@ int cond_variant() {
     const char* e = std::getenv("ATPM_COND_VARIANT");
     if (e && e[0] >= '1' && e[0] <= '3' && e[1] == 0) return e[0] - '0';
     return 3;
+}
+
+// Newton iteration cap of the surface boundary condition (ATPM_NEWTON_CAP,
+// 1..200, default 200); a solve that reaches it stops with ATPM_E_ITERATION.
+// Read when a solve is created and when its thermal inertia is set.
+int newton_cap() {
+    const char* e = std::getenv("ATPM_NEWTON_CAP");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 200 ? v : 200;
 }
 
 bool autotune_enabled() {
@@ -1561,6 +1582,23 @@ ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double
     if (absorbed) *absorbed = d[0];
     if (emitted) *emitted = d[1];
     if (mean_t) *mean_t = d[2] / n;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_selftest_bounded_wait(int32_t device, int64_t limit_cycles, int32_t* status_bits) {
+    if (limit_cycles < 0) return fail(ATPM_E_INVALID, "negative wait limit");
+    CK(cudaSetDevice(device));
+    int* st = nullptr;
+    CK(cudaMalloc(&st, sizeof(int)));
+    int h = 0;
+    cudaError_t e = cudaMemset(st, 0, sizeof(int));
+    if (e == cudaSuccess && launch_wait_selftest(st, (long long)limit_cycles, nullptr)) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, st, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(st);
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "wait self-test: %s", cudaGetErrorString(e));
+    if (status_bits) *status_bits = h;
+    if (h & ST_TC_TIMEOUT) return fail(ATPM_E_ITERATION, "bounded wait gave up after %lld cycles",
+                                       (long long)limit_cycles);
     return ATPM_OK;
 }
 

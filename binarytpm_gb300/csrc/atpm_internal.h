@@ -235,6 +235,7 @@ int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t st);
 // tensor-core self-heating (atpm_spmm_tc.cu)
 int launch_w_bf16_one(const DevSolve& s, stream_t st);
 int launch_spmm_tc(const Batch& b, stream_t st);
+int launch_wait_selftest(int* status, long long limit, stream_t st);
 size_t spmm_tc_smem_bytes(int N, int stages = 0);  // 0: deepest ring that fits
 int tc_max_chunk();  // largest step chunk N of the tensor-core product
 bool conduction_nx_supported(int nx);

@@ -78,13 +78,18 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// bounded wait: false after ~1 s
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// bounded wait: false after `limit` clock cycles
+__device__ __forceinline__ bool mbar_wait_lim(uint64_t* bar, uint32_t parity, long long limit) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > WAIT_CYCLES) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
+}
+
+// bounded wait of the product pipeline: false after ~1 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_lim(bar, parity, WAIT_CYCLES);
 }
 
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
@@ -581,6 +586,28 @@ __global__ void __launch_bounds__(256) k_w_bf16_one(DevSolve sv) {
     const __nv_bfloat16 hi = __float2bfloat16_rn(w);
     W[base + swz(s % N, f % TC_K)] = hi;
     W[base + (size_t)N * TC_K + swz(s % N, f % TC_K)] = __float2bfloat16_rn(w - __bfloat162float(hi));
+}
+
+// Self-test of the bounded wait: one thread waits on an mbarrier that
+// nothing arrives at, gives up after `limit` cycles and reports
+// ST_TC_TIMEOUT, the path every wait of k_spmm_tc takes when its copies or
+// products never land.  No copy, product or TMEM allocation is involved.
+__global__ void k_wait_selftest(int* status, long long limit) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_lim(&bar, 0u, limit)) atomicOr(status, ST_TC_TIMEOUT);
+}
+
+int launch_wait_selftest(int* status, long long limit, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    if (limit < 0) limit = 0;
+    if (limit > WAIT_CYCLES) limit = WAIT_CYCLES;
+    k_wait_selftest<<<1, 32, 0, st>>>(status, limit);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 int launch_w_bf16_one(const DevSolve& s, stream_t stv) {

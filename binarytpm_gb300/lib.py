@@ -77,6 +77,7 @@ _SIGS = {
     "atpm_last_run_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_last_run_config": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_selftest_bounded_wait": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p]),
     "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_scattering_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

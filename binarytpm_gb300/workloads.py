@@ -92,6 +92,42 @@ def fast_vs_fp64(ctx, prob, tis, revs, shadow, illum):
             "schedule": f"{revs} revolutions, every facet advancing (freeze off), same forcing"}
 
 
+def fp64_errors(ctx, prob, solves, tis, revs, shadow, illum, freeze=True, run=False):
+    """Errors of already-prepared solves (any precision, one per thermal
+    inertia in ``tis``) against plain FP64 run on the same schedule: FP64
+    solves from the same forcing and initial temperatures for ``revs``
+    revolutions with the same freeze setting.  With ``run`` the given
+    solves are first given the forcing and run as one batch; otherwise
+    their current state is compared (they must have run that schedule).
+    Returns the max |T - T_fp64| and the relative error of the
+    disk-integrated 12 um flux seen from the Sun (FP64 on the GPU)."""
+    from . import lib
+
+    if run:
+        for s, ti in zip(solves, tis):
+            s.set_forcing(shadow, illum)
+            s.set_thermal_inertia(ti)
+            s.initialise_temperatures()
+        lib.batch_run(solves)
+    ref = lib.Solve(ctx, prob, precision=lib.FP64, revcap=revs, freeze=freeze)
+    ref.set_forcing(shadow, illum)
+    errs, ferrs, nrev = {}, {}, {}
+    for s, ti in zip(solves, tis):
+        ref.set_thermal_inertia(ti)
+        ref.initialise_temperatures()
+        nrev[str(ti)] = int(len(ref.run()))
+        t64 = ref.surface_temperature64()
+        errs[str(ti)] = float(np.max(np.abs(s.surface_temperature64() - t64)))
+        F64 = ref.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
+        F = s.disk_flux(prob.polar, (12.0,), shadow)[:, 0]
+        ferrs[str(ti)] = float(np.max(np.abs(F - F64) / np.abs(F64)))
+    ref.close()
+    return {"max_temperature_error_K": max(errs.values()), "max_rel_flux_error_12um": max(ferrs.values()),
+            "per_ti_max_K": errs, "per_ti_rel_flux": ferrs, "fp64_revolutions": nrev,
+            "schedule": f"revolution cap {revs}, freeze {'on' if freeze else 'off'}, same forcing and "
+                        "initial temperatures"}
+
+
 def single_problem(ctx, subdiv=3, ntau=720, nx=56, seed=1) -> P.Problem:
     v, f = P.single_body_mesh(subdiv, 0.39, 0.05, seed)
     ptr, idx, vf = _lists(ctx, v, f)

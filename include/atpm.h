@@ -215,6 +215,14 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,
                                          double* mean_temperature);
+/* Failure-path self-test of the bounded waits: a one-thread kernel waits on
+ * an mbarrier that nothing arrives at, with the bounded wait every pipeline
+ * wait of the tensor-core product uses (limit_cycles clock cycles, at most
+ * ~1 s), records ST_TC_TIMEOUT (16) in status_bits and returns.  Returns
+ * ATPM_E_ITERATION when the wait gave up (the expected outcome) and leaves
+ * the device context usable.  No copy, product or TMEM allocation runs.
+ * No counterpart in the reference, whose kernels have no bounded waits. */
+ATPM_API atpm_status atpm_selftest_bounded_wait(int32_t device, int64_t limit_cycles, int32_t* status_bits);
 /* Launch configuration of the last atpm_batch_run led by s (FAST): the
  * conduction register/occupancy variant (1-3), the tensor-core pipeline
  * depth, and whether that run timed the candidates (the autotuner does so

@@ -504,29 +504,71 @@ def build_nonsync(cfg: dict, threads: int = 1, revcap: int = 301) -> Path:
     return exe
 
 
-def patch_selfheating(nv: int, nf: int, shape: str, threads: int) -> str:
+def patch_selfheating(nv: int, nf: int, shape: str) -> str:
     src = (REF_ROOT / SELFHEAT_SRC).read_text(errors="replace")
     src = _sub_const(src, "ASTNUMVTX", str(nv))
     src = _sub_const(src, "ASTNUMFACE", str(nf))
     src = _sub_const(src, "filename", '"%s"' % shape)
-    src = _sub_const(src, "num_threads", str(threads))
+    # a compile-time macro, so one scratch copy serves every host
+    src = _sub_const(src, "num_threads", "ORACLE_THREADS")
     return src
 
 
-def build_selfheating(nv: int, nf: int, shape: str, threads: int = 8) -> Path:
-    cfg = dict(nv=nv, nf=nf, shape=shape, threads=threads)
-    d = OUT_ROOT / _tag("selfheating", cfg)
-    exe = d / "selfheating"
+def selfheating_source(nv: int, nf: int, shape: str) -> Path:
+    """Write (once) the scratch copy of Shape_Selfheating for this mesh size."""
+    d = OUT_ROOT / _tag("selfheating", dict(nv=nv, nf=nf, shape=shape))
     src_path = d / "main.cpp"
-    if exe.exists():
-        return exe
-    d.mkdir(parents=True, exist_ok=True)
     if not src_path.exists():
         if not (REF_ROOT / SELFHEAT_SRC).exists():
             raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
-        src_path.write_text(patch_selfheating(nv, nf, shape, threads))
-    subprocess.run(["g++", *CXXFLAGS, str(src_path), "-o", str(exe)], check=True)
+        d.mkdir(parents=True, exist_ok=True)
+        src_path.write_text(patch_selfheating(nv, nf, shape))
+    return src_path
+
+
+def build_selfheating(nv: int, nf: int, shape: str, threads: int = 8) -> Path:
+    src_path = selfheating_source(nv, nf, shape)
+    exe = src_path.parent / ("selfheating_t%d" % threads)
+    if exe.exists():
+        return exe
+    subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % threads, str(src_path), "-o", str(exe)], check=True)
     return exe
+
+
+SELFHEATING_OUTPUTS = ("_selfheating_list.txt", "_selfheating_vector_list.txt", "_photovectors.txt")
+
+
+def _write_shape(path: Path, vertices, facets) -> None:
+    """The reference's text mesh: vertex rows (17 significant digits) then
+    facet rows of 0-based vertex indices, the layout its readers take
+    (3905/Shape_Selfheating/main.cpp:118-121, used as offsets from beginv())."""
+    with open(path, "w") as fh:
+        for x in vertices:
+            fh.write("%.17g\t%.17g\t%.17g\n" % (x[0], x[1], x[2]))
+        for t in facets:
+            fh.write("%d\t%d\t%d\n" % (t[0], t[1], t[2]))
+
+
+def selfheating_inputs(vertices, facets, threads: int, cache_root: Path, shape: str = "shape") -> Path:
+    """The Thermal stage's inputs for a mesh made the reference's way: the
+    mesh in the reference's text format and the view-factor lists, vector
+    list and photon vectors written by the reference's own Shape_Selfheating
+    program (scratch copy, compiled here).  Cached under
+    ``cache_root/refinputs_<mesh digest>/``; returns that directory."""
+    import numpy as np
+
+    v = np.ascontiguousarray(vertices, np.float64)
+    f = np.ascontiguousarray(facets, np.int32)
+    digest = hashlib.sha1(v.tobytes() + f.tobytes()).hexdigest()[:16]
+    d = Path(cache_root) / f"refinputs_{digest}"
+    if all((d / (shape + s)).exists() for s in SELFHEATING_OUTPUTS) and (d / "done").exists():
+        return d
+    d.mkdir(parents=True, exist_ok=True)
+    _write_shape(d / (shape + ".txt"), v, f)
+    exe = build_selfheating(len(v), len(f), shape, threads=threads)
+    run(exe, d)
+    (d / "done").write_text("reference Shape_Selfheating outputs complete\n")
+    return d
 
 
 def patch_visibility(cfg: dict) -> str:

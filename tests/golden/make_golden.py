@@ -57,6 +57,13 @@ CASES = {
     # crater partial visibility toward the observer (Visibility's GPU module)
     "vis_rough_s1s1": dict(kind="visibility", rough=True, mesh=("binary", 1, 1), ntau=48,
                            pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
+    # the single-body configuration at full size: icosphere subdivision 3
+    # (1,280 facets), NX = 56, NTAU = 720 (the explicit scheme's stable step
+    # count at NX = 56), TI 0 (instantaneous equilibrium) then TI 200 to
+    # convergence; large outputs stored as SHA-256 digests of the raw floats
+    "single_s3_nx56": dict(kind="thermal", digest=True, mesh=("single", 3, 1), ntau=720, nx=56, ti=[0.0, 200.0],
+                           pole=(math.pi / 2, 0.0), polar=(1.0, 0.0, 0.0), period_h=2.26, albedo=0.02,
+                           tacc=0.005),
     # crater (roughness) model on: TI 0 (instantaneous equilibrium) then 200
     "rough_s1s1": dict(kind="thermal", rough=True, mesh=("binary", 1, 1), ntau=48, nx=8, ti=[0.0, 200.0],
                        pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9,
@@ -228,6 +235,24 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
             rv = np.loadtxt(wd / "oracle_orbit_revs.txt", ndmin=2)
             out["orbit_counts"] = rv[:, 3].astype(np.int32)
             out["orbit_index"] = rv[:, 0].astype(np.int32)
+        elif c["kind"] == "thermal" and c.get("digest"):
+            import hashlib
+            write_thermal_inputs(wd, v, f, ptr, idx, vf)
+            refbuild.run(refbuild.build_thermal(thermal_cfg(name, threads=c.get("threads", 1))), wd)
+            ntau, n = c["ntau"], nf * c["ntau"]
+            F = np.fromfile(wd / "oracle_forcing.bin", dtype=np.int32).reshape(3, nf, ntau)
+            for k, key in enumerate(("shadow", "illumination", "cosillum")):
+                out["sha256_" + key] = np.array(hashlib.sha256(F[k].tobytes()).hexdigest())
+            for ti in c["ti"]:
+                T = np.fromfile(wd / ("oracle_temps_%g.bin" % ti), dtype=np.float32)
+                for key, a in (("stemp1", T[:n]), ("stemp0", T[n:2 * n]), ("temp", T[2 * n:])):
+                    out["sha256_%s_%g" % (key, ti)] = np.array(hashlib.sha256(a.tobytes()).hexdigest())
+                # every 97th surface temperature, to locate a difference
+                out["stemp1_sample_%g" % ti] = T[:n:97].copy()
+            revs = np.loadtxt(wd / "oracle_revs.txt", ndmin=2)
+            counts = [revs[np.isclose(revs[:, 0], ti), 2].astype(np.int32) for ti in c["ti"]]
+            out["counts"] = np.concatenate(counts)
+            out["counts_split"] = np.array([len(x) for x in counts], np.int32)
         elif c["kind"] == "thermal":
             exe = refbuild.build_thermal(thermal_cfg(name))
             refbuild.run(exe, wd)

@@ -91,3 +91,22 @@ def test_crater_visibility_oracle_reproduces_golden_digest(tmp_path):
     refbuild.run(refbuild.build_visibility(make_golden.visibility_cfg("vis_rough_s1s1")), tmp_path)
     raw = (tmp_path / "shape_roughness_visibility.dat").read_bytes()
     assert hashlib.sha256(raw).hexdigest() == str(ref["sha256"][0])
+
+
+def test_oracle_reproduces_reference_at_nx56():
+    """At the benchmark's NX = 56 and NTAU = 720 (single body, 1,280 facets,
+    TI 0 then 200 to convergence): the oracle's float mode reproduces the
+    reference run's digests and every per-revolution count."""
+    import hashlib
+
+    prob, ref = golden("single_s3_nx56")
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    o = oracle.single_model(prob, precision=0)
+    assert sha(o["shadow"]) == str(ref["sha256_shadow"])
+    assert sha(o["illumination"]) == str(ref["sha256_illumination"])
+    assert sha(o["cosillum"]) == str(ref["sha256_cosillum"])
+    assert sha(o["stemp1"]) == str(ref["sha256_stemp1_200"])
+    assert sha(o["stemp0"]) == str(ref["sha256_stemp0_200"])
+    assert sha(o["temp"]) == str(ref["sha256_temp_200"])
+    for got, want in zip(o["counts"], ref["counts_list"]):
+        assert np.array_equal(got, want)
