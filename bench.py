@@ -85,7 +85,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
 
@@ -312,13 +312,22 @@ def run_reference_arm(args, world, rank):
     inputs, dims = reference_inputs(threads)
     inputs_s = time.perf_counter() - t0
     need = args.warmup + args.steps
-    samples = []
-    k = 0
-    while len(samples) < need:
-        ti = BATCH_TI[k % len(BATCH_TI)]
-        n = min(HEADLINE_REVS, need - len(samples))
-        samples += [(ti,) + r for r in reference_revolutions(inputs, dims, ti, n, threads)]
+    plan, k = [], 0
+    while sum(n for _, n in plan) < need:
+        plan.append((BATCH_TI[k % len(BATCH_TI)], min(HEADLINE_REVS, need - sum(n for _, n in plan))))
         k += 1
+    # the thermal inertia is a compile-time constant of the reference program:
+    # one build per run, compiled in parallel before any timing
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import refbuild
+
+    with ThreadPoolExecutor(max_workers=min(len(plan), threads)) as ex:
+        list(ex.map(lambda p: refbuild.build_thermal(_ref_cfg(dims, p[0], threads, p[1])), plan))
+    build_s = time.perf_counter() - t0 - inputs_s
+    samples = []
+    for ti, n in plan:
+        samples += [(ti,) + r for r in reference_revolutions(inputs, dims, ti, n, threads)]
     timed = samples[args.warmup:need]
     fs = sum(r[2] for r in timed)
     secs = sum(r[3] for r in timed)
@@ -334,6 +343,7 @@ def run_reference_arm(args, world, rank):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "reference_inputs": {"viewfactor_lists": "the reference's Shape_Selfheating program on the same mesh",
                                  "seconds": inputs_s, "nnz": _count_list_entries(inputs)},
+            "reference_build_s": build_s,
             "per_revolution_s": [r[3] for r in timed]}
     print(json.dumps(line), flush=True)
 
@@ -745,8 +755,7 @@ def e2e_run(ctx, prob, tis, steps):
     # caller owns, allocated once (the copies themselves are timed every job)
     prob = dataclasses.replace(prob, **{k: lib.pinned_copy(getattr(prob, k))
                                         for k in ("vertices", "facets", "dep_ptr", "dep_idx", "dep_vf")})
-    outs = [(lib.host_buffer((prob.nf, prob.ntau), np.float32), lib.host_buffer((prob.nf, prob.ntau), np.float32))
-            for _ in tis]
+    outs = [lib.host_buffer((prob.nf, prob.ntau), np.float32) for _ in tis]
     vals, h2d, d2h = [], 0, 0
     for _ in range(steps):
         torch.cuda.synchronize()
@@ -761,20 +770,21 @@ def e2e_run(ctx, prob, tis, steps):
             s.initialise_temperatures()
         lib.batch_run(solves)
         fs = solves[0].last_run_stats()[2]
-        temps = [s.surface_temperature(out=o) for s, o in zip(solves, outs)]
+        # the stage's result: every facet's surface temperature at every step
+        temps = [s.result_temperature(out=o) for s, o in zip(solves, outs)]
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         vals.append(fs / dt)
         shape_bytes = prob.vertices.nbytes + prob.facets.nbytes + prob.dep_ptr.nbytes + prob.dep_idx.nbytes + prob.dep_vf.nbytes
         h2d = shape_bytes
-        d2h = sum(t[0].nbytes + t[1].nbytes for t in temps)
+        d2h = sum(t.nbytes for t in temps)
         for s in solves:
             s.close()
     return {"value": statistics.median(vals), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h),
             "what": "C-ABI job from host arrays: solve create (H2D), geometry+shadowing+scattering, "
                     "device clones for the other inertias, the timed workload's batched revolutions, "
-                    "temperatures D2H; "
+                    "surface temperatures (the Thermal stage's result) D2H; "
                     "inputs and read-back buffers page-locked, allocated once before the timed jobs"}
 
 

@@ -51,14 +51,8 @@ template <> struct Ca<MODE_FAST> {
 };
 
 __device__ __forceinline__ float cpow4_exact(const PowTab& t, float x, int* st) {
-    // double-float x^4 corrected to this host's libm powf (atpm_powtab.cpp)
-    float h = __fmul_rn(x, x);
-    float l = __fmaf_rn(x, x, -h);
-    float p = __fmul_rn(h, h);
-    float e = __fmaf_rn(h, h, -p);
-    float c = __fmaf_rn(__fmul_rn(2.0f, h), l, e);
-    float v = __fadd_rn(p, c);
-    return pow_table_fix(t, x, v, st);
+    // x^4 corrected to this host's libm powf (atpm_powtab.cpp)
+    return pow_table_fix(t, x, dev_pow4(x), st);
 }
 
 template <int MODE>

@@ -57,6 +57,34 @@ __device__ __forceinline__ float pow_table_fix(const PowTab& t, float x, float v
     if (x != 0.0f) atomicOr(status, 4 /* ST_POW_RANGE */);
     return v;
 }
+// x^4 and x^3 as the device evaluates them before the exception table
+// (host twins emu_pow4 / emu_pow3): a double-float product from 2^-4 up, and
+// below 2^-4, where that product underflows, one double product rounded to
+// float (x^2 is exact in double)
+__device__ __forceinline__ float dev_pow4(float x) {
+    if (x < 0.0625f) {
+        const double d = (double)x, d2 = __dmul_rn(d, d);
+        return __double2float_rn(__dmul_rn(d2, d2));
+    }
+    const float h = __fmul_rn(x, x);
+    const float l = __fmaf_rn(x, x, -h);
+    const float p = __fmul_rn(h, h);
+    const float e = __fmaf_rn(h, h, -p);
+    const float c = __fmaf_rn(__fmul_rn(2.0f, h), l, e);
+    return __fadd_rn(p, c);
+}
+__device__ __forceinline__ float dev_pow3(float x) {
+    if (x < 0.0625f) {
+        const double d = (double)x;
+        return __double2float_rn(__dmul_rn(__dmul_rn(d, d), d));
+    }
+    const float h = __fmul_rn(x, x);
+    const float l = __fmaf_rn(x, x, -h);
+    const float p = __fmul_rn(h, x);
+    const float e = __fmaf_rn(h, x, -p);
+    const float c = __fmaf_rn(l, x, e);
+    return __fadd_rn(p, c);
+}
 // x^0.25 through two correctly rounded double square roots (host: emu_qroot)
 __device__ __forceinline__ float dev_qroot(float x) { return (float)__dsqrt_rn(__dsqrt_rn((double)x)); }
 #endif
@@ -281,8 +309,9 @@ struct HostPowTab {
     uint32_t log2slots = 0, lo_bits = 0, hi_bits = 0;
     int64_t exceptions = 0;
 };
-// builds the table for exponent e in {3, 4} over [2^-4, 2^12), or for the
-// quarter power (e = -4) over [2^-24, 2^44), and uploads it
+// builds the table for exponent e in {3, 4} over the positive floats below
+// 2^12, or for the quarter power (e = -4) below 2^44 (subnormals included),
+// and uploads it
 int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen);
 // host emulation of the device's double-float x^e (exact IEEE ops)
 float emu_pow3(float x);

@@ -6,17 +6,23 @@
 // correctly rounded: over the floats in [0.5, 5000] about 0.07 % of the
 // results differ by one unit in the last place from the correctly rounded
 // power.  The device evaluates x^e with a double-float product (exact IEEE
-// operations, see emu_pow4/emu_pow3) and then consults an exception table of
-// every float x in [2^-4, 2^12) for which this process's powf(x, e) differs.
+// operations, see emu_pow4/emu_pow3) from 2^-4 up and with one double
+// product rounded to float below 2^-4, where the double-float product
+// underflows, and then consults an exception table of every positive float
+// x below 2^12 (subnormals included) for which this process's powf(x, e)
+// differs.  The low end matters: with TI = 0 the night side of a facet
+// without neighbours in view falls to 0 K and facets seeing it to tiny
+// temperatures (about 0.02 % of the low-range powers differ).
 // The table is built here by calling powf itself on every float of that
 // range (multi-threaded), so it reproduces whatever libm the host links; no
 // libm code or constant is restated.
 //
 // x^0.25 (e = -4) is evaluated on the device as (float)sqrt(sqrt((double)x))
 // (two correctly rounded square roots); about 0.06 % of glibc's powf(x, 0.25f)
-// results differ from it.  Its table covers x in [2^-24, 2^44), temperatures
-// from 2^-6 K to 2048 K (about 3.6e5 exceptions, 1 s on 8 host threads), and
-// is only built when a REFERENCE solve needs it.
+// results differ from it.  Its table covers every positive float below 2^44
+// (temperatures up to 2048 K), and is only built when a REFERENCE solve needs
+// it.  Each table takes one powf call per float of its range, about 2 s on
+// 8 host threads.
 //
 // Build with -ffp-contract=off: the emulation must round each operation.
 #include <cuda_runtime.h>
@@ -36,6 +42,10 @@ namespace atpm {
 // double-float evaluation shared bit-for-bit with the device code
 // (atpm_thermal.cu: dev_pow4 / dev_pow3)
 float emu_pow4(float x) {
+    if (x < 0.0625f) {  // below 2^-4 the double-float product underflows
+        const double d = (double)x, d2 = d * d;
+        return (float)(d2 * d2);
+    }
     float h = x * x;
     float l = std::fma(x, x, -h);        // x^2 = h + l exactly
     float p = h * h;
@@ -45,6 +55,10 @@ float emu_pow4(float x) {
 }
 
 float emu_pow3(float x) {
+    if (x < 0.0625f) {
+        const double d = (double)x;
+        return (float)((d * d) * d);
+    }
     float h = x * x;
     float l = std::fma(x, x, -h);
     float p = h * x;
@@ -64,8 +78,9 @@ static inline uint32_t slot_of(uint32_t key, uint32_t log2slots) {
 
 int build_pow_table(int e, HostPowTab* out, char* err, size_t errlen) {
     const bool q = (e == -4);
-    const float lo = q ? std::ldexp(1.0f, -24) : 0.0625f, hi = q ? std::ldexp(1.0f, 44) : 4096.0f;
-    const uint32_t lo_bits = fbits(lo), hi_bits = fbits(hi);
+    // from the smallest subnormal (bits 1); zero needs no entry (0^e = 0)
+    const float hi = q ? std::ldexp(1.0f, 44) : 4096.0f;
+    const uint32_t lo_bits = 1u, hi_bits = fbits(hi);
     const float ef = q ? 0.25f : (float)e;
     unsigned nth = std::thread::hardware_concurrency();
     if (nth == 0) nth = 4;

@@ -55,24 +55,6 @@ template <> struct Ar<MODE_FAST> {
     static __device__ __forceinline__ R fabs_(R a) { return fabsf(a); }
 };
 
-// double-float x^4 / x^3 (bit-identical to emu_pow4 / emu_pow3 on the host)
-__device__ __forceinline__ float dev_pow4(float x) {
-    float h = __fmul_rn(x, x);
-    float l = __fmaf_rn(x, x, -h);
-    float p = __fmul_rn(h, h);
-    float e = __fmaf_rn(h, h, -p);
-    float c = __fmaf_rn(__fmul_rn(2.0f, h), l, e);
-    return __fadd_rn(p, c);
-}
-__device__ __forceinline__ float dev_pow3(float x) {
-    float h = __fmul_rn(x, x);
-    float l = __fmaf_rn(x, x, -h);
-    float p = __fmul_rn(h, x);
-    float e = __fmaf_rn(h, x, -p);
-    float c = __fmaf_rn(l, x, e);
-    return __fadd_rn(p, c);
-}
-
 __device__ __forceinline__ float pow_fix(const PowTab& t, float x, float v, int* status) {
     return pow_table_fix(t, x, v, status);
 }

@@ -334,6 +334,16 @@ class Solve:
         _ck(load().atpm_get_surface_temperature(self.h, _p(s1), _p(s0)))
         return s1, s0
 
+    def result_temperature(self, out=None):
+        """stemp1 alone as [nf][ntau] FP32: the surface temperature of every
+        facet and step that the Thermal stage writes as its result
+        (writeglobaltemperature, 3905/Thermal/NominalPole/main.cpp:2302-2306).
+        ``out``: an array to fill instead of a new one."""
+        shp = (self.nf, self.ntau)
+        s1 = _host_out(shp, np.float32) if out is None else _out_arg(out, shp, np.float32, "out")
+        _ck(load().atpm_get_surface_temperature(self.h, _p(s1), None))
+        return s1
+
     def surface_temperature64(self):
         s1 = _host_out((self.nf, self.ntau), np.float64)
         _ck(load().atpm_get_surface_temperature64(self.h, _p(s1)))
