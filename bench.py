@@ -270,8 +270,9 @@ def profile_case(nsolves: int = 2):
         s.initialise_temperatures()
     for _ in range(3):
         k = lib.profile_revolution(solves)
-    tiles, lo = _tile_stats(prob)
-    print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz, "tiles": tiles, "lo_tiles": lo}))
+    tiles, lo, rem = _tile_stats(prob)
+    print(json.dumps({"profile_case": k, "nf": prob.nf, "nnz": prob.nnz, "tiles": tiles, "lo_tiles": lo,
+                      "remainder_entries": rem}))
 
 
 def precision_stress(p_subdiv: int):
@@ -289,11 +290,11 @@ def precision_stress(p_subdiv: int):
     s0.scattering()
     shadow, illum = s0.shadow(), s0.illumination()
     s0.close()
-    tiles, lo = _tile_stats(prob)
+    tiles, lo, rem = _tile_stats(prob)
     t1 = time.perf_counter()
     err = workloads.fast_vs_fp64(ctx, prob, [50.0, 800.0], ACC_REVS, shadow, illum)
     print(json.dumps({"precision_stress": err, "workload": prob.name, "nf": prob.nf, "nnz": int(prob.nnz),
-                      "mean_list_length": prob.nnz / prob.nf, "tiles": tiles, "lo_tiles": lo,
+                      "mean_list_length": prob.nnz / prob.nf, "tiles": tiles, "lo_tiles": lo, "remainder_entries": rem,
                       "viewfactor_s": vf_s, "comparison_s": time.perf_counter() - t1}), flush=True)
 
 
@@ -624,6 +625,13 @@ def cpu_baseline(prob):
         return {"value": None, "unit": UNIT, "cores": threads, "kind": "reference", "sample": f"failed: {ex}"}
 
 
+def _tc_min_entries() -> int:
+    from binarytpm_gb300 import workloads
+
+    e = os.environ.get("ATPM_TC_MIN_ENTRIES")
+    return int(e) if e and e.isdigit() and 1 <= int(e) <= 8192 else workloads.TC_MIN_ENTRIES
+
+
 def _mesh_digest(v, f) -> str:
     import hashlib
 
@@ -680,44 +688,59 @@ ACC_REVS = 40
 
 
 def _tile_stats(prob, slices=False):
-    """Tile structure of the FAST tensor-core product: 128x64 tiles touched,
-    how many of them carry the residual (workloads.tc_tile_structure), and
-    with ``slices`` the 128x16 K slices holding an entry (all tiles; residual
-    tiles): the products the kernel issues."""
+    """Tile structure of the FAST tensor-core product: 128x64 tiles kept,
+    how many of them carry the residual, and the list entries left to the
+    sparse FP32 remainder (workloads.tc_tile_structure); with ``slices`` also
+    the 128x16 K slices holding an entry (all tiles; residual tiles): the
+    products the kernel issues."""
     from binarytpm_gb300 import workloads
 
     tiles, inv, sl, has_lo = workloads.tc_tile_structure(prob.nf, prob.dep_ptr, prob.dep_idx, prob.dep_vf)
+    rem = int((inv < 0).sum())
     if not slices:
-        return len(tiles), int(has_lo.sum())
-    sk = np.unique(inv.astype(np.int64) * 4 + sl)
-    return len(tiles), int(has_lo.sum()), len(sk), int(has_lo[sk // 4].sum())
+        return len(tiles), int(has_lo.sum()), rem
+    t = inv >= 0
+    sk = np.unique(inv[t].astype(np.int64) * 4 + sl[t])
+    return len(tiles), int(has_lo.sum()), rem, len(sk), int(has_lo[sk // 4].sum())
 
 
 def _roofline(kern, n, prob, hbm, bf16, kind):
-    """Dominant kernel of the revolution loop: the tensor-core self-heating
-    product (k_spmm_tc).  Algorithmic FLOP per solve-revolution =
-    2 * nnz * NTAU (the list sum); executed = every issued 128x16 K slice x
-    step chunk x (2 or 3 BF16 products for the hi/lo compensation).  The conduction sweep
-    is reported beside it: 20 B algorithmic HBM per facet-step."""
+    """Dominant kernel of the revolution loop: the self-heating product
+    (k_spmm_tc, tensor-core tiles plus the FP32 sparse remainder in its
+    epilogue).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
+    BF16 + 4 B index) + 8 F NTAU bytes per solve, is ~52 FLOP/B, below the
+    GB300 ridge (~290), so the bound is HBM: achieved = algorithmic bytes per
+    launch (view factors once, shared by the batch's clones; W read and Q
+    written per solve) / CUDA-event duration.  The tensor-pipe figures are
+    beside it: algorithmic FLOP/s, and executed = every issued 128x16 K
+    slice x step chunk x (2 or 3 BF16 products for the hi/lo compensation).
+    The conduction sweep is reported beside it."""
     out = {}
     k = kern.get("selfheat_q")
     if k and k["ms"]:
+        sec = k["ms"] / 1e3
         flops = 2.0 * prob.nnz * prob.ntau * n
-        tiles, lo, sl, sl_lo = _tile_stats(prob, slices=True)
+        alg_bytes = prob.nnz * 6.0 + n * 8.0 * prob.nf * prob.ntau
+        tiles, lo, rem, sl, sl_lo = _tile_stats(prob, slices=True)
         ntau_pad = -(-prob.ntau // 144) * 144 if prob.ntau > 160 else -(-prob.ntau // 16) * 16
         exe = (2 * sl + sl_lo) * 128.0 * 16 * ntau_pad * 2 * n
         traffic = None
         tf = ROOT / "profiles" / "spmm_tc_traffic.json"
         if tf.exists():
             t = json.loads(tf.read_text())
-            traffic = t["dram_bytes_per_tile_chunk"] * tiles * (ntau_pad // 144 if prob.ntau > 160 else 1) * n
-        ach = flops / (k["ms"] / 1e3) / 1e12
-        out = {"kernel": "k_spmm_tc", "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-               "frac": ach / bf16, "peak_kind": kind, "traffic": traffic, "algorithmic_flop": flops,
-               "executed_tflops": exe / (k["ms"] / 1e3) / 1e12, "executed_frac": exe / (k["ms"] / 1e3) / 1e12 / bf16,
-               "note": "algorithmic = 2 nnz NTAU; executed counts the zero padding of the issued 128x16 K "
-                       f"slices ({sl} of the {4 * tiles} in {tiles} tiles; {sl_lo} in the {lo} tiles with "
-                       "residual) and the hi/lo products"}
+            if "dram_bytes_per_solve_revolution" in t:
+                traffic = t["dram_bytes_per_solve_revolution"] * n
+        gbs = alg_bytes / sec / 1e9
+        out = {"kernel": "k_spmm_tc", "bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+               "frac": gbs / hbm, "peak_kind": kind, "traffic": traffic, "algorithmic_bytes": alg_bytes,
+               "tensor": {"achieved_tflops": flops / sec / 1e12, "peak_tflops": bf16,
+                          "frac": flops / sec / 1e12 / bf16, "algorithmic_flop": flops,
+                          "executed_tflops": exe / sec / 1e12, "executed_frac": exe / sec / 1e12 / bf16},
+               "tiles": tiles, "residual_tiles": lo, "remainder_entries": rem, "nnz": int(prob.nnz),
+               "note": "algorithmic bytes = nnz x 6 B + solves x 8 B x F x NTAU; executed tensor FLOP count the "
+                       f"zero padding of the issued 128x16 K slices ({sl} of the {4 * tiles} in {tiles} tiles; "
+                       f"{sl_lo} in the {lo} tiles with residual) and the hi/lo products; {rem} of {prob.nnz} "
+                       f"entries (cells with < {_tc_min_entries()} entries) are summed in FP32 in the epilogue"}
     c = kern.get("conduction")
     if c and c["ms"]:
         nx = prob.nx

@@ -310,6 +310,22 @@ int warp_tail_per_sm() {
     return v >= 1 && v <= 64 ? v : 12;
 }
 
+// Fewest list entries a (128-row, 64-column) cell needs to become a
+// tensor-core tile (ATPM_TC_MIN_ENTRIES, 1..8192, default 32).  The entries of
+// sparser cells form the per-row remainder, summed in FP32 against W32 by
+// k_spmm_rem after the tiles' product.  On the 21,760-facet binary the 4,173
+// cells with at least 32 entries hold 99.0 % of the 5.8 M entries and the
+// other 8,784 cells (68 % of all cells, mostly facets of one body seeing
+// each other across its surface relief) 1.0 %; per 8-solve revolution the
+// product took 1.76 / 1.71 / 1.73 / 1.82 ms at thresholds 16 / 32 / 64 / 128
+// against 2.12 ms with every cell a tile.  The split changes rounding (the
+// remainder is FP32 instead of BF16 hi/lo), not the result beyond it.
+int tc_min_entries() {
+    const char* e = std::getenv("ATPM_TC_MIN_ENTRIES");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 128 * 64 ? v : 32;
+}
+
 bool tc_enabled() {
     const char* e = std::getenv("ATPM_TC");
     return !(e && e[0] == '0');
@@ -371,27 +387,30 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     tc_chunks(ntau, &N, &nch);
     const size_t ncell = (size_t)nmb * nkb;
     if (nkb >= (1 << 24)) return fail(ATPM_E_UNSUPPORTED, "tensor-core tiles: %d facets exceed the column-block index", nf);
-    (void)sh;
     std::vector<float> vm(ncell, -1.0f);
     std::vector<uint8_t> km(ncell, 0);  // which 16-wide K slices of the tile hold an entry
     std::vector<unsigned> need(ncell, 0);  // the tile needs its residual for some row's flux
+    const unsigned min_entries = (unsigned)tc_min_entries();
     {
-        std::vector<unsigned> cmax(ncell), cmask(ncell);
+        std::vector<unsigned> cmax(ncell), cmask(ncell), cnt(ncell);
         unsigned* dc = nullptr;
-        CK(cudaMalloc((void**)&dc, ncell * 3 * sizeof(unsigned)));
-        cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 3 * sizeof(unsigned), s->st);
-        if (e == cudaSuccess && launch_tc_cells(s->ds, nkb, dc, dc + ncell, s->st)) e = cudaGetLastError();
+        CK(cudaMalloc((void**)&dc, ncell * 4 * sizeof(unsigned)));
+        cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 4 * sizeof(unsigned), s->st);
+        if (e == cudaSuccess && launch_tc_cells(s->ds, nkb, dc, dc + ncell, dc + 3 * ncell, s->st))
+            e = cudaGetLastError();
         if (e == cudaSuccess && launch_tc_rowneed(s->ds, nkb, dc + 2 * ncell, s->st) == 2) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(cmax.data(), dc, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(cmask.data(), dc + ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(need.data(), dc + 2 * ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(cnt.data(), dc + 3 * ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
         cudaFree(dc);
         if (e != cudaSuccess) return fail(ATPM_E_CUDA, "tile structure: %s", cudaGetErrorString(e));
         for (size_t c = 0; c < ncell; ++c) {
-            if (!cmax[c]) continue;
+            if (!cmax[c] || cnt[c] < min_entries) continue;  // empty, or left to the remainder
             uint32_t bits = cmax[c] - 1u;
             float v;
             std::memcpy(&v, &bits, 4);
@@ -416,6 +435,25 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     }
     const size_t ntiles = tcol.size();
     const size_t tile_el = 128 * 64;
+    // the sparse remainder: entries of cells without a tile, per row in list order
+    std::vector<int> rptr(nf + 1, 0), ridx;
+    std::vector<float> rvf;
+    for (int f = 0; f < nf; ++f) {
+        const size_t row = (size_t)(f >> 7) * nkb;
+        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
+            const int g = sh->dep_idx[k];
+            if (slot[row + (size_t)(g >> 6)] >= 0) continue;
+            ridx.push_back(g);
+            rvf.push_back(sh->dep_vf[k]);
+        }
+        rptr[f + 1] = (int)ridx.size();
+    }
+    const size_t rnnz = ridx.size();
+    const size_t b_rptr = rnnz ? align256((size_t)(nf + 1) * 4) : 0, b_ridx = rnnz ? align256(rnnz * 4) : 0;
+    const size_t b_rvf = b_ridx;
+    // W32 row stride: the steps rounded up to the remainder kernel's 32-step
+    // chunks (every lane's load stays inside its row; the pad stays zero)
+    const int w32_ld = (ntau + 31) & ~31;
     if (lo_of.empty()) lo_of.push_back(-1);
     const size_t b_tiles = align256(std::max<size_t>(ntiles, 1) * tile_el * 2);
     const size_t b_ptr = align256((nmb + 1) * 4), b_col = align256(std::max<size_t>(ntiles, 1) * 4);
@@ -424,7 +462,9 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     const size_t b_slot = align256(ncell * 4);
     auto* tc = new TcShared();
     s->tc = tc;
-    tc->bytes = b_tiles + b_ptr + b_col + b_lo + b_loi + b_slot;
+    tc->bytes = b_tiles + b_ptr + b_col + b_lo + b_loi + b_slot + b_rptr + b_ridx + b_rvf;
+    tc->tiles = ntiles;
+    tc->remainder = rnnz;
     tc->rb_tiles.resize(nmb);
     for (int mb = 0; mb < nmb; ++mb) tc->rb_tiles[mb] = tptr[mb + 1] - tptr[mb];
     CK(cudaMalloc(&tc->mem, tc->bytes));
@@ -440,6 +480,15 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     CK(cudaMemsetAsync(p_lo, 0, b_lo, s->st));
     CK(cudaMemcpyAsync(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(d_slot, slot.data(), ncell * 4, cudaMemcpyHostToDevice, s->st));
+    char* p_rem = p_lo + b_lo + b_loi + b_slot;
+    if (rnnz) {
+        CK(cudaMemcpyAsync(p_rem, rptr.data(), (size_t)(nf + 1) * 4, cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(p_rem + b_rptr, ridx.data(), rnnz * 4, cudaMemcpyHostToDevice, s->st));
+        CK(cudaMemcpyAsync(p_rem + b_rptr + b_ridx, rvf.data(), rnnz * 4, cudaMemcpyHostToDevice, s->st));
+        s->w32_bytes = align256((size_t)nf * w32_ld * 4);
+        CK(cudaMalloc(&s->w32_mem, s->w32_bytes));
+        CK(cudaMemsetAsync(s->w32_mem, 0, s->w32_bytes, s->st));
+    }
     if (launch_tc_fill(s->ds, nkb, d_slot, reinterpret_cast<const int*>(p_lo + b_lo), m, p_lo, s->st))
         return fail(ATPM_E_CUDA, "tile fill launch: %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaStreamSynchronize(s->st));  // the host tables must outlive their copies
@@ -454,6 +503,11 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     d.tc_nchunks = nch;
     d.tc_nmb = nmb;
     d.tc_nkb = nkb;
+    d.rem_ptr = rnnz ? reinterpret_cast<const int*>(p_rem) : nullptr;
+    d.rem_idx = rnnz ? reinterpret_cast<const int*>(p_rem + b_rptr) : nullptr;
+    d.rem_vf = rnnz ? reinterpret_cast<const float*>(p_rem + b_rptr + b_ridx) : nullptr;
+    d.W32 = static_cast<float*>(s->w32_mem);
+    d.w32_ld = w32_ld;
     std::vector<int4> q;
     atpm_solve* one[1] = {s};
     build_tc_items(one, 1, q);
@@ -491,7 +545,20 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     // the thread-per-facet sweep's latency-bound last warps
     b.tail_limit = warp_tail_per_sm() * ctx->sm_count;
     b.sms = ctx->sm_count;
+    b.rem_nmb = 0;
+    b.rem_ntau = 0;
     return b;
+}
+
+// the remainder kernel's grid: the largest row-block count and step count of
+// the solves that have a sparse remainder
+void set_remainder_grid(Batch& b, atpm_solve* const* solves, int n) {
+    for (int i = 0; i < n; ++i) {
+        const DevSolve& d = solves[i]->ds;
+        if (!d.rem_ptr) continue;
+        b.rem_nmb = std::max(b.rem_nmb, (d.nf + 127) / 128);
+        b.rem_ntau = std::max(b.rem_ntau, d.ntau);
+    }
 }
 
 
@@ -503,6 +570,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
         *out = make_batch(s0->ctx, s0->ds_dev, 1, s0->wmap, s0->nw, s0->fmap, s0->nfb, s0->P.precision, s0->P.nx);
         set_tc_map(*out, s0->qmap, (size_t)s0->nq);
         out->tc_nmax = s0->ds.tc_n;
+        set_remainder_grid(*out, solves, n);
         return ATPM_OK;
     }
     std::vector<DevSolve> tab(n);
@@ -531,6 +599,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
                       reinterpret_cast<int2*>(t + bt + bw), (int)fm.size(), s0->P.precision, s0->P.nx);
     set_tc_map(*out, reinterpret_cast<int4*>(t + bt + bw + bf), qm.size());
     out->tc_nmax = nmax;
+    set_remainder_grid(*out, solves, n);
     return ATPM_OK;
 }
 
@@ -730,6 +799,7 @@ atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cud
                          reinterpret_cast<int2*>(t + h.bt + h.bw), (int)h.fm.size(), s0->P.precision, s0->P.nx);
     set_tc_map(b, reinterpret_cast<int4*>(t + h.bt + h.bw + h.bf), h.qm.size());
     b.tc_nmax = h.nmax;
+    set_remainder_grid(b, solves, n);
     for (int r = 0; r < k; ++r)
         if (launch_revolution(b, st)) return fail(ATPM_E_CUDA, "batched revolution launch");
     return ATPM_OK;
@@ -800,6 +870,7 @@ ATPM_API atpm_status atpm_solve_footprint(const atpm_shape* sh, const atpm_param
         int N, nch;
         tc_chunks(P->ntau, &N, &nch);
         wb = align256((size_t)((sh->nf + 63) / 64) * nch * N * 64 * 2 * 2);
+        wb += align256((size_t)sh->nf * ((P->ntau + 31) & ~31) * 4);  // W32 of the sparse remainder (when it has one)
     }
     *bytes = (uint64_t)(L.total + wb + std::max(geo, sct) + 64 * 1024);
     return ATPM_OK;
@@ -931,6 +1002,7 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
         delete s->tc;
     }
     if (s->wb_mem) cudaFree(s->wb_mem);
+    if (s->w32_mem) cudaFree(s->w32_mem);
     if (s->qmap) cudaFree(s->qmap);
     if (s->arena) cudaFree(s->arena);
     if (s->st) cudaStreamDestroy(s->st);
@@ -984,6 +1056,15 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
             s->wb_bytes = src->wb_bytes;
             e = cudaMemcpyAsync(s->wb_mem, src->wb_mem, s->wb_bytes, cudaMemcpyDeviceToDevice, s->st);
             s->ds.Wb = s->wb_mem;
+        }
+        s->ds.W32 = nullptr;
+        if (e == cudaSuccess && src->w32_mem) {
+            e = cudaMalloc(&s->w32_mem, src->w32_bytes);
+            if (e == cudaSuccess) {
+                s->w32_bytes = src->w32_bytes;
+                e = cudaMemcpyAsync(s->w32_mem, src->w32_mem, s->w32_bytes, cudaMemcpyDeviceToDevice, s->st);
+                s->ds.W32 = static_cast<float*>(s->w32_mem);
+            }
         }
     }
     if (e == cudaSuccess && src->qmap) {
@@ -1159,7 +1240,13 @@ ATPM_API atpm_status atpm_revolution(atpm_solve* s, int32_t rev, int32_t* numcon
     c.active = 1;
     CK(cudaMemcpyAsync(s->ds.ctl, &c, sizeof c, cudaMemcpyHostToDevice, s->st));
     CK(reset_active_lists(s));  // the caller chooses the revolution: no list carries over
-    Batch b = make_batch(s->ctx, s->ds_dev, 1, s->wmap, s->nw, s->fmap, s->nfb, s->P.precision, s->P.nx);
+    // the same kernels as the revolution loop (tensor-core product and its
+    // sparse remainder for FAST)
+    Batch b;
+    void* tmp = nullptr;
+    atpm_solve* one[1] = {s};
+    atpm_status rb = make_batch_for(one, 1, &b, &tmp);
+    if (rb) return rb;
     if (launch_revolution(b, s->st)) return fail(ATPM_E_CUDA, "revolution launch");
     int st = 0;
     CK(cudaMemcpyAsync(&c, s->ds.ctl, sizeof c, cudaMemcpyDeviceToHost, s->st));

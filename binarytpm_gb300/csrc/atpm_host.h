@@ -38,6 +38,8 @@ struct TcShared {
     void* mem = nullptr;
     size_t bytes = 0;
     std::vector<int> rb_tiles;  // tiles per 128-facet row block (work ordering)
+    size_t tiles = 0;           // tensor-core tiles
+    size_t remainder = 0;       // list entries of the sparse remainder
 };
 
 struct atpm_solve {
@@ -56,6 +58,8 @@ struct atpm_solve {
     TcShared* tc = nullptr;   // tensor-core tiles (FAST), shared with clones
     void* wb_mem = nullptr;   // this solve's BF16 W tiles
     size_t wb_bytes = 0;
+    void* w32_mem = nullptr;  // this solve's FP32 W rows for the sparse remainder
+    size_t w32_bytes = 0;
     int4* qmap = nullptr;
     int nq = 0;
     cudaGraphExec_t graph = nullptr;

@@ -153,6 +153,15 @@ struct DevSolve {
     const void* tc_lo_tiles; // [nlo][128*64] BF16 residual V - bf16(V) of tiles with large entries
     void* Wb;                // [nkb][nchunks][2][tc_n*64] BF16 eps*sigma*T^4 (hi, lo), swizzled
     int tc_n, tc_nchunks, tc_nmb, tc_nkb;
+    // sparse remainder of the view-factor lists (FAST): the entries of the
+    // (128-row, 64-column) cells too sparse for a tensor-core tile, per row
+    // in list order (CSR, FP32 values), summed by the product's epilogue
+    // against W32, this solve's eps*sigma*T^4 facet-major in FP32
+    const int* rem_ptr;      // [nf+1], or null when every entry is in a tile
+    const int* rem_idx;      // [rem_nnz]
+    const float* rem_vf;     // [rem_nnz]
+    float* W32;              // [nf][w32_ld] FP32 (null without a remainder)
+    int w32_ld;              // row stride of W32: ntau rounded up to 8
 };
 
 // element offset of (row, k) inside a 128-byte-swizzled K-major tile with 64
@@ -216,6 +225,8 @@ struct Batch {
                              // (thread per facet; warp per facet below tail_limit)
     int tail_limit;          // active facets of the batch up to which they do
     int sms;                 // SMs of the device (persistent tensor-core grid)
+    int rem_nmb, rem_ntau;   // largest row-block count / steps of the batch's solves with a
+                             // sparse remainder (0: none; the remainder kernel's grid)
 };
 // deepest tensor-core pipeline that fits shared memory for step chunk N
 int tc_max_stages(int N);
@@ -227,7 +238,7 @@ int kernels_per_revolution(const Batch& b);          // kernels launch_revolutio
 // per (row block, column block) cell of the view-factor lists: largest
 // |value| as float bits + 1 (0: no entry) and the mask of 16-wide K slices
 // with an entry; cmax and cmask zeroed by the caller (atpm_spmm_tc.cu)
-int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, stream_t st);
+int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, unsigned* count, stream_t st);
 // cells whose tile needs the BF16 residual for some row's flux (need zeroed
 // by the caller); returns 1 when the shape is too large for the per-row maps
 int launch_tc_rowneed(const DevSolve& s, int nkb, unsigned* need, stream_t st);

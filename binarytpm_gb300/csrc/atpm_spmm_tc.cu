@@ -14,8 +14,16 @@
 // Row blocks whose 128 facets are all frozen (reference freeze protocol)
 // are skipped: their flux is not read.
 //
+// Only the dense part of V goes to the tensor cores: a (128-facet row block,
+// 64-facet column block) cell becomes a tile when it holds at least
+// ATPM_TC_MIN_ENTRIES list entries (32).  The entries of sparser cells (1 %
+// of the binary's entries, in 68 % of its cells: facets of one body seeing
+// each other across its relief) are the sparse remainder, summed in FP32 by
+// k_spmm_rem against W32 (eps sigma T^4 facet-major, written by the
+// conduction sweep beside the BF16 tiles) and added to the tiles' Q.
+//
 // V is stored as 128 x 64 BF16 tiles (block-sparse rows: every 128-facet row
-// block keeps the 64-facet column blocks it touches; one set per shape,
+// block keeps the 64-facet column blocks it has tiles in; one set per shape,
 // shared by clones) and W as 64-facet x N-step tiles (per solve, written by
 // the conduction sweep).  Both are laid out in HBM already in the
 // 128-byte-swizzled K-major form the tensor core reads, so each tile moves
@@ -179,10 +187,11 @@ __device__ __forceinline__ uint16_t bf16_rne(float x) {
 
 // tile structure from the uploaded lists, one warp per facet row: for every
 // (128-facet row block, 64-facet column block) cell the largest |view
-// factor| (its float bits + 1, so 0 marks an empty cell: max and or do not
-// depend on the order the entries arrive in) and the mask of 16-wide K
-// slices holding an entry
-__global__ void __launch_bounds__(256) k_tc_cells(DevSolve s, int nkb, unsigned* cmax, unsigned* cmask) {
+// factor| (its float bits + 1, so 0 marks an empty cell: max, or and add do
+// not depend on the order the entries arrive in), the mask of 16-wide K
+// slices holding an entry and the number of entries
+__global__ void __launch_bounds__(256) k_tc_cells(DevSolve s, int nkb, unsigned* cmax, unsigned* cmask,
+                                                  unsigned* count) {
     const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (f >= s.nf) return;
@@ -192,13 +201,14 @@ __global__ void __launch_bounds__(256) k_tc_cells(DevSolve s, int nkb, unsigned*
         const size_t cell = row + (size_t)(g >> 6);
         atomicMax(&cmax[cell], __float_as_uint(fabsf(s.dep_vf[k])) + 1u);
         atomicOr(&cmask[cell], 1u << ((g & 63) >> 4));
+        atomicAdd(&count[cell], 1u);
     }
 }
 
-int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, stream_t stv) {
+int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, unsigned* count, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const size_t threads = (size_t)s.nf * 32;
-    k_tc_cells<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, cmax, cmask);
+    k_tc_cells<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, cmax, cmask, count);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
@@ -255,8 +265,10 @@ int launch_tc_rowneed(const DevSolve& s, int nkb, unsigned* need, stream_t stv) 
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-// one warp per facet row: every list entry goes to its swizzled slot of its
-// (row block, column block) tile, plus the BF16 residual where the tile has one
+// one warp per facet row: every list entry of a kept tile goes to its
+// swizzled slot of its (row block, column block) tile, plus the BF16 residual
+// where the tile has one; entries of cells without a tile (slot -1) belong to
+// the sparse remainder
 __global__ void __launch_bounds__(256) k_tc_fill(DevSolve s, int nkb, const int* slot, const int* lo_of,
                                                  uint16_t* tiles, uint16_t* lo_tiles) {
     const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
@@ -268,6 +280,7 @@ __global__ void __launch_bounds__(256) k_tc_fill(DevSolve s, int nkb, const int*
         const int g = s.dep_idx[k];
         const float v = s.dep_vf[k];
         const int t = srow[g >> 6];
+        if (t < 0) continue;
         const uint32_t off = swz(row, (uint32_t)(g & 63));
         const uint16_t hb = bf16_rne(v);
         tiles[(size_t)t * (TC_M * TC_K) + off] = hb;
@@ -495,7 +508,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_spmm_tc(Batch b) {
             }
             tc_fence_after();
             const int f = w.y * TC_M + q * 32 + lane;
-            if (T == 0) {  // no other facet seen by this row block
+            if (T == 0) {  // no tile in this row block
                 if (f < nf)
                     for (int n = 0; n < N; ++n) {
                         const int s = nc * N + n;
@@ -547,6 +560,63 @@ size_t spmm_tc_smem_bytes(int N, int stages) {
 
 int tc_max_stages(int N) { return tc_stages(N); }
 
+// The sparse remainder of the product: the list entries of the cells too
+// sparse for a tensor-core tile, added to the tiles' Q in FP32.  One CTA per
+// (solve, 128-facet row block, 32-step chunk); a warp per facet row, lane j
+// on step s0 + j, so every entry is one coalesced 128-byte load of its
+// column facet's W32 row; entries accumulate in list order (four loads in
+// flight), the block's 128 x 32 sums go through shared memory, and Q is
+// updated along facets (coalesced).  Row blocks the tensor-core product
+// skips (all facets frozen) are skipped alike.
+constexpr int REM_STEPS = 32;
+
+__global__ void __launch_bounds__(128) k_spmm_rem(Batch b) {
+    const DevSolve& sv = b.tab[blockIdx.z];
+    const int rb = blockIdx.x, s0 = blockIdx.y * REM_STEPS;
+    const int nf = sv.nf, ntau = sv.ntau;
+    if (!sv.rem_ptr || rb * 128 >= nf || s0 >= ntau || !sv.ctl->active) return;
+    const bool everyone = !sv.freeze || sv.ti == 0.0f;
+    if (!everyone && !sv.rb_act[rb]) return;
+    __shared__ float acc[128][REM_STEPS + 1];
+    __shared__ int any;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    const float* W32 = sv.W32;
+    const size_t ld = (size_t)sv.w32_ld;
+    const int s = s0 + lane;  // W32 rows are padded to the chunk grid: s < w32_ld
+    for (int r = warp; r < 128; r += 4) {
+        const int f = rb * 128 + r;
+        float a = 0.0f;
+        if (f < nf) {
+            int k = __ldg(&sv.rem_ptr[f]);
+            const int k1 = __ldg(&sv.rem_ptr[f + 1]);
+            if (k < k1 && lane == 0) any = 1;
+            for (; k + 4 <= k1; k += 4) {
+                const int g0 = __ldg(&sv.rem_idx[k]), g1 = __ldg(&sv.rem_idx[k + 1]);
+                const int g2 = __ldg(&sv.rem_idx[k + 2]), g3 = __ldg(&sv.rem_idx[k + 3]);
+                const float w0 = W32[(size_t)g0 * ld + s], w1 = W32[(size_t)g1 * ld + s];
+                const float w2 = W32[(size_t)g2 * ld + s], w3 = W32[(size_t)g3 * ld + s];
+                a = fmaf(__ldg(&sv.rem_vf[k]), w0, a);
+                a = fmaf(__ldg(&sv.rem_vf[k + 1]), w1, a);
+                a = fmaf(__ldg(&sv.rem_vf[k + 2]), w2, a);
+                a = fmaf(__ldg(&sv.rem_vf[k + 3]), w3, a);
+            }
+            for (; k < k1; ++k) a = fmaf(__ldg(&sv.rem_vf[k]), W32[(size_t)__ldg(&sv.rem_idx[k]) * ld + s], a);
+        }
+        acc[r][lane] = a;
+    }
+    __syncthreads();
+    if (!any) return;  // no row of this block has a remainder entry
+    float* Q = static_cast<float*>(sv.Q);
+    const int f = rb * 128 + threadIdx.x;
+    if (f >= nf || __ldg(&sv.rem_ptr[f]) == __ldg(&sv.rem_ptr[f + 1])) return;
+    for (int j = 0; j < REM_STEPS && s0 + j < ntau; ++j) {
+        const size_t o = (size_t)(s0 + j) * nf + f;
+        Q[o] = Q[o] + acc[threadIdx.x][j];
+    }
+}
+
 int launch_spmm_tc(const Batch& b, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     if (b.nq == 0) return 0;
@@ -570,6 +640,10 @@ int launch_spmm_tc(const Batch& b, stream_t stv) {
     k_tc_compact<<<(b.nq + 127) / 128, 128, 0, st>>>(b);
     const int grid = b.nq < b.sms ? b.nq : b.sms;  // one persistent CTA per SM
     k_spmm_tc<<<grid, TC_THREADS, smem, st>>>(b);
+    if (b.rem_nmb > 0) {
+        const dim3 g((unsigned)b.rem_nmb, (unsigned)((b.rem_ntau + REM_STEPS - 1) / REM_STEPS), (unsigned)b.n);
+        k_spmm_rem<<<g, 128, 0, st>>>(b);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
@@ -610,11 +684,41 @@ int launch_wait_selftest(int* status, long long limit, stream_t stv) {
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+// W32[f][s] = eps sigma T^4 from the current surface temperatures (FP32,
+// facet-major) through 32 x 32 tiles transposed in shared memory: the
+// remainder's operand, set up with the temperatures (the conduction sweeps
+// keep it current after that)
+__global__ void __launch_bounds__(256) k_w32_fill(DevSolve sv) {
+    __shared__ float t[32][33];
+    const int f0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const float* S1 = static_cast<const float*>(sv.stemp1);
+    for (int j = ty; j < 32; j += 8) {
+        const int s = s0 + j, f = f0 + tx;
+        float w = 0.0f;
+        if (s < sv.ntau && f < sv.nf) {
+            const float x = S1[(size_t)s * sv.nf + f];
+            const float x2 = x * x;
+            w = sv.es_w * (x2 * x2);
+        }
+        t[j][tx] = w;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int f = f0 + j, s = s0 + tx;
+        if (f < sv.nf && s < sv.ntau) sv.W32[(size_t)f * sv.w32_ld + s] = t[tx][j];
+    }
+}
+
 int launch_w_bf16_one(const DevSolve& s, stream_t stv) {
     if (!s.tc_tiles) return 0;
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const size_t n = (size_t)s.nf * s.ntau;
     k_w_bf16_one<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s);
+    if (s.W32) {
+        dim3 g((unsigned)((s.nf + 31) / 32), (unsigned)((s.ntau + 31) / 32));
+        k_w32_fill<<<g, 256, 0, st>>>(s);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

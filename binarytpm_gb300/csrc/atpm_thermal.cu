@@ -231,6 +231,7 @@ __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float 
     const __nv_bfloat16 hi = __float2bfloat16_rn(w);
     W[base + o] = hi;
     W[base + (size_t)N * 64 + o] = __float2bfloat16_rn(w - __bfloat162float(hi));
+    if (sv.W32) sv.W32[(size_t)f * sv.w32_ld + s] = w;
 }
 
 // FAST precision: the same update, scheduled for the FP32 pipes.
@@ -308,6 +309,11 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     // behind other warps
     constexpr int D = kFastPrefetch;
     __shared__ float pre[D][3][128];
+    // the last 8 values of eps sigma T^4, written to this facet's W32 row
+    // as two 16-byte stores per 8 steps (one full 32-byte sector)
+    __shared__ float w8[8][128];
+    float* W32 = Wb ? sv.W32 : nullptr;
+    float* w32row = W32 ? W32 + (size_t)f * sv.w32_ld : nullptr;
     const int lt = threadIdx.x;
     for (int j = 0; j < D; ++j) {
         if (j < ntau) {
@@ -356,6 +362,14 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
             Wb[wrow + off] = hi;
             Wb[wrow + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
             if (++wn == N) { wn = 0; wrow += chunk; }
+            if (w32row) {
+                w8[s & 7][lt] = w;
+                if ((s & 7) == 7) {
+                    float4* d = reinterpret_cast<float4*>(w32row + (s - 7));
+                    d[0] = make_float4(w8[0][lt], w8[1][lt], w8[2][lt], w8[3][lt]);
+                    d[1] = make_float4(w8[4][lt], w8[5][lt], w8[6][lt], w8[7][lt]);
+                }
+            }
         }
         T[NX] = T[NX - 1];
         hot = hot || (fabsf(Tsurf - old) >= tacc);
@@ -370,6 +384,8 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         if (++slot == D) slot = 0;
     }
     cp_async_wait<0>();
+    if (w32row)  // the steps after the last full group of 8
+        for (int s = ntau & ~7; s < ntau; ++s) w32row[s] = w8[s & 7][lt];
     if (!isfinite(T[0] + Tref)) flags |= ST_NONFINITE;
 #pragma unroll
     for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = Tref + T[i];
@@ -485,6 +501,7 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
                 const __nv_bfloat16 hi = __float2bfloat16_rn(w);
                 Wb[base + off] = hi;
                 Wb[base + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
+                if (sv.W32) sv.W32[(size_t)f * sv.w32_ld + s] = w;  // 32 lanes: one 128-byte row segment
             }
         }
         ca = fmaf(oma, ne, nq);
@@ -819,7 +836,8 @@ int launch_revolution_part(const Batch& b, int part, stream_t stv) {
 
 int kernels_per_revolution(const Batch& b) {
     const bool tc = b.mode == MODE_FAST && b.nq > 0;
-    const int selfheat = tc ? 2 : (b.nw > 0 ? 2 : 0);  // k_tc_compact + k_spmm_tc, or W + Q
+    // k_tc_compact + k_spmm_tc (+ k_spmm_rem), or W + Q
+    const int selfheat = tc ? 2 + (b.rem_nmb > 0 ? 1 : 0) : (b.nw > 0 ? 2 : 0);
     const int conduction = b.mode == MODE_FAST ? 3 : 1;  // + k_tail_mode, k_conduction_warp
     return selfheat + conduction + 2;                    // + k_converge, k_advance
 }

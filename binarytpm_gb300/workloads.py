@@ -137,20 +137,33 @@ def single_problem(ctx, subdiv=3, ntau=720, nx=56, seed=1) -> P.Problem:
                      thermal_inertia=200.0, tacc=0.005, name=f"single_s{subdiv}")
 
 
-def tc_tile_structure(nf, dep_ptr, dep_idx, dep_vf):
+# fewest list entries a (128-row, 64-column) cell needs to become a
+# tensor-core tile (the library's default, ATPM_TC_MIN_ENTRIES)
+TC_MIN_ENTRIES = 32
+
+
+def tc_tile_structure(nf, dep_ptr, dep_idx, dep_vf, min_entries=TC_MIN_ENTRIES):
     """The FAST tensor-core tiling of a view-factor list, restated in numpy:
-    the 128 x 64 tiles touched (keys row block * nkb + column block, sorted),
-    the tile of every list entry, the entries' 16-wide K slices, and which
-    tiles carry the residual V - bf16(V): a view factor >= 1e-4, or, for
-    some facet row, at least 1 % of that row's mean |view factor| per
-    64-facet column block it touches (the rule of build_tc/k_tc_rowneed)."""
+    the 128 x 64 tiles kept (keys row block * nkb + column block, sorted:
+    cells holding at least ``min_entries`` list entries), the tile of every
+    list entry (-1 for the entries of sparser cells, the sparse remainder
+    summed in FP32 outside the tensor cores), the entries' 16-wide K slices,
+    and which tiles carry the residual V - bf16(V): a view factor >= 1e-4,
+    or, for some facet row, at least 1 % of that row's mean |view factor|
+    per 64-facet column block it touches (the rule of build_tc/k_tc_rowneed;
+    that mean counts every column block the row touches, tile or not)."""
     nkb = (nf + 63) // 64
     rows = np.repeat(np.arange(nf), np.diff(dep_ptr))
     av = np.abs(np.asarray(dep_vf, np.float32))
     key = (rows // 128).astype(np.int64) * nkb + np.asarray(dep_idx) // 64
-    tiles, inv = np.unique(key, return_inverse=True)
-    vmax = np.zeros(len(tiles), np.float32)
-    np.maximum.at(vmax, inv, av)
+    cells, cinv, ccount = np.unique(key, return_inverse=True, return_counts=True)
+    keep = ccount >= min_entries
+    tiles = cells[keep]
+    tile_of_cell = np.full(len(cells), -1, np.int64)
+    tile_of_cell[keep] = np.arange(keep.sum())
+    inv = tile_of_cell[cinv] if len(cinv) else np.zeros(0, np.int64)
+    vmax = np.zeros(len(cells), np.float32)
+    np.maximum.at(vmax, cinv, av)
     has_lo = vmax >= np.float32(1e-4)
     rk = rows.astype(np.int64) * nkb + np.asarray(dep_idx) // 64
     u, rinv = np.unique(rk, return_inverse=True)
@@ -160,9 +173,9 @@ def tc_tile_structure(nf, dep_ptr, dep_idx, dep_vf):
     n = np.bincount(r, minlength=nf)
     need = 100.0 * n[r] * m >= M[r]
     need_keys = np.unique((r[need] // 128) * nkb + u[need] % nkb)
-    has_lo |= np.isin(tiles, need_keys)
+    has_lo |= np.isin(cells, need_keys)
     slices = np.asarray(dep_idx) % 64 // 16
-    return tiles, inv, slices, has_lo
+    return tiles, inv, slices, has_lo[keep]
 
 
 def facet_areas(problem) -> np.ndarray:

@@ -20,33 +20,43 @@ def _bf16(x):
     return (u.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
 
 
-def _host_q(prob, T, rounded):
-    """Q[s][f] = sum_g vf * eps sigma T[g][s]^4 (float64 accumulation)."""
+def _host_q(prob, T, rounded, min_entries=None):
+    """Q[s][f] = sum_g vf * eps sigma T[g][s]^4 (float64 accumulation).
+    With ``rounded``, the operands the FAST product uses: BF16 V (+ residual
+    in the tiles that carry one) times hi + lo BF16 W for the entries of
+    tensor-core tiles, and FP32 V times FP32 W for the sparse remainder."""
+    from binarytpm_gb300 import workloads
+
     es = np.float32(prob.emissivity) * SIGMA
     T2 = (T * T).astype(np.float32)
     W = (es * (T2 * T2)).astype(np.float32)          # [nf][ntau]
-    vf = prob.dep_vf
+    vf = prob.dep_vf.astype(np.float64)
     rows = np.repeat(np.arange(prob.nf), np.diff(prob.dep_ptr))
+    Wg = W[prob.dep_idx].astype(np.float64)
     if rounded:
         hi = _bf16(W)
         lo = _bf16((W - hi.astype(np.float32)).astype(np.float32))
-        W = hi + lo
-        # V_hi everywhere; V_lo added in the tiles that carry the residual
-        from binarytpm_gb300 import workloads
-
-        _, inv, _, has_lo = workloads.tc_tile_structure(prob.nf, prob.dep_ptr, prob.dep_idx, vf)
-        vhi = _bf16(vf)
-        vlo = _bf16((vf - vhi.astype(np.float32)).astype(np.float32))
-        vf = vhi + np.where(has_lo[inv], vlo, 0.0)
+        me = workloads.TC_MIN_ENTRIES if min_entries is None else min_entries
+        _, inv, _, has_lo = workloads.tc_tile_structure(prob.nf, prob.dep_ptr, prob.dep_idx, prob.dep_vf, me)
+        tile = inv >= 0
+        vhi = _bf16(prob.dep_vf)
+        vlo = _bf16((prob.dep_vf - vhi.astype(np.float32)).astype(np.float32))
+        lo_of_entry = has_lo[np.maximum(inv, 0)] & tile if len(has_lo) else np.zeros(len(inv), bool)
+        vt = vhi + np.where(lo_of_entry, vlo, 0.0)
+        vf = np.where(tile, vt, vf)
+        Wg = np.where(tile[:, None], (hi + lo)[prob.dep_idx], Wg)
     Q = np.zeros((prob.nf, T.shape[1]))
-    np.add.at(Q, rows, vf[:, None] * W[prob.dep_idx].astype(np.float64))
+    np.add.at(Q, rows, vf[:, None] * Wg)
     return Q.T
 
 
-@pytest.mark.parametrize("ntau", [48, 300, 720])
-def test_tensorcore_selfheating_matches_host(gpu_ctx, ntau):
+@pytest.mark.parametrize("ntau,min_entries", [(48, 64), (300, 64), (720, 64), (720, 1), (720, 8192)])
+def test_tensorcore_selfheating_matches_host(gpu_ctx, ntau, min_entries, monkeypatch):
+    """The default split, every cell a tile (threshold 1), and every entry in
+    the sparse remainder (threshold 8192: no cell of 128 x 64 can hold more)."""
     from binarytpm_gb300 import lib
 
+    monkeypatch.setenv("ATPM_TC_MIN_ENTRIES", str(min_entries))
     prob, ref = golden("binary_s3s1")
     prob = prob.with_(ntau=ntau)
     rng = np.random.default_rng(ntau)
@@ -59,7 +69,7 @@ def test_tensorcore_selfheating_matches_host(gpu_ctx, ntau):
     s.run()  # evolve so temperatures vary with facet and step
     T, _ = s.surface_temperature()
     q = s.selfheating_flux().astype(np.float64)
-    q_bf = _host_q(prob, T, rounded=True)
+    q_bf = _host_q(prob, T, rounded=True, min_entries=min_entries)
     q_ex = _host_q(prob, T, rounded=False)
     scale = np.abs(q_bf).max()
     assert scale > 1.0
