@@ -844,13 +844,21 @@ ATPM_API atpm_status atpm_context_create(int32_t device, atpm_context** out) {
     return ATPM_OK;
 }
 
-ATPM_API atpm_status atpm_context_destroy(atpm_context* c) {
-    if (!c) return ATPM_OK;
+extern "C++" void atpm_context_retain(atpm_context* c) {
+    if (c) c->refs.fetch_add(1, std::memory_order_relaxed);
+}
+
+extern "C++" void atpm_context_release(atpm_context* c) {
+    if (!c || c->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
     cudaSetDevice(c->device);
     if (c->p4.slots_dev) cudaFree(c->p4.slots_dev);
     if (c->p3.slots_dev) cudaFree(c->p3.slots_dev);
     if (c->pq.slots_dev) cudaFree(c->pq.slots_dev);
     delete c;
+}
+
+ATPM_API atpm_status atpm_context_destroy(atpm_context* c) {
+    atpm_context_release(c);  // freed now, or when its last solve, server or crater goes
     return ATPM_OK;
 }
 
@@ -917,6 +925,7 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     }
     auto* s = new atpm_solve();
     s->ctx = ctx;
+    atpm_context_retain(ctx);
     s->P = *P;
     s->nf = sh->nf;
     s->nv = sh->nv;
@@ -924,11 +933,11 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     s->rs = (P->precision == ATPM_FP64) ? 8 : 4;
     Layout L = layout(s->nv, s->nf, s->nnz, *P);
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) { atpm_context_release(s->ctx); delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
     e = cudaMalloc(&s->arena, L.total);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s->st);
-        delete s;
+        atpm_context_release(s->ctx); delete s;
         return fail(ATPM_E_NOMEM, "cudaMalloc(%zu): %s", L.total, cudaGetErrorString(e));
     }
     s->arena_bytes = L.total;
@@ -1006,7 +1015,9 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->qmap) cudaFree(s->qmap);
     if (s->arena) cudaFree(s->arena);
     if (s->st) cudaStreamDestroy(s->st);
+    atpm_context* ctx = s->ctx;
     delete s;
+    atpm_context_release(ctx);
     return ATPM_OK;
 }
 
@@ -1016,6 +1027,7 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
     CK(cudaStreamSynchronize(src->st));  // the source's state is complete
     auto* s = new atpm_solve();
     s->ctx = src->ctx;
+    atpm_context_retain(s->ctx);
     s->P = src->P;
     s->nf = src->nf; s->nv = src->nv; s->nnz = src->nnz; s->rs = src->rs;
     s->nw = src->nw; s->nfb = src->nfb; s->nq = src->nq;
@@ -1030,11 +1042,11 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
     s->ti = src->ti;
     s->ds = src->ds;  // scalars; device pointers rebased below
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) { atpm_context_release(s->ctx); delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
     e = cudaMalloc(&s->arena, src->arena_bytes);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s->st);
-        delete s;
+        atpm_context_release(s->ctx); delete s;
         return fail(ATPM_E_NOMEM, "cudaMalloc(%zu): %s", src->arena_bytes, cudaGetErrorString(e));
     }
     s->arena_bytes = src->arena_bytes;
@@ -1282,19 +1294,12 @@ struct LoopOut {
 // the revolution loop of one group on its leader's stream: the graph of one
 // revolution, replayed in chunks that double up to 32 revolutions, the
 // solves' control words read back after each chunk
-LoopOut revolution_loop(atpm_solve* const* solves, int n, const Batch& b, int maxcap, int done_revs,
-                        std::vector<Ctl>& ctl) {
+LoopOut revolution_loop(atpm_solve* const* solves, int n, const Batch& b, cudaGraphExec_t gx, int maxcap,
+                        int done_revs, std::vector<Ctl>& ctl) {
     LoopOut o;
     atpm_solve* lead = solves[0];
     if (cudaSetDevice(lead->ctx->device) != cudaSuccess) {
         o.st = fail(ATPM_E_CUDA, "cudaSetDevice");
-        o.err = g_err;
-        return o;
-    }
-    cudaGraphExec_t gx = nullptr;
-    atpm_status r = capture_graph(lead, b, &gx);
-    if (r) {
-        o.st = r;
         o.err = g_err;
         return o;
     }
@@ -1315,7 +1320,6 @@ LoopOut revolution_loop(atpm_solve* const* solves, int n, const Batch& b, int ma
         if (!any) break;
         chunk = std::min(chunk * 2, 32);
     }
-    cudaGraphExecDestroy(gx);
     if (e != cudaSuccess) {
         o.st = fail(ATPM_E_CUDA, "revolution loop: %s", cudaGetErrorString(e));
         o.err = g_err;
@@ -1385,15 +1389,28 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     std::vector<std::vector<Ctl>> ctl(ng);
     for (int g = 0; g < ng; ++g) ctl[g].resize(gs[g].size());
     std::vector<LoopOut> outs(ng);
+    // every group's revolution graph is captured here, on the calling
+    // thread, before any group's thread launches: no capture runs beside
+    // another thread's launches
+    std::vector<cudaGraphExec_t> gx(ng, nullptr);
+    auto free_graphs = [&]() {
+        for (cudaGraphExec_t x : gx)
+            if (x) cudaGraphExecDestroy(x);
+    };
+    for (int g = 0; g < ng; ++g) {
+        atpm_status rc = capture_graph(gs[g][0], bs[g], &gx[g]);
+        if (rc) { free_graphs(); free_tmps(); return rc; }
+    }
     {
         std::vector<std::thread> workers;
         for (int g = 1; g < ng; ++g)
             workers.emplace_back([&, g]() {
-                outs[g] = revolution_loop(gs[g].data(), (int)gs[g].size(), bs[g], maxcap[g], done[g], ctl[g]);
+                outs[g] = revolution_loop(gs[g].data(), (int)gs[g].size(), bs[g], gx[g], maxcap[g], done[g], ctl[g]);
             });
-        outs[0] = revolution_loop(gs[0].data(), (int)gs[0].size(), bs[0], maxcap[0], done[0], ctl[0]);
+        outs[0] = revolution_loop(gs[0].data(), (int)gs[0].size(), bs[0], gx[0], maxcap[0], done[0], ctl[0]);
         for (auto& w : workers) w.join();
     }
+    free_graphs();
     free_tmps();
     for (int g = 0; g < ng; ++g) {
         launches += outs[g].launches;

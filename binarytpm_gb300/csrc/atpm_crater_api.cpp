@@ -85,6 +85,7 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
     if (r) return r;
     auto* c = new atpm_crater();
     c->ctx = ctx;
+    atpm_context_retain(ctx);
     c->nf = nf;
     c->ntau = ntau;
     c->nx = nx;
@@ -102,6 +103,7 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
     if (e == cudaSuccess) e = cudaMalloc(&c->mem, total);
     if (e != cudaSuccess) {
         if (c->st) cudaStreamDestroy(c->st);
+        atpm_context_release(c->ctx);
         delete c;
         return cfail(ATPM_E_NOMEM, "allocation", e);
     }
@@ -147,7 +149,9 @@ ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c) {
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->mem) cudaFree(c->mem);
     if (c->st) cudaStreamDestroy(c->st);
+    atpm_context* ctx = c->ctx;
     delete c;
+    atpm_context_release(ctx);
     return ATPM_OK;
 }
 

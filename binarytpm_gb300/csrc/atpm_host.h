@@ -20,7 +20,12 @@ struct atpm_tune_choice {
     float tc_ms[2] = {0, 0};
 };
 
+// A context lives while its creator's handle or any solve, server or crater
+// made from it does: atpm_context_destroy drops the creator's reference and
+// the last object destroyed frees it, so destroy calls may come in any order
+// (a garbage collector's, at interpreter exit, for one).
 struct atpm_context {
+    std::atomic<int> refs{1};
     int device = 0;
     int sm_count = 1;
     std::mutex mu;
@@ -90,3 +95,7 @@ size_t batch_table_bytes(atpm_solve* const* solves, int n);
 atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st);
 atpm_status fail_status(atpm_status s, const char* msg);
 }  // namespace atpm
+
+// context references held by solves, servers and craters (atpm_capi.cpp)
+void atpm_context_retain(atpm_context* c);
+void atpm_context_release(atpm_context* c);

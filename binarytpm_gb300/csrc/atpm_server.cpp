@@ -271,6 +271,7 @@ ATPM_API atpm_status atpm_server_create(atpm_context* ctx, int32_t precision, in
         return atpm::fail_status(ATPM_E_INVALID, "server_create: bad arguments");
     auto* S = new atpm_server();
     S->ctx = ctx;
+    atpm_context_retain(ctx);
     S->precision = precision;
     S->nx = nx;
     S->budget = budget_bytes;
@@ -279,6 +280,7 @@ ATPM_API atpm_status atpm_server_create(atpm_context* ctx, int32_t precision, in
     cudaSetDevice(ctx->device);
     if (cudaStreamCreateWithFlags(&S->run_st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->setup_st, cudaStreamNonBlocking) != cudaSuccess) {
+        atpm_context_release(S->ctx);
         delete S;
         return atpm::fail_status(ATPM_E_CUDA, "server_create: stream creation failed");
     }
@@ -407,7 +409,9 @@ ATPM_API atpm_status atpm_server_destroy(atpm_server* S) {
     if (S->run_st) cudaStreamDestroy(S->run_st);
     if (S->setup_st) cudaStreamDestroy(S->setup_st);
     atpm_status st = S->loop_error;
+    atpm_context* ctx = S->ctx;
     delete S;
+    atpm_context_release(ctx);
     return st;
 }
 

@@ -535,6 +535,28 @@ def build_selfheating(nv: int, nf: int, shape: str, threads: int = 8) -> Path:
     return exe
 
 
+def build_selfheating_dropin(nv: int, nf: int, shape: str, lib_dir: Path, include_dir: Path, glue_dir: Path,
+                             threads: int = 8) -> Path:
+    """Shape_Selfheating with selfheating(A) (hidden + betterviewfactors
+    included) replaced by the drop-in glue
+    (binarytpm_gb300/driver/selfheating_dropin.inc) over libatpm; the
+    program's own main() and writers run unchanged."""
+    src_path = selfheating_source(nv, nf, shape)
+    d = src_path.parent
+    src = src_path.read_text()
+    i = src.find("void initialise(Asteroid &A) {")
+    if i < 0:
+        raise RuntimeError("initialise() not found in the scratch copy")
+    src = src[:i] + '#include "selfheating_dropin.inc"\n' + src[i:]
+    src = _replace_from(src, src.find("void initialise(Asteroid &A) {"), "\tselfheating(A);", "\tselfheating_atpm(A);")
+    drop = d / "main_dropin.cpp"
+    drop.write_text(src)
+    exe = d / ("selfheating_dropin_t%d" % threads)
+    subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % threads, "-I", str(include_dir), "-I", str(glue_dir),
+                    str(drop), "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir), "-o", str(exe)], check=True)
+    return exe
+
+
 SELFHEATING_OUTPUTS = ("_selfheating_list.txt", "_selfheating_vector_list.txt", "_photovectors.txt")
 
 
@@ -631,6 +653,37 @@ def build_visibility_shim(cfg: dict, lib_dir: Path, include_dir: Path, shim: Pat
     exe = src_path.parent / "visibility_shim"
     subprocess.run(["g++", *CXXFLAGS, *_vis_defines(cfg), "-I", str(include_dir), str(src_path), str(shim),
                     "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir), "-o", str(exe)], check=True)
+    return exe
+
+
+def build_visibility_dropin(cfg: dict, lib_dir: Path, include_dir: Path, glue_dir: Path) -> Path:
+    """The Visibility driver with its all-pairs shape visibility loop
+    (main.cpp:929-936) replaced by the drop-in glue
+    (binarytpm_gb300/driver/visibility_dropin.inc) over libatpm; the crater
+    visibility, when on, goes through the Visibility GPU module shim."""
+    import re
+
+    src_path = visibility_source(cfg)
+    d = src_path.parent
+    drop = d / "main_dropin.cpp"
+    src = src_path.read_text()
+    i = src.find("int main() {")
+    if i < 0:
+        raise RuntimeError("main() not found in the scratch copy")
+    src = src[:i] + '#include "visibility_dropin.inc"\n' + src[i:]
+    pat = re.compile(r"if \(shape_visibility_test==1\) \{\s*omp_set_num_threads\(num_threads\);\s*"
+                     r"#pragma omp parallel for schedule\(dynamic\)\s*for \(step=0;step<NTAU;step\+\+\) \{"
+                     r"\s*astshadow\(A,step\);[^\n]*\n[^\n]*\n\s*\}\n\s*\}")
+    src, n = pat.subn("if (shape_visibility_test==1) { shape_visibility_atpm(A, O); }", src, count=1)
+    if n != 1:
+        raise RuntimeError("shape visibility loop not found in the scratch copy")
+    drop.write_text(src)
+    exe = d / "visibility_dropin"
+    extra = [str(HERE.parent / "binarytpm_gb300" / "driver" / "atpm_ref_vis_gpu_shim.cpp")] \
+        if cfg.get("roughness") else [str(HERE / "ref_gpu_cpu.cpp")]
+    subprocess.run(["g++", *CXXFLAGS, *_vis_defines(cfg), "-I", str(include_dir), "-I", str(glue_dir), str(drop),
+                    *extra, "-L", str(lib_dir), "-latpm", "-Wl,-rpath," + str(lib_dir), "-o", str(exe)],
+                   check=True)
     return exe
 
 

@@ -156,9 +156,13 @@ def prepare_sources() -> None:
     """Write the scratch copies of the golden Thermal and Visibility
     configurations (so a host without the reference checkout can compile them)."""
     for name, c in CASES.items():
-        if c["kind"] == "visibility" and c.get("rough"):
+        if c["kind"] == "visibility":
             refbuild.visibility_source(visibility_cfg(name))
+        if c["kind"] == "visibility" and c.get("rough"):
             refbuild.visibility_gpu_module_source(visibility_cfg(name))
+        if c["kind"] in ("thermal", "visibility"):
+            v, f = case_mesh(c["mesh"])
+            refbuild.selfheating_source(len(v), len(f), "shape")
         if c["kind"] == "thermal":
             refbuild.thermal_source(thermal_cfg(name))
             if c.get("rough"):

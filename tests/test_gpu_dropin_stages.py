@@ -1,0 +1,111 @@
+"""The reference Visibility and Shape_Selfheating programs themselves, with
+their hot functions routed through the C ABI (binarytpm_gb300/driver/
+visibility_dropin.inc, selfheating_dropin.inc), against the same programs
+run unmodified on the CPU: the files their own writers produce.
+
+* Visibility: the all-pairs occultation flags toward the observer
+  (astshadow, 3905/Visibility/NominalPole/main.cpp:674-704), written by
+  writeglobalshadow (main.cpp:830-850): _visibility.txt byte for byte.
+* Shape_Selfheating: selfheating + hidden + betterviewfactors
+  (3905/Shape_Selfheating/main.cpp:628-744, 187-368, 374-622), written by
+  main() (main.cpp:837-888): the same index lists and counts; view factors,
+  direction vectors, photon vectors and total view factors at the files'
+  6 significant digits, a last-digit difference allowed in a few values
+  (the device's acosf/cosf are not glibc's).
+"""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT / "tests" / "golden"))
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_both(tmp_path, ref_exe, drop_exe, write_inputs):
+    out = {}
+    for tag, exe in (("ref", ref_exe), ("gpu", drop_exe)):
+        d = tmp_path / tag
+        d.mkdir()
+        write_inputs(d)
+        from oracle import refbuild
+
+        refbuild.run(exe, d)
+        out[tag] = d
+    return out["ref"], out["gpu"]
+
+
+def test_visibility_driver_through_c_abi(gpu_ctx, tmp_path):
+    import make_golden
+    from binarytpm_gb300 import build, mesh
+    from oracle import refbuild
+
+    prob, ref = golden("vis_s3s1")
+    lib = build.build()
+    cfg = make_golden.visibility_cfg("vis_s3s1")
+    ref_exe = refbuild.build_visibility(cfg)
+    drop_exe = refbuild.build_visibility_dropin(cfg, lib.parent, ROOT / "include", ROOT / "binarytpm_gb300" / "driver")
+    a, b = _run_both(tmp_path, ref_exe, drop_exe, lambda d: mesh.write_shape(d / "shape.txt", prob.vertices,
+                                                                             prob.facets))
+    want = (a / "shape_visibility.txt").read_bytes()
+    got = (b / "shape_visibility.txt").read_bytes()
+    assert got == want
+    # and the flags are the golden run's
+    from binarytpm_gb300 import formats
+
+    flags = formats.read_values_after_header(b / "shape_visibility.txt", prob.nv, prob.nf, np.int32)
+    assert np.array_equal(flags.reshape(prob.nf, prob.ntau), ref["visibility"])
+
+
+def _tokens(path):
+    return [line.split() for line in Path(path).read_text().splitlines()]
+
+
+def _close_tokens(ra, rb, rel=2e-5):
+    """Two text files of numbers: same shape, integers equal, floats equal
+    or within one unit of their 6th significant digit; returns the number of
+    float tokens that differ."""
+    assert len(ra) == len(rb)
+    diff = 0
+    for la, lb in zip(ra, rb):
+        assert len(la) == len(lb)
+        for x, y in zip(la, lb):
+            if x == y:
+                continue
+            fx, fy = float(x), float(y)
+            assert abs(fx - fy) <= rel * max(abs(fx), abs(fy)) + 1e-30, (x, y)
+            diff += 1
+    return diff
+
+
+def test_selfheating_program_through_c_abi(gpu_ctx, tmp_path):
+    import make_golden
+    from binarytpm_gb300 import build, mesh
+    from oracle import refbuild
+
+    v, f = make_golden.case_mesh(("binary", 3, 1))
+    lib = build.build()
+    ref_exe = refbuild.build_selfheating(len(v), len(f), "shape", threads=8)
+    drop_exe = refbuild.build_selfheating_dropin(len(v), len(f), "shape", lib.parent, ROOT / "include",
+                                                 ROOT / "binarytpm_gb300" / "driver")
+    a, b = _run_both(tmp_path, ref_exe, drop_exe, lambda d: mesh.write_shape(d / "shape.txt", v, f))
+    # vertices, facets and dependency counts: identical bytes
+    assert (b / "shape_selfheating_map.txt").read_bytes() == (a / "shape_selfheating_map.txt").read_bytes()
+    la, lb = _tokens(a / "shape_selfheating_list.txt"), _tokens(b / "shape_selfheating_list.txt")
+    nvals, ndiff = 0, 0
+    for ta, tb in zip(la, lb):
+        n = int(ta[0])
+        assert tb[:n + 1] == ta[:n + 1]  # count and indices
+        nvals += n
+    ndiff = _close_tokens(la, lb)
+    assert nvals > 10000 and ndiff <= 1e-3 * nvals, (ndiff, nvals)
+    for name in ("shape_selfheating_vector_list.txt", "shape_photovectors.txt", "shape_total_viewfactor_map.txt"):
+        ta, tb = _tokens(a / name), _tokens(b / name)
+        d = _close_tokens(ta, tb, rel=1e-4)
+        total = sum(len(x) for x in ta)
+        assert d <= 1e-2 * total, (name, d, total)
