@@ -106,3 +106,83 @@ def disk_flux(vertices, facets, ntau, pole, polar, observer, eps, temps, visibil
         inten = np.nan_to_num(inten, nan=0.0)
         out[s] = np.where(vis[:, None], inten * mult[:, None], 0.0).sum(axis=0)
     return out
+
+
+def crater_geometry(crater_vertices, crater_facets):
+    """The crater's sub-facet unit normals and areas, and its projected area
+    sum(area * n_z), in double from the float vertex positions the stage
+    reads from the roughness visibility file (wise_main.cpp:407-420 read,
+    464-490 surfacegeometry)."""
+    p = np.asarray(crater_vertices, np.float32).astype(np.float64)
+    fc = np.asarray(crater_facets)
+    a, b, c = p[fc[:, 0]], p[fc[:, 1]], p[fc[:, 2]]
+    n = _cross(b - a, c - a)
+    nn = _norm(n)
+    area = nn / 2.0
+    n = n / nn[:, None]
+    total = 0.0
+    for j in range(len(fc)):  # the stage's summation order
+        total = total + (area[j] * n[j, 2])
+    return n, area, total
+
+
+def rough_disk_flux(vertices, facets, ntau, pole, polar, observer, eps, sub_temps, sub_vis, crater_vertices,
+                    crater_facets, visibility, wavelengths_um):
+    """The rough-surface sum of observe (wise_main.cpp:695-727): for every
+    facet visible at a step, the crater sub-facets with a visible fraction
+    > 0 add B(T_sub) eps a_sub vis_sub cos(e_sub) / d^2 (e_sub from the view
+    vector in the facet frame and the sub-facet normal, wise_main.cpp:515),
+    and the facet's sum enters the disk total scaled by its area over the
+    crater's projected area.  sub_temps, sub_vis: [nf][nsf][ntau] (the
+    stage's file order).  Returns [ntau][nwl]."""
+    v = np.asarray(vertices, np.float64)
+    fc = np.asarray(facets)
+    tm = pole_matrix(pole)
+    car = centre(polar)
+    obs = car - centre(observer)
+    wl = np.asarray(wavelengths_um, np.float64) * 1.0e-6
+    b1 = (2.0 * HCON * CVEL * CVEL) / wl ** 5.0
+    lk = wl * KCON
+    hc = HCON * CVEL
+    sn, sa, stot = crater_geometry(crater_vertices, crater_facets)
+    ST = np.asarray(sub_temps, np.float32).astype(np.float64)
+    SV = np.asarray(sub_vis, np.float32).astype(np.float64)
+
+    def edges(step):
+        h = _vertices(v, tm, car, step, ntau)
+        h0, h1, h2 = h[fc[:, 0]], h[fc[:, 1]], h[fc[:, 2]]
+        return ((h0 + h1) + h2) / 3.0, h1 - h0, h2 - h0
+
+    _, e0, e1 = edges(ntau - 1)
+    area = _norm(_cross(e0, e1)) / 2.0
+    out = np.zeros((ntau, len(wl)))
+    for s in range(ntau):
+        hm, e0, e1 = edges(s)
+        n = _cross(e0, e1)
+        n = n / _norm(n)[:, None]
+        xh = e0 / _norm(e0)[:, None]
+        y = _cross(n, xh)
+        ov = hm - obs
+        o = _norm(ov)
+        vv = -np.stack([(xh * ov).sum(1), (y * ov).sum(1), (n * ov).sum(1)], axis=1)
+        va = np.arccos(vv[:, 2] / o)
+        vis = ~(va > math.pi / 2.0)
+        if visibility is not None:
+            vis &= np.asarray(visibility)[:, s] != 0
+        d = _norm(vv)
+        dots = ((vv[:, None, 0] * sn[None, :, 0] + vv[:, None, 1] * sn[None, :, 1]) + vv[:, None, 2] * sn[None, :, 2])
+        ca = np.cos(np.arccos(dots / d[:, None]))
+        T = ST[:, :, s]
+        vsub = SV[:, :, s]
+        with np.errstate(over="ignore", divide="ignore", invalid="ignore"):
+            mult = (eps * sa[None, :]) * vsub * ca / (d * d)[:, None]
+            mult = np.nan_to_num(mult, nan=0.0)
+            for li in range(len(wl)):
+                inten = b1[li] * (1.0 / (np.exp(hc / (lk[li] * T)) - 1.0))
+                inten = np.nan_to_num(inten, nan=0.0)
+                term = np.where(vsub > 0.0, inten * mult, 0.0)
+                sfc = np.zeros(len(fc))
+                for j in range(term.shape[1]):  # the stage's sub-facet order
+                    sfc = sfc + term[:, j]
+                out[s, li] = np.where(vis, sfc * area / stot, 0.0).sum()
+    return out

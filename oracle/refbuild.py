@@ -720,9 +720,12 @@ def build_visibility_refgpu(cfg: dict, cuda_home: str = "/usr/local/cuda") -> Pa
 
 _OBSERVE_HOOK = r'''
 #include <cstdio>
-static void __oracle_dump_flux(const double* smooth) {
+static void __oracle_dump_flux(const double* smooth, const double* rough) {
 	FILE* fp = fopen("oracle_flux.bin", "ab");
 	fwrite(smooth, sizeof(double), num_wavelengths, fp);
+	fclose(fp);
+	fp = fopen("oracle_rough_flux.bin", "ab");
+	fwrite(rough, sizeof(double), num_wavelengths, fp);
 	fclose(fp);
 }
 '''
@@ -751,13 +754,13 @@ def patch_observe(cfg: dict) -> str:
     src = src[:i] + _OBSERVE_HOOK + "\n" + src[i:]
     src = _insert_after(src, i, "\t\tchisqr_smooth=100.0, chisqr_rough=100.0;", "")
     j = src.find("\t\tchisqr_smooth=100.0, chisqr_rough=100.0;", i)
-    src = src[:j] + "\t\t__oracle_dump_flux(astsmoothfluxtotal);\n" + src[j:]
+    src = src[:j] + "\t\t__oracle_dump_flux(astsmoothfluxtotal, astroughfluxtotal);\n" + src[j:]
     return src
 
 
 def build_observe(cfg: dict) -> Path:
     """Reference Observe stage (disk-integrated flux), scratch copy."""
-    full = dict(shape="shape")
+    full = dict(shape="shape", hooks=2)  # hooks: the instrumentation's version (smooth + rough flux dumps)
     full.update(cfg)
     d = OUT_ROOT / _tag("observe", full)
     exe = d / "observe"

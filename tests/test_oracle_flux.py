@@ -40,3 +40,62 @@ def test_flux_restatement_matches_reference_observe(tmp_path, observer):
     scale = np.abs(want).max(axis=0, keepdims=True)
     assert np.all(scale > 0)
     assert np.all(np.abs(got - want) <= 1e-12 * scale), np.max(np.abs(got - want) / scale)
+
+
+def _crater_model():
+    """The crater (roughness) model the reference ships, carried in the crater
+    golden fixture: vertices [61][3], facets [100][3]."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden
+
+    _, ref = golden("rough_s1s1")
+    tok = make_golden.crater_texts_from(ref)["new_crater2.txt"].split()
+    cv = np.array(tok[:183], dtype=np.float64).reshape(61, 3)
+    cf = np.array(tok[183:483], dtype=np.int32).reshape(100, 3)
+    return cv, cf
+
+
+def _rough_file(path, cv, cf, per_facet):
+    """The stage's binary crater file: float crater vertices, int facets, then
+    [nf][nsf][ntau] floats (binary_writesfcroughshadow layout)."""
+    with open(path, "wb") as fh:
+        fh.write(np.asarray(cv, np.float32).tobytes())
+        fh.write(np.asarray(cf, np.int32).tobytes())
+        fh.write(np.ascontiguousarray(per_facet, np.float32).tobytes())
+
+
+def test_rough_flux_restatement_matches_reference_observe(tmp_path):
+    """The rough-surface sum of the Observe stage (observe,
+    3905/Observe/NominalPole/wise_main.cpp:695-727): seeded sub-facet
+    temperatures and visible fractions (some zero) in the stage's files."""
+    from binarytpm_gb300 import formats
+    from oracle import flux, refbuild
+
+    prob, ref = golden("single_s2")
+    nv, nf, ntau = prob.nv, prob.nf, prob.ntau
+    obs = (0.9, 0.1, 0.3)
+    ti = 200
+    v, f = prob.vertices, prob.facets
+    cv, cf = _crater_model()
+    rng = np.random.default_rng(7)
+    sub_t = rng.uniform(80.0, 400.0, (nf, 100, ntau)).astype(np.float32)
+    sub_v = np.where(rng.random((nf, 100, ntau)) < 0.3, 0.0, rng.integers(1, 101, (nf, 100, ntau)) / 100.0)
+    sub_v = sub_v.astype(np.float32)
+    flags = (rng.random((nf, ntau)) < 0.9).astype(np.int32)
+    formats.write_shadow(tmp_path / "shape_visibility.txt", v, f, flags)
+    formats.write_temperature(tmp_path / ("shape_temperature(%d).txt" % ti), v, f, ref["stemp1"])
+    _rough_file(tmp_path / "shape_roughness_visibility.dat", cv, cf, sub_v)
+    _rough_file(tmp_path / ("shape_roughness_temperature(%d).dat" % ti), cv, cf, sub_t)
+    (tmp_path / "wise_colour_corrections.txt").write_text("1\t1\t1\n" * 467)
+    exe = refbuild.build_observe(dict(nv=nv, nf=nf, ntau=ntau, polar=prob.polar, observer=obs, rot=prob.pole, ti=ti))
+    refbuild.run(exe, tmp_path)
+    got = np.fromfile(tmp_path / "oracle_rough_flux.bin", dtype=np.float64).reshape(ntau, 3)
+    raw = (tmp_path / "shape_visibility.txt").read_text().split()
+    vv = np.array(raw[:3 * nv], dtype=np.float64).reshape(nv, 3)
+    want = flux.rough_disk_flux(vv, f, ntau, prob.pole, prob.polar, obs, 0.9, sub_t, sub_v, cv, cf, flags, WL)
+    scale = np.abs(want).max(axis=0, keepdims=True)
+    assert np.all(scale > 0)
+    assert np.all(np.abs(got - want) <= 1e-12 * scale), np.max(np.abs(got - want) / scale)
