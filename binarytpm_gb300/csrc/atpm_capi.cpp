@@ -1613,15 +1613,23 @@ ATPM_API atpm_status atpm_set_position(atpm_solve* s, const double* car_km) {
     return ATPM_OK;
 }
 
-ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
-                                    double emissivity, int32_t nwl, const double* wavelength_um, double* flux) {
+namespace {
+// smooth (rough == null) or rough disk-integrated flux of a solve
+atpm_status disk_flux_impl(atpm_solve* s, const double* observer, const int32_t* visibility, double emissivity,
+                           int32_t nwl, const double* wavelength_um, double* flux, const FluxArgs* rough) {
     if (!s || !observer || !wavelength_um || !flux || nwl < 1 || nwl > kMaxFluxWavelengths)
         return fail(ATPM_E_INVALID, "disk_flux: bad arguments (1 <= nwl <= %d)", kMaxFluxWavelengths);
-    if (!s->have_temps && s->ti != 0.0f) return fail(ATPM_E_STATE, "disk_flux: no temperatures yet");
+    if (!rough && !s->have_temps && s->ti != 0.0f) return fail(ATPM_E_STATE, "disk_flux: no temperatures yet");
     CK(cudaSetDevice(s->ctx->device));
     const atpm_params& P = s->P;
     const int nf = s->nf, ntau = P.ntau;
     FluxArgs a{};
+    if (rough) {
+        a.sub_T = rough->sub_T;
+        a.sub_vis = rough->sub_vis;
+        a.nsf = rough->nsf;
+        a.sub_total = rough->sub_total;
+    }
     std::vector<double> rot, rot2;
     geometry_tables(P, a.tm, a.car, rot, s->revs_p);
     geometry_tables(P, a.tm, a.car, rot2, s->revs_s);
@@ -1651,18 +1659,22 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
         for (size_t i = 0; i < vis.size(); ++i) vis[i] = visibility[i] ? 1 : 0;
     }
     const size_t b_rot = align256(rot.size() * 8), b_part = align256(flux_partial_bytes(s->ds, nwl)),
-                 b_out = align256((size_t)ntau * nwl * 8), b_vis = align256(vis.size());
+                 b_out = align256((size_t)ntau * nwl * 8), b_vis = align256(vis.size()),
+                 b_geo = rough ? align256((size_t)rough->nsf * 4 * 8) : 0;
     void* tmp = nullptr;
-    CK(cudaMallocAsync(&tmp, b_rot + b_part + b_out + b_vis, s->st));
+    CK(cudaMallocAsync(&tmp, b_rot + b_part + b_out + b_vis + b_geo, s->st));
     char* t = static_cast<char*>(tmp);
     a.rot = reinterpret_cast<const double*>(t);
     a.rot2 = a.rot + 2 * (size_t)ntau;
     a.partial = reinterpret_cast<double*>(t + b_rot);
     a.out = reinterpret_cast<double*>(t + b_rot + b_part);
     a.visible = visibility ? reinterpret_cast<const uint8_t*>(t + b_rot + b_part + b_out) : nullptr;
+    if (rough) a.sub_geo = reinterpret_cast<const double*>(t + b_rot + b_part + b_out + b_vis);
     cudaError_t e = cudaMemcpyAsync((void*)a.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess && visibility)
         e = cudaMemcpyAsync((void*)a.visible, vis.data(), vis.size(), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess && rough)
+        e = cudaMemcpyAsync((void*)a.sub_geo, rough->sub_geo, (size_t)rough->nsf * 4 * 8, cudaMemcpyHostToDevice, s->st);
     int rc = 0;
     if (e == cudaSuccess) rc = launch_disk_flux(s->ds, a, s->st);
     if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(flux, a.out, (size_t)ntau * nwl * 8, cudaMemcpyDeviceToHost, s->st);
@@ -1672,6 +1684,62 @@ ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const
     if (rc) return fail(ATPM_E_CUDA, "disk_flux launch: %s", cudaGetErrorString(cudaGetLastError()));
     if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "disk_flux: %s", cudaGetErrorString(e2));
     return ATPM_OK;
+}
+}  // namespace
+
+ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
+                                    double emissivity, int32_t nwl, const double* wavelength_um, double* flux) {
+    return disk_flux_impl(s, observer, visibility, emissivity, nwl, wavelength_um, flux, nullptr);
+}
+
+ATPM_API atpm_status atpm_disk_flux_rough(atpm_solve* s, const atpm_crater* temperatures,
+                                          const atpm_crater* sub_visibility, int32_t nsv, const float* crater_vertices,
+                                          const int32_t* crater_facets, const double* observer,
+                                          const int32_t* visibility, double emissivity, int32_t nwl,
+                                          const double* wavelength_um, double* flux) {
+    if (!s || !temperatures || !sub_visibility || !crater_vertices || !crater_facets || nsv < 3)
+        return fail(ATPM_E_INVALID, "disk_flux_rough: bad arguments");
+    const CraterDev& ct = atpm_crater_device(temperatures);
+    const CraterDev& cv = atpm_crater_device(sub_visibility);
+    if (!ct.stemp1) return fail(ATPM_E_STATE, "disk_flux_rough: the temperature crater holds no temperatures");
+    if (!cv.sfc_shadow) return fail(ATPM_E_STATE, "disk_flux_rough: the visibility crater holds no sub-facet array");
+    if (ct.nf != s->nf || cv.nf != s->nf || ct.ntau != s->P.ntau || cv.ntau != s->P.ntau || ct.nsf != cv.nsf)
+        return fail(ATPM_E_INVALID, "disk_flux_rough: craters and solve differ in facets, steps or sub-facets");
+    const int nsf = ct.nsf;
+    for (int i = 0; i < 3 * nsf; ++i)
+        if (crater_facets[i] < 0 || crater_facets[i] >= nsv)
+            return fail(ATPM_E_INVALID, "disk_flux_rough: crater facet vertex %d out of range", crater_facets[i]);
+    // the crater's sub-facet normals and areas in double from its float
+    // vertices, as the stage computes them (wise_main.cpp:464-490)
+    std::vector<double> geo(4 * (size_t)nsf);
+    double total = 0.0;
+    for (int j = 0; j < nsf; ++j) {
+        const float* p0 = crater_vertices + 3 * crater_facets[3 * j];
+        const float* p1 = crater_vertices + 3 * crater_facets[3 * j + 1];
+        const float* p2 = crater_vertices + 3 * crater_facets[3 * j + 2];
+        double a[3], b[3], n[3];
+        for (int k = 0; k < 3; ++k) {
+            a[k] = (double)p1[k] - (double)p0[k];
+            b[k] = (double)p2[k] - (double)p0[k];
+        }
+        n[0] = (a[1] * b[2]) - (a[2] * b[1]);
+        n[1] = (a[2] * b[0]) - (a[0] * b[2]);
+        n[2] = (a[0] * b[1]) - (a[1] * b[0]);
+        const double nn = std::sqrt((n[0] * n[0]) + (n[1] * n[1]) + (n[2] * n[2]));
+        const double area = nn / 2.0;
+        for (int k = 0; k < 3; ++k) geo[4 * j + k] = n[k] / nn;
+        geo[4 * j + 3] = area;
+        total = total + (area * geo[4 * j + 2]);
+    }
+    CK(atpm_crater_sync(temperatures));
+    CK(atpm_crater_sync(sub_visibility));
+    FluxArgs r{};
+    r.sub_T = ct.stemp1;
+    r.sub_vis = cv.sfc_shadow;
+    r.sub_geo = geo.data();  // host copy, uploaded with the call's tables
+    r.nsf = nsf;
+    r.sub_total = total;
+    return disk_flux_impl(s, observer, visibility, emissivity, nwl, wavelength_um, flux, &r);
 }
 
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted, double* mean_t) {

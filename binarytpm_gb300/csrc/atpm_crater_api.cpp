@@ -62,6 +62,12 @@ atpm_status launch(atpm_crater* c, int what, std::initializer_list<float> f, voi
 }
 }  // namespace
 
+const CraterDev& atpm_crater_device(const atpm_crater* c) { return c->d; }
+cudaError_t atpm_crater_sync(const atpm_crater* c) {
+    cudaError_t e = cudaSetDevice(c->ctx->device);
+    return e == cudaSuccess ? cudaStreamSynchronize(c->st) : e;
+}
+
 namespace atpm {
 atpm_status ensure_pow_tables(atpm_context* c);
 atpm_status ensure_pow_tables_qroot(atpm_context* c);

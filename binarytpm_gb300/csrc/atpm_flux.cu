@@ -17,6 +17,11 @@
 //                   shared-memory tree sums each 256-facet block
 //   k_flux_sum      sums the block partials of every (step, wavelength) in
 //                   block order: the result does not depend on scheduling
+//
+// The rough-surface sum (observe, wise_main.cpp:695-727) replaces each
+// facet's own term by its crater's: the sub-facets with a visible fraction
+// toward the observer > 0 add B(T_sub) eps a_sub vis cos(e_sub) / d^2, and
+// the facet's total enters scaled by A_f over the crater's projected area.
 #include <cuda_runtime.h>
 
 #include "atpm_internal.h"
@@ -71,7 +76,7 @@ __device__ __forceinline__ double norm3(const double* v) {
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
 }
 
-template <class R>
+template <class R, bool ROUGH>
 __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(DevSolve s, FluxArgs a) {
     __shared__ double red[kFluxThreads];
     const int step = blockIdx.y;
@@ -106,15 +111,44 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(DevSolve s, FluxA
         const double va = acos(__ddiv_rn(v2, o));
         if (!(va > (3.141592653589793 / 2.0))) {
             const double d = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v0, v0), __dmul_rn(v1, v1)), __dmul_rn(v2, v2)));
-            double mult = __ddiv_rn(__dmul_rn(__dmul_rn(a.eps, area), cos(va)), __dmul_rn(d, d));
-            if (mult != mult) mult = 0.0;
-            const double T = temp_at<R>(s, f, step);
-            for (int l = 0; l < a.nwl; ++l) {
-                // (2hc^2 / lambda^5) * (1 / (exp(hc / (lambda k T)) - 1))
-                const double arg = __ddiv_rn(a.hc, __dmul_rn(a.lk[l], T));
-                double b = __dmul_rn(a.b1[l], __ddiv_rn(1.0, __dsub_rn(exp(arg), 1.0)));
-                if (b != b) b = 0.0;
-                term[l] = __dmul_rn(b, mult);
+            if constexpr (!ROUGH) {
+                double mult = __ddiv_rn(__dmul_rn(__dmul_rn(a.eps, area), cos(va)), __dmul_rn(d, d));
+                if (mult != mult) mult = 0.0;
+                const double T = temp_at<R>(s, f, step);
+                for (int l = 0; l < a.nwl; ++l) {
+                    // (2hc^2 / lambda^5) * (1 / (exp(hc / (lambda k T)) - 1))
+                    const double arg = __ddiv_rn(a.hc, __dmul_rn(a.lk[l], T));
+                    double b = __dmul_rn(a.b1[l], __ddiv_rn(1.0, __dsub_rn(exp(arg), 1.0)));
+                    if (b != b) b = 0.0;
+                    term[l] = __dmul_rn(b, mult);
+                }
+            } else {
+                // the facet's crater: every sub-facet with a visible fraction
+                // > 0, its view angle from the view vector in the facet frame
+                // (wise_main.cpp:515), in sub-facet order; then the facet's
+                // share of the crater's projected area (wise_main.cpp:718)
+                const size_t base = ((size_t)f * s.ntau + step) * (size_t)a.nsf;
+                double sfc[kMaxFluxWavelengths];
+#pragma unroll
+                for (int l = 0; l < kMaxFluxWavelengths; ++l) sfc[l] = 0.0;
+                const double dd = __dmul_rn(d, d);
+                for (int j = 0; j < a.nsf; ++j) {
+                    const double vis = (double)a.sub_vis[base + j];
+                    if (!(vis > 0.0)) continue;
+                    const double* g = a.sub_geo + 4 * j;
+                    const double c = __dadd_rn(__dadd_rn(__dmul_rn(v0, g[0]), __dmul_rn(v1, g[1])), __dmul_rn(v2, g[2]));
+                    const double vj = acos(__ddiv_rn(c, d));
+                    double mult = __ddiv_rn(__dmul_rn(__dmul_rn(__dmul_rn(a.eps, g[3]), vis), cos(vj)), dd);
+                    if (mult != mult) mult = 0.0;
+                    const double T = (double)a.sub_T[base + j];
+                    for (int l = 0; l < a.nwl; ++l) {
+                        const double arg = __ddiv_rn(a.hc, __dmul_rn(a.lk[l], T));
+                        double b = __dmul_rn(a.b1[l], __ddiv_rn(1.0, __dsub_rn(exp(arg), 1.0)));
+                        if (b != b) b = 0.0;
+                        sfc[l] = __dadd_rn(sfc[l], __dmul_rn(b, mult));
+                    }
+                }
+                for (int l = 0; l < a.nwl; ++l) term[l] = __ddiv_rn(__dmul_rn(sfc[l], area), a.sub_total);
             }
         }
     }
@@ -151,8 +185,13 @@ int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t stv) {
     if (a.nwl < 1 || a.nwl > kMaxFluxWavelengths) return 1;
     const int nblk = (s.nf + kFluxThreads - 1) / kFluxThreads;
     const dim3 grid(nblk, s.ntau);
-    if (s.mode == MODE_FP64) k_flux_partial<double><<<grid, kFluxThreads, 0, st>>>(s, a);
-    else k_flux_partial<float><<<grid, kFluxThreads, 0, st>>>(s, a);
+    if (a.sub_T) {
+        if (s.mode == MODE_FP64) k_flux_partial<double, true><<<grid, kFluxThreads, 0, st>>>(s, a);
+        else k_flux_partial<float, true><<<grid, kFluxThreads, 0, st>>>(s, a);
+    } else {
+        if (s.mode == MODE_FP64) k_flux_partial<double, false><<<grid, kFluxThreads, 0, st>>>(s, a);
+        else k_flux_partial<float, false><<<grid, kFluxThreads, 0, st>>>(s, a);
+    }
     k_flux_sum<<<(s.ntau * a.nwl + 127) / 128, 128, 0, st>>>(a, s.ntau, nblk);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

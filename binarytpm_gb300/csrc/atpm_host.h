@@ -96,6 +96,10 @@ atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cud
 atpm_status fail_status(atpm_status s, const char* msg);
 }  // namespace atpm
 
+// a crater's device arrays and a wait for its queued work (atpm_crater_api.cpp)
+const atpm::CraterDev& atpm_crater_device(const atpm_crater* c);
+cudaError_t atpm_crater_sync(const atpm_crater* c);
+
 // context references held by solves, servers and craters (atpm_capi.cpp)
 void atpm_context_retain(atpm_context* c);
 void atpm_context_release(atpm_context* c);

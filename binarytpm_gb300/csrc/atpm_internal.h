@@ -268,6 +268,12 @@ struct FluxArgs {
     double hc;                       // h * c
     double* partial;         // [ntau][blocks][nwl]
     double* out;             // [ntau][nwl]
+    // rough surface (crater sub-facets); null for the smooth-surface sum
+    const float* sub_T;      // [nf][ntau][nsf] sub-facet surface temperatures
+    const float* sub_vis;    // [nf][ntau][nsf] visible fraction toward the observer
+    const double* sub_geo;   // [nsf][4] unit normal, area
+    int nsf;
+    double sub_total;        // sum over sub-facets of area * normal_z
 };
 size_t flux_partial_bytes(const DevSolve& s, int nwl);
 int launch_disk_flux(const DevSolve& s, const FluxArgs& a, stream_t st);

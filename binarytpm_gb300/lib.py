@@ -112,6 +112,10 @@ _SIGS = {
     "atpm_crater_inst_equilibrium": (C.c_int, [C.c_void_p, C.c_float, C.c_float]),
     "atpm_crater_converged": (C.c_int, [C.c_void_p, C.c_float]),
     "atpm_crater_get_temperatures": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "atpm_crater_set_array_strided": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64]),
+    "atpm_crater_get_array_strided": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64]),
+    "atpm_disk_flux_rough": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -387,6 +391,21 @@ class Solve:
         _ck(load().atpm_disk_flux(self.h, _p(ob), _p(vis), float(emissivity), len(wl), _p(wl), _p(out)))
         return out
 
+    def disk_flux_rough(self, temperatures: "Crater", sub_visibility: "Crater", crater_vertices, crater_facets,
+                        observer, wavelengths_um=(12.0,), visibility=None, emissivity=0.9):
+        """[ntau][nwl] FP64 rough-surface flux (atpm_disk_flux_rough): the
+        sub-facet temperatures of ``temperatures``, the visible fractions in
+        ``sub_visibility``'s sub-facet shadow array."""
+        cv = np.ascontiguousarray(crater_vertices, np.float32)
+        cf = np.ascontiguousarray(crater_facets, np.int32)
+        ob = np.ascontiguousarray(observer, np.float64)
+        wl = np.ascontiguousarray(wavelengths_um, np.float64)
+        vis = None if visibility is None else np.ascontiguousarray(visibility, np.int32)
+        out = np.zeros((self.ntau, len(wl)), np.float64)
+        _ck(load().atpm_disk_flux_rough(self.h, temperatures.h, sub_visibility.h, len(cv), _p(cv), _p(cf), _p(ob),
+                                        _p(vis), float(emissivity), len(wl), _p(wl), _p(out)))
+        return out
+
     def energy_balance(self):
         a, e, m = C.c_double(), C.c_double(), C.c_double()
         _ck(load().atpm_energy_balance(self.h, C.byref(a), C.byref(e), C.byref(m)))
@@ -578,6 +597,18 @@ class Crater:
         out = np.zeros(shape, dt)
         _ck(load().atpm_crater_get_array(self.h, which, _p(out)))
         return out
+
+    # strided-transfer slots of the temperature arrays ([nf][ntau][nsf], depth [nf][nx+1][nsf])
+    STEMP0, STEMP1, DEPTH = 7, 8, 9
+
+    def set_temperatures(self, stemp1, stemp0=None):
+        """Sub-facet surface temperatures [nf][ntau][nsf] (and the previous
+        revolution's) into the crater's state."""
+        for which, a in ((self.STEMP1, stemp1), (self.STEMP0, stemp0)):
+            if a is None:
+                continue
+            a = np.ascontiguousarray(np.asarray(a, np.float32).reshape(self.nf, self.ntau, self.nsf))
+            _ck(load().atpm_crater_set_array_strided(self.h, which, _p(a), self.ntau * self.nsf * 4))
 
     def partial_shadow(self):
         _ck(load().atpm_crater_partial_shadow(self.h))

@@ -202,3 +202,10 @@ def disk_flux(problem, stemp1: np.ndarray, cosillum: np.ndarray, shadow: np.ndar
     vis = (shadow > 0) & (cosillum > 0)
     w = np.where(vis, A * cosillum.astype(np.float64), 0.0) * problem.emissivity
     return (w * planck(wavelength_um, stemp1.astype(np.float64))).sum(axis=0)
+
+
+def roughness_mix(smooth, rough, fraction):
+    """The fitting's model flux for a surface covered by craters over the
+    given fraction of its area: fraction * rough + (1 - fraction) * smooth
+    (175706/Run-04/fitting.cpp:460-461), per step and wavelength."""
+    return fraction * np.asarray(rough) + (1.0 - fraction) * np.asarray(smooth)

@@ -90,6 +90,7 @@ typedef struct atpm_params {
 
 typedef struct atpm_context atpm_context;
 typedef struct atpm_solve atpm_solve;
+typedef struct atpm_crater atpm_crater;  /* crater (surface roughness) module, below */
 
 ATPM_API const char* atpm_status_string(atpm_status s);
 ATPM_API const char* atpm_last_error(void);
@@ -211,6 +212,26 @@ ATPM_API atpm_status atpm_set_position(atpm_solve* s, const double* car_km);
  * (deterministic). */
 ATPM_API atpm_status atpm_disk_flux(atpm_solve* s, const double* observer, const int32_t* visibility,
                                     double emissivity, int32_t nwl, const double* wavelength_um, double* flux);
+/* The rough-surface sum of the same stage (observe, wise_main.cpp:695-727),
+ * FP64 on the device, for the fitting's roughness mix R * rough +
+ * (1 - R) * smooth (175706/Run-04/fitting.cpp:460-461): every facet visible
+ * at a step contributes its crater's sub-facets with a visible fraction > 0,
+ * B(T_sub) * eps * a_sub * vis_sub * cos(e_sub) / d^2, the facet's total
+ * scaled by its area over the crater's projected area sum(a_sub * n_sub,z).
+ * temperatures: a crater (atpm_crater_create with nx > 0) holding the
+ * sub-facet surface temperatures of this solve's facets (its stemp1);
+ * sub_visibility: a crater whose sub-facet shadow array (set/get_array 1)
+ * holds each sub-facet's visible fraction toward the observer (the
+ * Visibility stage's crater output: a crater shadow run with the observer
+ * as the light source); crater_vertices [nsv][3] float and crater_facets
+ * [nsf][3]: the crater model as the stage reads it from the roughness
+ * visibility file.  Other arguments as atpm_disk_flux; flux [ntau][nwl].
+ * The stage computes this sum in the loop of atpm_disk_flux's. */
+ATPM_API atpm_status atpm_disk_flux_rough(atpm_solve* s, const atpm_crater* temperatures,
+                                          const atpm_crater* sub_visibility, int32_t nsv, const float* crater_vertices,
+                                          const int32_t* crater_facets, const double* observer,
+                                          const int32_t* visibility, double emissivity, int32_t nwl,
+                                          const double* wavelength_um, double* flux);
 /* FP64 diagnostics of the last revolution: sum over facets and steps of the
  * absorbed flux, emitted flux and the mean surface temperature. */
 ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double* emitted,
@@ -258,7 +279,6 @@ ATPM_API atpm_status atpm_viewfactors_free(atpm_vf_result* r);
  * sub-facets (100 for the shipped crater).  REFERENCE precision follows the
  * module's float expressions operand by operand (no contraction, this host's
  * libm powf), FAST contracts. */
-typedef struct atpm_crater atpm_crater;
 /* initialise_GPU_*_arrays (GPU_code.cu:696-768).  nx = 0 creates a
  * shadow-only crater (the Visibility stage's module,
  * 3905/Visibility/NominalPole/GPU_code.cu:146-283): only the shadow arrays
