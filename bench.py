@@ -298,6 +298,50 @@ def precision_stress(p_subdiv: int):
                       "viewfactor_s": vf_s, "comparison_s": time.perf_counter() - t1}), flush=True)
 
 
+# exact ray-triangle test (astshadowtest, 3905/Thermal/NominalPole/main.cpp:1187-1247):
+# FP64 operations executed per test (a plane intersection, three edge cross
+# products and their projections on the normal)
+SHADOW_TEST_FLOP = 74
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
+
+
+def visibility(ctx):
+    """The Visibility stage's all-pairs occultation toward an observer
+    (astshadow, 3905/Visibility/NominalPole/main.cpp:674-704) at 720 steps,
+    REFERENCE precision (FP64 tests, the reference's flags): the 21,760-facet
+    binary and the 87,040-facet precision-stress system.  rays = facet x step
+    queries; exact tests = ray-triangle tests run after the box cull."""
+    from binarytpm_gb300 import lib, mesh, problem as P
+
+    out = {}
+    prim = mesh.grf_body(6, 0.39, 0.15, 0.3, 3)
+    sec = mesh.perturbed_body(4, 0.08, 0.08, 1003)
+    sv, sf = mesh.binary_system(prim, sec, 1.19)
+    bv, bf = P.binary_mesh(5, 3, 2)
+    for name, (v, f) in (("binary_21760", (bv, bf)), ("stress_87040", (sv, sf))):
+        ptr, idx, vf = P.empty_lists(len(f))
+        prob = P.Problem(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf, ntau=720,
+                         nx=56, polar=(1.2, 0.1, 0.3), pole=P.BINARY_POLE, shadowing=2)
+        s = lib.Solve(ctx, prob, precision=lib.REFERENCE)
+        best = None
+        for _ in range(3):
+            s.geometry_shadow()
+            st = s.last_shadow_stats()
+            if best is None or st[0] < best[0]:
+                best = st
+        s.close()
+        ms, rays, tests = best
+        sec_ = ms / 1e3
+        out[name] = {"facets": len(f), "steps": 720, "shadow_ms": ms, "rays_per_s": rays / sec_,
+                     "exact_tests_per_s": tests / sec_, "exact_tests_per_ray": tests / rays,
+                     "fp64_tflops": tests * SHADOW_TEST_FLOP / sec_ / 1e12,
+                     "fp64_frac_of_nominal": tests * SHADOW_TEST_FLOP / sec_ / 1e12 / FP64_NOMINAL_TFLOPS,
+                     "all_pairs": len(f) * (len(f) - 1) // 2 * 720}
+    out["note"] = ("exact tests are FP64 in the reference's operand order (bit-identical flags); "
+                   f"{SHADOW_TEST_FLOP} FP64 operations per test against the nominal FP64 rate; best of 3")
+    return out
+
+
 def run_reference_arm(args, world, rank):
     """The reference's own CPU implementation of the timed workload on this
     host's cores.  Nothing of this repository's library is loaded: the
@@ -367,6 +411,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU reference timing")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-visibility", action="store_true", help="skip the all-pairs visibility measurement")
     ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving run (1/s)")
@@ -475,6 +520,7 @@ def main():
     e2e = e2e_run(ctx, prob, tis, max(1, min(args.steps, 3)))  # median of up to 3 jobs
 
     serve = serving(ctx, args.serve_requests, args.serve_rate) if args.serve_requests > 0 else None
+    vis = None if args.no_visibility else visibility(ctx)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -503,6 +549,7 @@ def main():
                         "what": f"serving: submit to result, Poisson arrivals {serve['arrival_rate_per_s']}/s, "
                                 f"{serve['requests']} requests"} if serve else None),
         "serving": serve,
+        "visibility": vis,
         "energy_balance_fp64": energy,
         "kernels_ms": kern,
         "launch_config": launch_config,

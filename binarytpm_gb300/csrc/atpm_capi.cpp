@@ -1113,10 +1113,12 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
         for (int k = 0; k < 3; ++k) g.car[k] = s->position[k];
     const size_t nt = (size_t)s->nf * ntau;
     const size_t bytes = align256((size_t)s->nv * ntau * 24) + align256(nt * 24) * 2 + align256(nt * 8) +
-                         align256((size_t)ntau * 32);
+                         align256((size_t)ntau * 32) + 64 * 8;
     void* tmp = nullptr;
     CK(cudaMallocAsync(&tmp, bytes, s->st));
     char* t = static_cast<char*>(tmp);
+    g.tests = reinterpret_cast<unsigned long long*>(t + bytes - 64 * 8);
+    CK(cudaMemsetAsync(g.tests, 0, 64 * 8, s->st));
     g.hp = reinterpret_cast<double*>(t);
     t += align256((size_t)s->nv * ntau * 24);
     g.hm = reinterpret_cast<double*>(t);
@@ -1133,14 +1135,37 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     // shadow drivers: the projected-box cull in front of the exact test (the
     // same flags); ATPM_SHADOW_CULL=0 runs the plain drivers
     const bool shadows = (P.shadowing == 1 && s->nnz > 0) || P.shadowing == 2;
+    // the shadow drivers' time (events) and exact-test count (culled drivers)
+    cudaEvent_t sh0 = nullptr, sh1 = nullptr;
+    unsigned long long counts[64] = {};
+    bool culled = false;
     if (e == cudaSuccess && !rc && shadows) {
+        if (cudaEventCreate(&sh0) == cudaSuccess && cudaEventCreate(&sh1) == cudaSuccess)
+            cudaEventRecord(sh0, s->st);
         int cr = shadow_cull_enabled() ? launch_shadow_culled(s->ds, g, P.shadowing == 2, s->st) : -1;
+        culled = cr != -1;
         if (cr == -1) cr = (P.shadowing == 2) ? launch_shadow_allpairs(s->ds, g, s->st)
                                               : launch_shadow_deplist(s->ds, g, s->st);
         rc = cr;
+        if (sh1) cudaEventRecord(sh1, s->st);
+        if (!rc) e = cudaMemcpyAsync(counts, g.tests, sizeof counts, cudaMemcpyDeviceToHost, s->st);
     }
     cudaFreeAsync(tmp, s->st);
     cudaError_t e2 = cudaStreamSynchronize(s->st);  // `rot` must outlive the copy
+    s->last_shadow_ms = 0.0;
+    s->last_shadow_rays = shadows ? (int64_t)nt : 0;
+    s->last_shadow_tests = -1;  // not counted by the plain drivers
+    if (sh0 && sh1 && e2 == cudaSuccess && !rc) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, sh0, sh1) == cudaSuccess) s->last_shadow_ms = ms;
+        if (culled) {
+            unsigned long long tot = 0;
+            for (unsigned long long c : counts) tot += c;
+            s->last_shadow_tests = (int64_t)tot;
+        }
+    }
+    if (sh0) cudaEventDestroy(sh0);
+    if (sh1) cudaEventDestroy(sh1);
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "geometry upload: %s", cudaGetErrorString(e));
     if (rc) return fail(ATPM_E_CUDA, "geometry launch: %s", cudaGetErrorString(cudaGetLastError()));
     if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "geometry: %s", cudaGetErrorString(e2));
@@ -1771,6 +1796,14 @@ ATPM_API atpm_status atpm_selftest_bounded_wait(int32_t device, int64_t limit_cy
     if (status_bits) *status_bits = h;
     if (h & ST_TC_TIMEOUT) return fail(ATPM_E_ITERATION, "bounded wait gave up after %lld cycles",
                                        (long long)limit_cycles);
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_last_shadow_stats(atpm_solve* s, double* shadow_ms, int64_t* rays, int64_t* exact_tests) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (shadow_ms) *shadow_ms = s->last_shadow_ms;
+    if (rays) *rays = s->last_shadow_rays;
+    if (exact_tests) *exact_tests = s->last_shadow_tests;
     return ATPM_OK;
 }
 

@@ -249,6 +249,17 @@ __device__ __forceinline__ bool in_box(float2 q, float4 b) {
     return q.x >= b.x && q.x <= b.y && q.y >= b.z && q.y <= b.w;
 }
 
+// adds a thread's exact-test count to the launch's tally: one add per group
+// of lanes leaving together, spread over 64 counters
+__device__ __forceinline__ void count_tests(unsigned long long* ctr, unsigned n) {
+    if (!ctr) return;
+    const unsigned m = __activemask();
+    const unsigned t = __reduce_add_sync(m, n);
+    unsigned lane;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    if (lane == (unsigned)(__ffs(m) - 1) && t) atomicAdd(&ctr[blockIdx.x & 63], (unsigned long long)t);
+}
+
 // dependent-list shadowing with the box test in front of the exact test
 __global__ void __launch_bounds__(256) k_shadow_dep_cull(GeomArgs a, ProjArgs p) {
     const int nf = a.s.nf, ntau = a.s.ntau;
@@ -262,15 +273,20 @@ __global__ void __launch_bounds__(256) k_shadow_dep_cull(GeomArgs a, ProjArgs p)
     bool lit = valid && a.s.shadow[o] == 1;
     const double gd = a.g.dist[o];
     const float2 q = valid ? mid_uv(a, p, g, s) : make_float2(0.f, 0.f);
+    unsigned ntest = 0;
     for (int k = d0; k < d1; ++k) {
         if (!__any_sync(0xffffffffu, lit)) break;
         const int h = __ldg(&a.s.dep_idx[k]);
         if (lit && in_box(q, facet_box(a, p, h, s))) {
             const double hd = a.g.dist[(size_t)h * ntau + s];
-            if (gd > hd && dev_shadowtest(a, g, h, s) == 0) lit = false;
+            if (gd > hd) {
+                ++ntest;
+                if (dev_shadowtest(a, g, h, s) == 0) lit = false;
+            }
         }
     }
     if (valid && !lit) a.s.shadow[o] = 0;
+    count_tests(a.g.tests, ntest);
 }
 
 struct GridArgs {
@@ -362,6 +378,7 @@ __global__ void __launch_bounds__(256) k_shadow_grid(GeomArgs a, ProjArgs p, Gri
     const int n = gr.G * gr.G;
     const int* st = gr.start + (size_t)k * (n + 1);
     const int* li = gr.list + (size_t)k * nf;
+    unsigned ntest = 0;
     for (int y = max(cy - 1, 0); y <= min(cy + 1, gr.G - 1); ++y)
         for (int x = max(cx - 1, 0); x <= min(cx + 1, gr.G - 1); ++x) {
             const int c = y * gr.G + x;
@@ -370,12 +387,16 @@ __global__ void __launch_bounds__(256) k_shadow_grid(GeomArgs a, ProjArgs p, Gri
                 if (h == g || !in_box(q, facet_box(a, p, h, s))) continue;
                 const double hd = a.g.dist[(size_t)h * ntau + s];
                 const bool g_tested = (g < h) ? (gd > hd) : !(hd > gd);
-                if (g_tested && dev_shadowtest(a, g, h, s) == 0) {
+                if (!g_tested) continue;
+                ++ntest;
+                if (dev_shadowtest(a, g, h, s) == 0) {
                     a.s.shadow[o] = 0;
+                    count_tests(a.g.tests, ntest);
                     return;
                 }
             }
         }
+    count_tests(a.g.tests, ntest);
 }
 
 namespace {

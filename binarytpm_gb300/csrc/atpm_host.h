@@ -65,6 +65,9 @@ struct atpm_solve {
     size_t wb_bytes = 0;
     void* w32_mem = nullptr;  // this solve's FP32 W rows for the sparse remainder
     size_t w32_bytes = 0;
+    // the last atpm_geometry_shadow's shadow drivers
+    double last_shadow_ms = 0.0;
+    int64_t last_shadow_rays = 0, last_shadow_tests = -1;
     int4* qmap = nullptr;
     int nq = 0;
     cudaGraphExec_t graph = nullptr;

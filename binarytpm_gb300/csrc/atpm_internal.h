@@ -185,6 +185,7 @@ struct GeomWork {
     int vsplit;         // first vertex of the secondary (nv when synchronous)
     double tm[9];    // pole transformation matrix
     double car[3];   // heliocentric centre (km)
+    unsigned long long* tests;  // [64] exact ray-triangle tests of the culled drivers (or null)
 };
 int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t st);
 int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t st);

@@ -78,6 +78,7 @@ _SIGS = {
     "atpm_last_run_config": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_cosillum": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_selftest_bounded_wait": (C.c_int, [C.c_int32, C.c_int64, C.c_void_p]),
+    "atpm_last_shadow_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_selfheating_flux": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_profile_revolution": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_scattering_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -417,6 +418,13 @@ class Solve:
         v, d, t = C.c_int32(), C.c_int32(), C.c_int32()
         _ck(load().atpm_last_run_config(self.h, C.byref(v), C.byref(d), C.byref(t)))
         return v.value, d.value, bool(t.value)
+
+    def last_shadow_stats(self):
+        """(device ms, rays, exact ray-triangle tests or -1) of the last
+        geometry_shadow's shadow drivers."""
+        ms, r, t = C.c_double(), C.c_int64(), C.c_int64()
+        _ck(load().atpm_last_shadow_stats(self.h, C.byref(ms), C.byref(r), C.byref(t)))
+        return ms.value, r.value, t.value
 
     def last_run_stats(self):
         ms, la, fs = C.c_double(), C.c_int64(), C.c_int64()

@@ -244,6 +244,13 @@ ATPM_API atpm_status atpm_energy_balance(atpm_solve* s, double* absorbed, double
  * the device context usable.  No copy, product or TMEM allocation runs.
  * No counterpart in the reference, whose kernels have no bounded waits. */
 ATPM_API atpm_status atpm_selftest_bounded_wait(int32_t device, int64_t limit_cycles, int32_t* status_bits);
+/* The shadow drivers of the last atpm_geometry_shadow: their device time
+ * (ms, CUDA events), the rays they answered (facet x step queries: is this
+ * facet's midpoint occluded toward the Sun or observer at this step) and the
+ * exact ray-triangle tests (astshadowtest, main.cpp:1187-1247) the culled
+ * drivers ran after their box tests; exact_tests is -1 when the plain
+ * drivers ran (ATPM_SHADOW_CULL=0). */
+ATPM_API atpm_status atpm_last_shadow_stats(atpm_solve* s, double* shadow_ms, int64_t* rays, int64_t* exact_tests);
 /* Launch configuration of the last atpm_batch_run led by s (FAST): the
  * conduction register/occupancy variant (1-3), the tensor-core pipeline
  * depth, and whether that run timed the candidates (the autotuner does so
