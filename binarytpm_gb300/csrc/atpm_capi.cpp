@@ -435,22 +435,6 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     }
     const size_t ntiles = tcol.size();
     const size_t tile_el = 128 * 64;
-    // the sparse remainder: entries of cells without a tile, per row in list order
-    std::vector<int> rptr(nf + 1, 0), ridx;
-    std::vector<float> rvf;
-    for (int f = 0; f < nf; ++f) {
-        const size_t row = (size_t)(f >> 7) * nkb;
-        for (int k = sh->dep_ptr[f]; k < sh->dep_ptr[f + 1]; ++k) {
-            const int g = sh->dep_idx[k];
-            if (slot[row + (size_t)(g >> 6)] >= 0) continue;
-            ridx.push_back(g);
-            rvf.push_back(sh->dep_vf[k]);
-        }
-        rptr[f + 1] = (int)ridx.size();
-    }
-    const size_t rnnz = ridx.size();
-    const size_t b_rptr = rnnz ? align256((size_t)(nf + 1) * 4) : 0, b_ridx = rnnz ? align256(rnnz * 4) : 0;
-    const size_t b_rvf = b_ridx;
     // W32 row stride: the steps rounded up to the remainder kernel's 32-step
     // chunks (every lane's load stays inside its row; the pad stays zero)
     const int w32_ld = (ntau + 31) & ~31;
@@ -462,9 +446,8 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     const size_t b_slot = align256(ncell * 4);
     auto* tc = new TcShared();
     s->tc = tc;
-    tc->bytes = b_tiles + b_ptr + b_col + b_lo + b_loi + b_slot + b_rptr + b_ridx + b_rvf;
+    tc->bytes = b_tiles + b_ptr + b_col + b_lo + b_loi + b_slot;
     tc->tiles = ntiles;
-    tc->remainder = rnnz;
     tc->rb_tiles.resize(nmb);
     for (int mb = 0; mb < nmb; ++mb) tc->rb_tiles[mb] = tptr[mb + 1] - tptr[mb];
     CK(cudaMalloc(&tc->mem, tc->bytes));
@@ -480,15 +463,40 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     CK(cudaMemsetAsync(p_lo, 0, b_lo, s->st));
     CK(cudaMemcpyAsync(p_lo + b_lo, lo_of.data(), lo_of.size() * 4, cudaMemcpyHostToDevice, s->st));
     CK(cudaMemcpyAsync(d_slot, slot.data(), ncell * 4, cudaMemcpyHostToDevice, s->st));
-    char* p_rem = p_lo + b_lo + b_loi + b_slot;
-    if (rnnz) {
-        CK(cudaMemcpyAsync(p_rem, rptr.data(), (size_t)(nf + 1) * 4, cudaMemcpyHostToDevice, s->st));
-        CK(cudaMemcpyAsync(p_rem + b_rptr, ridx.data(), rnnz * 4, cudaMemcpyHostToDevice, s->st));
-        CK(cudaMemcpyAsync(p_rem + b_rptr + b_ridx, rvf.data(), rnnz * 4, cudaMemcpyHostToDevice, s->st));
-        s->w32_bytes = align256((size_t)nf * w32_ld * 4);
-        CK(cudaMalloc(&s->w32_mem, s->w32_bytes));
-        CK(cudaMemsetAsync(s->w32_mem, 0, s->w32_bytes, s->st));
+    // the sparse remainder: entries of cells without a tile, per row in list
+    // order (counted and gathered on the device from the uploaded lists)
+    size_t rnnz = 0;
+    const size_t b_rptr = align256((size_t)(nf + 1) * 4);
+    {
+        int* cnt_d = nullptr;
+        CK(cudaMalloc((void**)&cnt_d, (size_t)nf * 4));
+        std::vector<int> rptr(nf + 1, 0);
+        int rc = launch_rem_count(s->ds, nkb, d_slot, cnt_d, s->st);
+        cudaError_t e = rc ? cudaGetLastError() : cudaMemcpyAsync(rptr.data() + 1, cnt_d, (size_t)nf * 4,
+                                                                   cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        cudaFree(cnt_d);
+        if (e != cudaSuccess) return fail(ATPM_E_CUDA, "remainder count: %s", cudaGetErrorString(e));
+        for (int f = 0; f < nf; ++f) rptr[f + 1] += rptr[f];
+        rnnz = (size_t)rptr[nf];
+        if (rnnz) {
+            const size_t b_ridx = align256(rnnz * 4);
+            CK(cudaMalloc(&tc->rem_mem, b_rptr + 2 * b_ridx));
+            char* p = static_cast<char*>(tc->rem_mem);
+            CK(cudaMemcpyAsync(p, rptr.data(), (size_t)(nf + 1) * 4, cudaMemcpyHostToDevice, s->st));
+            if (launch_rem_fill(s->ds, nkb, d_slot, reinterpret_cast<int*>(p), reinterpret_cast<int*>(p + b_rptr),
+                                reinterpret_cast<float*>(p + b_rptr + b_ridx), s->st))
+                return fail(ATPM_E_CUDA, "remainder fill: %s", cudaGetErrorString(cudaGetLastError()));
+            s->ds.rem_ptr = reinterpret_cast<const int*>(p);
+            s->ds.rem_idx = reinterpret_cast<const int*>(p + b_rptr);
+            s->ds.rem_vf = reinterpret_cast<const float*>(p + b_rptr + b_ridx);
+            s->w32_bytes = align256((size_t)nf * w32_ld * 4);
+            CK(cudaMalloc(&s->w32_mem, s->w32_bytes));
+            CK(cudaMemsetAsync(s->w32_mem, 0, s->w32_bytes, s->st));
+            CK(cudaStreamSynchronize(s->st));  // rptr must outlive its copy
+        }
     }
+    tc->remainder = rnnz;
     if (launch_tc_fill(s->ds, nkb, d_slot, reinterpret_cast<const int*>(p_lo + b_lo), m, p_lo, s->st))
         return fail(ATPM_E_CUDA, "tile fill launch: %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaStreamSynchronize(s->st));  // the host tables must outlive their copies
@@ -503,9 +511,6 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     d.tc_nchunks = nch;
     d.tc_nmb = nmb;
     d.tc_nkb = nkb;
-    d.rem_ptr = rnnz ? reinterpret_cast<const int*>(p_rem) : nullptr;
-    d.rem_idx = rnnz ? reinterpret_cast<const int*>(p_rem + b_rptr) : nullptr;
-    d.rem_vf = rnnz ? reinterpret_cast<const float*>(p_rem + b_rptr + b_ridx) : nullptr;
     d.W32 = static_cast<float*>(s->w32_mem);
     d.w32_ld = w32_ld;
     std::vector<int4> q;
@@ -1008,6 +1013,7 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->ds_dev) cudaFree(s->ds_dev);
     if (s->tc && --s->tc->refs == 0) {
         cudaFree(s->tc->mem);
+        if (s->tc->rem_mem) cudaFree(s->tc->rem_mem);
         delete s->tc;
     }
     if (s->wb_mem) cudaFree(s->wb_mem);

@@ -45,6 +45,7 @@ struct TcShared {
     std::vector<int> rb_tiles;  // tiles per 128-facet row block (work ordering)
     size_t tiles = 0;           // tensor-core tiles
     size_t remainder = 0;       // list entries of the sparse remainder
+    void* rem_mem = nullptr;    // the remainder's row offsets, columns and view factors
 };
 
 struct atpm_solve {

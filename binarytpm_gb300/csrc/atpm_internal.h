@@ -240,6 +240,10 @@ int kernels_per_revolution(const Batch& b);          // kernels launch_revolutio
 // |value| as float bits + 1 (0: no entry) and the mask of 16-wide K slices
 // with an entry; cmax and cmask zeroed by the caller (atpm_spmm_tc.cu)
 int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, unsigned* count, stream_t st);
+// the sparse remainder's per-row counts, then (rptr scanned) its lists in list order
+int launch_rem_count(const DevSolve& s, int nkb, const int* slot, int* count, stream_t st);
+int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf,
+                    stream_t st);
 // cells whose tile needs the BF16 residual for some row's flux (need zeroed
 // by the caller); returns 1 when the shape is too large for the per-row maps
 int launch_tc_rowneed(const DevSolve& s, int nkb, unsigned* need, stream_t st);

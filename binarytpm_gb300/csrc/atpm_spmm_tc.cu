@@ -298,6 +298,57 @@ int launch_tc_fill(const DevSolve& s, int nkb, const int* slot, const int* lo_of
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+// The sparse remainder's lists from the uploaded view-factor lists and the
+// tile slot table (-1: the cell has no tile), a warp per facet row: first
+// the number of each row's entries in cells without a tile, then (after
+// the caller's scan into rptr) the entries themselves, in list order.
+__global__ void __launch_bounds__(256) k_rem_count(DevSolve s, int nkb, const int* slot, int* count) {
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (f >= s.nf) return;
+    const int* srow = slot + (size_t)(f >> 7) * nkb;
+    int n = 0;
+    for (int k = s.dep_ptr[f] + lane; k < s.dep_ptr[f + 1]; k += 32) n += srow[s.dep_idx[k] >> 6] < 0 ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (lane == 0) count[f] = n;
+}
+
+__global__ void __launch_bounds__(256) k_rem_fill(DevSolve s, int nkb, const int* slot, const int* rptr, int* ridx,
+                                                  float* rvf) {
+    const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (f >= s.nf) return;  // warp-uniform
+    const int* srow = slot + (size_t)(f >> 7) * nkb;
+    int out = rptr[f];
+    const int k0 = s.dep_ptr[f], k1 = s.dep_ptr[f + 1];
+    for (int kb = k0; kb < k1; kb += 32) {
+        const int k = kb + lane;
+        const bool take = k < k1 && srow[s.dep_idx[k] >> 6] < 0;
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (take) {
+            const int o = out + __popc(m & ((1u << lane) - 1u));
+            ridx[o] = s.dep_idx[k];
+            rvf[o] = s.dep_vf[k];
+        }
+        out += __popc(m);
+    }
+}
+
+int launch_rem_count(const DevSolve& s, int nkb, const int* slot, int* count, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t threads = (size_t)s.nf * 32;
+    k_rem_count<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, count);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf,
+                    stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    const size_t threads = (size_t)s.nf * 32;
+    k_rem_fill<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, rptr, ridx, rvf);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 // Work items whose row block has an active facet, compacted before every
 // launch (in map order within each warp), so tickets are spent on work only.
 __global__ void __launch_bounds__(128) k_tc_compact(Batch b) {
