@@ -413,7 +413,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-visibility", action="store_true", help="skip the all-pairs visibility measurement")
     ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
-    ap.add_argument("--serve-requests", type=int, default=48, help="requests in the serving run (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving run (1/s)")
     ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
     ap.add_argument("--precision-stress", type=int, default=0, metavar="SUBDIV",
@@ -688,42 +688,71 @@ def _mesh_digest(v, f) -> str:
 
 
 def serving(ctx, n_requests: int, rate: float, seed: int = 5):
-    """Poisson stream of thermal solves through the continuous-batching
-    server: binaries with a subdivision-3/4/5 primary (2,560 / 6,400 / 21,760
-    facets, secondary subdivision 3), thermal inertia log-uniform in
-    [10, 2000] SI, NX = 56, NTAU = 720, FAST precision.  Shapes are
-    registered once (view factors, shadows and scattering on the device);
-    requests arrive at exponential intervals of mean 1/rate."""
+    """The serving configuration: a Poisson stream (mean rate ``rate``) of
+    binary thermal solves through the continuous-batching server.  Each
+    request: a primary icosphere of subdivision 3, 4, 5 or 6 (1,280 ...
+    81,920 facets; equally likely, i.e. log-uniform in facets, r = 0.39 km,
+    +-5 %), a secondary of subdivision 3 or 4 (1,280 / 5,120 facets, r = 0.08
+    km, +-8 %), thermal inertia log-uniform in [10, 2000] SI; NX = 56,
+    NTAU = 720, FAST, solved to convergence.  The 8 shapes are registered
+    once (view factors, shadows and scattering on the device); requests are
+    admitted by HBM budget and batch slots, results collected by a waiter
+    thread as they finish."""
+    import queue
+    import threading
+
     from binarytpm_gb300 import lib, workloads
 
     rng = np.random.default_rng(seed)
-    srv = lib.Server(ctx, precision=lib.FAST, nx=56, budget_bytes=48 << 30, max_active=48, revs_per_tick=4)
+    srv = lib.Server(ctx, precision=lib.FAST, nx=56, budget_bytes=160 << 30, max_active=128, revs_per_tick=8)
     shapes = {}
-    for sub in (3, 4, 5):
-        prob = workloads.binary_problem(ctx, p_subdiv=sub)
-        shapes[sub] = (srv.add_shape(prob), prob.nf)
-    subs = rng.choice([3, 4, 5], size=n_requests, p=[0.4, 0.35, 0.25])
+    t_reg = time.perf_counter()
+    for p in (3, 4, 5, 6):
+        for q in (3, 4):
+            prob = workloads.binary_problem(ctx, p_subdiv=p, s_subdiv=q)
+            shapes[(p, q)] = (srv.add_shape(prob), prob.nf)
+    register_s = time.perf_counter() - t_reg
+    subs = rng.integers(3, 7, size=n_requests)
+    secs = rng.integers(3, 5, size=n_requests)
     tis = np.exp(rng.uniform(np.log(10.0), np.log(2000.0), size=n_requests))
     gaps = rng.exponential(1.0 / rate, size=n_requests)
+    pending = queue.Queue()
+    lats, errors = [], []
+
+    def waiter():
+        while True:
+            item = pending.get()
+            if item is None:
+                return
+            rid, sid = item
+            try:
+                lats.append(srv.wait(rid, sid, timeout_s=3600.0)[2])
+            except lib.AtpmError as ex:
+                errors.append(str(ex))
+
+    th = threading.Thread(target=waiter)
+    th.start()
     t0 = time.perf_counter()
-    rids = []
-    for sub, ti, gap in zip(subs, tis, gaps):
+    for p, q, ti, gap in zip(subs, secs, tis, gaps):
         target = time.perf_counter() + gap
         while time.perf_counter() < target:
             time.sleep(min(0.001, max(0.0, target - time.perf_counter())))
-        rids.append((srv.submit(shapes[sub][0], float(ti)), shapes[sub][0]))
-    lats = []
-    for rid, sid in rids:
-        _, _, lat = srv.wait(rid, sid)
-        lats.append(lat)
+        sid = shapes[(int(p), int(q))][0]
+        pending.put((srv.submit(sid, float(ti)), sid))
+    submit_s = time.perf_counter() - t0
+    pending.put(None)
+    th.join()
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    return {"requests": n_requests, "arrival_rate_per_s": rate, "p50_ms": 1e3 * float(np.percentile(lats, 50)),
-            "p99_ms": 1e3 * float(np.percentile(lats, 99)), "facet_steps_per_s": st["facet_steps_per_s"],
-            "wall_s": wall, "mix": {"subdiv3": int((subs == 3).sum()), "subdiv4": int((subs == 4).sum()),
-                                    "subdiv5": int((subs == 5).sum())},
-            "what": "continuous batching, HBM-budget admission, state resident on the device"}
+    mix = {f"primary_subdiv{p}": int((subs == p).sum()) for p in (3, 4, 5, 6)}
+    mix.update({f"secondary_subdiv{q}": int((secs == q).sum()) for q in (3, 4)})
+    return {"requests": n_requests, "completed": len(lats), "errors": errors[:5], "arrival_rate_per_s": rate,
+            "p50_ms": 1e3 * float(np.percentile(lats, 50)), "p99_ms": 1e3 * float(np.percentile(lats, 99)),
+            "facet_steps_per_s": st["facet_steps_per_s"], "wall_s": wall, "arrivals_s": submit_s,
+            "shape_registration_s": register_s, "mix": mix,
+            "what": "continuous batching, HBM-budget admission (160 GB, 128 slots, 8 revolutions per tick), "
+                    "state resident on the device, solves pooled per shape"}
 
 
 FP64_TI = [200.0, 2000.0]

@@ -748,6 +748,9 @@ atpm_status get_transposed(atpm_solve* s, const void* dev, size_t rows, size_t c
 }
 }  // namespace
 
+// device pointers of a solve into its arena (defined with the C ABI below)
+extern "C" void wire_arena(atpm_solve* s, const Layout& L);
+
 namespace atpm {
 void set_last_error(const char* msg) { g_err = msg; }
 atpm_status fail_status(atpm_status s, const char* msg) {
@@ -787,6 +790,75 @@ size_t batch_table_bytes(atpm_solve* const* solves, int n) {
     HostTable h;
     host_table(solves, n, h);
     return h.bt + h.bw + h.bf + h.bq;
+}
+
+atpm_status batch_plan(atpm_solve* const* solves, int n, BatchPlan& plan, cudaStream_t st) {
+    HostTable h;
+    host_table(solves, n, h);
+    const size_t need = h.bt + h.bw + h.bf + h.bq;
+    if (need > plan.bytes) {
+        if (plan.table) cudaFree(plan.table);
+        plan.table = nullptr;
+        plan.bytes = 0;
+        CK(cudaMalloc(&plan.table, need * 2));  // headroom: a grown batch reuses it
+        plan.bytes = need * 2;
+    }
+    char* t = static_cast<char*>(plan.table);
+    CK(cudaMemcpyAsync(t, h.tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice, st));
+    if (!h.wm.empty()) CK(cudaMemcpyAsync(t + h.bt, h.wm.data(), h.wm.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(t + h.bt + h.bw, h.fm.data(), h.fm.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    if (!h.qm.empty())
+        CK(cudaMemcpyAsync(t + h.bt + h.bw + h.bf, h.qm.data(), h.qm.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));  // host staging above is released on return
+    atpm_solve* s0 = solves[0];
+    plan.b = make_batch(s0->ctx, reinterpret_cast<DevSolve*>(t), n, reinterpret_cast<int4*>(t + h.bt), (int)h.wm.size(),
+                        reinterpret_cast<int2*>(t + h.bt + h.bw), (int)h.fm.size(), s0->P.precision, s0->P.nx);
+    set_tc_map(plan.b, reinterpret_cast<int4*>(t + h.bt + h.bw + h.bf), h.qm.size());
+    plan.b.tc_nmax = h.nmax;
+    set_remainder_grid(plan.b, solves, n);
+    plan.solves.assign(solves, solves + n);
+    return ATPM_OK;
+}
+
+atpm_status batch_plan_step(const BatchPlan& plan, int k, cudaStream_t st) {
+    for (int r = 0; r < k; ++r)
+        if (launch_revolution(plan.b, st)) return fail(ATPM_E_CUDA, "batched revolution launch");
+    return ATPM_OK;
+}
+
+void batch_plan_free(BatchPlan& plan) {
+    if (plan.table) cudaFree(plan.table);
+    plan.table = nullptr;
+    plan.bytes = 0;
+    plan.solves.clear();
+}
+
+atpm_status solve_refresh(atpm_solve* dst, atpm_solve* src) {
+    if (dst->nf != src->nf || dst->nv != src->nv || dst->nnz != src->nnz || dst->tc != src->tc ||
+        dst->arena_bytes != src->arena_bytes || dst->wb_bytes != src->wb_bytes || dst->w32_bytes != src->w32_bytes)
+        return fail(ATPM_E_INVALID, "solve refresh: different shapes");
+    CK(cudaSetDevice(src->ctx->device));
+    CK(cudaStreamSynchronize(src->st));
+    dst->P = src->P;
+    dst->have_forcing = src->have_forcing;
+    dst->have_temps = src->have_temps;
+    dst->has_position = src->has_position;
+    std::memcpy(dst->position, src->position, sizeof dst->position);
+    dst->sec_vertex = src->sec_vertex;
+    dst->sec_facet = src->sec_facet;
+    dst->revs_p = src->revs_p;
+    dst->revs_s = src->revs_s;
+    dst->ir_abs = src->ir_abs;
+    dst->ti = src->ti;
+    dst->ds = src->ds;  // scalars; device pointers rebased below
+    wire_arena(dst, layout(dst->nv, dst->nf, dst->nnz, dst->P));
+    dst->ds.Wb = dst->wb_mem;
+    dst->ds.W32 = static_cast<float*>(dst->w32_mem);
+    CK(cudaMemcpyAsync(dst->arena, src->arena, dst->arena_bytes, cudaMemcpyDeviceToDevice, dst->st));
+    if (dst->wb_mem) CK(cudaMemcpyAsync(dst->wb_mem, src->wb_mem, dst->wb_bytes, cudaMemcpyDeviceToDevice, dst->st));
+    if (dst->w32_mem) CK(cudaMemcpyAsync(dst->w32_mem, src->w32_mem, dst->w32_bytes, cudaMemcpyDeviceToDevice, dst->st));
+    CK(cudaStreamSynchronize(dst->st));
+    return upload_table(dst);
 }
 
 atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st) {

@@ -97,6 +97,20 @@ namespace atpm {
 // device buffer of at least batch_table_bytes(solves, n) bytes
 size_t batch_table_bytes(atpm_solve* const* solves, int n);
 atpm_status batch_step(atpm_solve* const* solves, int n, int k, void* table, cudaStream_t st);
+// a batch's device table and launch description, built once for a set of
+// solves and reused for every tick until the set changes
+struct BatchPlan {
+    std::vector<atpm_solve*> solves;
+    void* table = nullptr;
+    size_t bytes = 0;
+    Batch b{};
+};
+atpm_status batch_plan(atpm_solve* const* solves, int n, BatchPlan& plan, cudaStream_t st);
+atpm_status batch_plan_step(const BatchPlan& plan, int k, cudaStream_t st);
+void batch_plan_free(BatchPlan& plan);
+// dst (a clone of src's shape) takes src's parameters and device state
+// again by device copies, without allocating
+atpm_status solve_refresh(atpm_solve* dst, atpm_solve* src);
 atpm_status fail_status(atpm_status s, const char* msg);
 }  // namespace atpm
 

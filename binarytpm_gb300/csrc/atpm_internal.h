@@ -232,6 +232,8 @@ struct Batch {
 // deepest tensor-core pipeline that fits shared memory for step chunk N
 int tc_max_stages(int N);
 int launch_revolution(const Batch& b, stream_t st);  // W, Q, conduction, convergence, advance
+// per solve: control word (4), status, counts of the last `window` revolutions
+int launch_progress(const Batch& b, int window, int* out, stream_t st);
 int kernels_per_revolution(const Batch& b);          // kernels launch_revolution starts
 // BF16 view-factor tiles (and residual tiles) of a solve from its uploaded
 // lists: slot[mb * nkb + kb] = tile of (row block, column block), lo_of[t] =

@@ -54,6 +54,7 @@ struct ShapeEntry {
     atpm_params params{};
     atpm_solve* proto = nullptr;  // resident forcing
     uint64_t footprint = 0;
+    std::vector<atpm_solve*> pool;  // retired requests' solves, re-seeded from proto on admission
 };
 
 struct Request {
@@ -67,6 +68,8 @@ struct Request {
     int64_t facet_steps = 0;
     std::vector<float> stemp1;
     atpm_solve* solve = nullptr;
+    bool pooled = false;  // solve taken from its shape's pool (re-seeded, not cloned)
+    int last_rev = 0;     // revolutions done after the last tick
     uint64_t footprint = 0;
 };
 
@@ -80,8 +83,13 @@ struct atpm_server {
     int max_active = 64;
     int revs_per_tick = 2;
     cudaStream_t run_st = nullptr, setup_st = nullptr;
-    void* table = nullptr;
-    size_t table_bytes = 0;
+    atpm::BatchPlan plan;      // device table of the resident set, rebuilt when the set changes
+    std::vector<int64_t> plan_ids;  // the requests the table was built for (ids are never reused)
+    int* prog_dev = nullptr;   // per-tick progress records (atpm::launch_progress)
+    int* prog_host = nullptr;  // page-locked read-back of them
+    size_t prog_cap = 0;       // records the buffers hold
+    uint64_t pooled = 0;       // bytes held by pooled solves (counted against the budget)
+    bool pooling = true;       // ATPM_SERVER_POOL=0: retired solves are freed, admissions clone
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Request*> queue;
@@ -107,18 +115,20 @@ atpm_status admit(atpm_server* S, Request* r) {
         std::lock_guard<std::mutex> lk(S->mu);
         sh = S->shapes[r->shape].get();
     }
-    atpm_solve* s = nullptr;
+    atpm_solve* s = r->solve;
     // a device copy of the prototype: forcing and (shared) tensor-core tiles
-    // come along, no host work on the shape
-    atpm_status st = atpm_solve_clone(sh->proto, &s);
-    if (st) return st;
+    // come along, no host work on the shape; a pooled solve of the shape
+    // takes the prototype's state by device copies, without allocating
+    atpm_status st = s ? atpm::solve_refresh(s, sh->proto) : atpm_solve_clone(sh->proto, &s);
     if (!st) st = atpm_set_thermal_inertia(s, r->ti);
     if (!st && r->ti != 0.0f) st = atpm_initialise_temperatures(s);
     if (st) {
-        atpm_solve_destroy(s);
+        if (s) atpm_solve_destroy(s);
+        r->solve = nullptr;
         return st;
     }
     r->solve = s;
+    r->last_rev = 0;  // atpm_set_thermal_inertia restarts the revolution count
     r->t_start = now_s();
     return ATPM_OK;
 }
@@ -130,7 +140,12 @@ void retire(atpm_server* S, Request* r, atpm_status st) {
         r->nrev = r->solve->last_nrev;
     }
     if (r->solve) {
-        atpm_solve_destroy(r->solve);
+        if (S->pooling && !S->stop && !st) {
+            S->shapes[r->shape]->pool.push_back(r->solve);
+            S->pooled += r->footprint;
+        } else {
+            atpm_solve_destroy(r->solve);
+        }
         r->solve = nullptr;
     }
     r->status = st;
@@ -138,27 +153,28 @@ void retire(atpm_server* S, Request* r, atpm_status st) {
     r->done = true;
 }
 
-// per-solve bookkeeping after a tick: counts -> revolutions and facet-steps
-int64_t tick_facet_steps(atpm_solve* s, const atpm::Ctl& before, const atpm::Ctl& after) {
+// facet-steps of the revolutions a tick advanced a solve by: revolutions
+// last_rev .. rev - 1, a frozen facet counted only while active; win holds
+// the convergence counts of revolutions rev - W .. rev - 1
+int64_t tick_facet_steps(const atpm_solve* s, int last_rev, int rev, const int* win, int W) {
     const int nf = s->nf, ntau = s->P.ntau;
     const bool all_active = !s->P.freeze || s->ti == 0.0f;
     int64_t fs = 0;
-    std::vector<int32_t> cnt(s->P.revcap, 0);
-    if (after.rev > before.rev) {
-        if (cudaMemcpy(cnt.data(), s->ds.counts, (size_t)s->P.revcap * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return 0;
-        for (int r = before.rev; r < after.rev; ++r) {
-            int active = nf;
-            if (!all_active && r - 1 > 5) active = nf - cnt[r - 1];
-            fs += (int64_t)active * ntau;
+    for (int r = last_rev; r < rev; ++r) {
+        int active = nf;
+        if (!all_active && r - 1 > 5) {
+            const int j = (r - 1) - (rev - W);
+            active = nf - (j >= 0 && j < W ? win[j] : 0);
         }
+        fs += (int64_t)active * ntau;
     }
     return fs;
 }
 
 void run_loop(atpm_server* S) {
     cudaSetDevice(S->ctx->device);
-    std::vector<atpm::Ctl> before, after;
+    std::vector<atpm_solve*> evict;
+    const int W = S->revs_per_tick + 1;  // counts of the revolutions a tick can add, and the one before
     while (true) {
         // admission (holding the lock only to pick requests)
         std::vector<Request*> to_admit;
@@ -176,12 +192,30 @@ void run_loop(atpm_server* S) {
                     S->cv_done.notify_all();
                     continue;
                 }
-                if (S->resident + r->footprint > S->budget) break;  // wait for memory to free up
+                ShapeEntry* sh = S->shapes[r->shape].get();
+                if (!sh->pool.empty()) {
+                    // the memory of a pooled solve of this shape is already held
+                    r->solve = sh->pool.back();
+                    sh->pool.pop_back();
+                    S->pooled -= r->footprint;
+                } else {
+                    // pooled solves of other shapes give their memory back first
+                    for (auto& e : S->shapes) {
+                        while (S->resident + S->pooled + r->footprint > S->budget && !e->pool.empty()) {
+                            evict.push_back(e->pool.back());
+                            e->pool.pop_back();
+                            S->pooled -= e->footprint;
+                        }
+                    }
+                    if (S->resident + S->pooled + r->footprint > S->budget) break;  // wait for memory to free up
+                }
                 S->queue.pop_front();
                 S->resident += r->footprint;
                 to_admit.push_back(r);
             }
         }
+        for (atpm_solve* x : evict) atpm_solve_destroy(x);
+        evict.clear();
         for (Request* r : to_admit) {
             atpm_status st = admit(S, r);
             std::lock_guard<std::mutex> lk(S->mu);
@@ -199,32 +233,44 @@ void run_loop(atpm_server* S) {
             act = S->active;
         }
         if (act.empty()) continue;
-        // one tick: K revolutions of every resident solve in shared launches
+        // one tick: K revolutions of every resident solve in shared launches;
+        // the batch table is rebuilt only when the resident set changed
         std::vector<atpm_solve*> sv;
-        for (Request* r : act) sv.push_back(r->solve);
-        const size_t need = atpm::batch_table_bytes(sv.data(), (int)sv.size());
-        if (need > S->table_bytes) {
-            if (S->table) cudaFree(S->table);
-            S->table = nullptr;
-            S->table_bytes = 0;
-            if (cudaMalloc(&S->table, need * 2) != cudaSuccess) {
-                S->loop_error = atpm::fail_status(ATPM_E_NOMEM, "server: batch table allocation failed");
+        std::vector<int64_t> ids;
+        for (Request* r : act) {
+            sv.push_back(r->solve);
+            ids.push_back(r->id);
+        }
+        atpm_status st = ATPM_OK;
+        if (ids != S->plan_ids) {
+            // a new set (a solve's address may be reused, and a pooled solve
+            // carries its new request's parameters): rebuild the table
+            st = atpm::batch_plan(sv.data(), (int)sv.size(), S->plan, S->run_st);
+            S->plan_ids = st ? std::vector<int64_t>() : ids;
+        }
+        const size_t rec = (size_t)(5 + W);
+        if (!st && act.size() > S->prog_cap) {
+            if (S->prog_dev) cudaFree(S->prog_dev);
+            if (S->prog_host) cudaFreeHost(S->prog_host);
+            S->prog_dev = nullptr;
+            S->prog_host = nullptr;
+            S->prog_cap = 0;
+            const size_t cap = act.size() * 2;
+            if (cudaMalloc((void**)&S->prog_dev, cap * rec * 4) != cudaSuccess ||
+                cudaMallocHost((void**)&S->prog_host, cap * rec * 4) != cudaSuccess) {
+                S->loop_error = atpm::fail_status(ATPM_E_NOMEM, "server: progress buffers");
                 break;
             }
-            S->table_bytes = need * 2;
+            S->prog_cap = cap;
         }
-        before.resize(act.size());
-        after.resize(act.size());
-        for (size_t i = 0; i < act.size(); ++i)
-            cudaMemcpy(&before[i], act[i]->solve->ds.ctl, sizeof(atpm::Ctl), cudaMemcpyDeviceToHost);
-        atpm_status st = atpm::batch_step(sv.data(), (int)sv.size(), S->revs_per_tick, S->table, S->run_st);
-        if (!st && cudaStreamSynchronize(S->run_st) != cudaSuccess)
+        if (!st) st = atpm::batch_plan_step(S->plan, S->revs_per_tick, S->run_st);
+        // every solve's progress in one gather and one read-back
+        if (!st && atpm::launch_progress(S->plan.b, W, S->prog_dev, S->run_st))
+            st = atpm::fail_status(ATPM_E_CUDA, "server: progress gather launch");
+        if (!st && (cudaMemcpyAsync(S->prog_host, S->prog_dev, act.size() * rec * 4, cudaMemcpyDeviceToHost,
+                                    S->run_st) != cudaSuccess ||
+                    cudaStreamSynchronize(S->run_st) != cudaSuccess))
             st = atpm::fail_status(ATPM_E_CUDA, "server: revolution tick failed");
-        std::vector<int> status(act.size(), 0);
-        for (size_t i = 0; i < act.size() && !st; ++i) {
-            cudaMemcpy(&after[i], act[i]->solve->ds.ctl, sizeof(atpm::Ctl), cudaMemcpyDeviceToHost);
-            cudaMemcpy(&status[i], act[i]->solve->ds.status, 4, cudaMemcpyDeviceToHost);
-        }
         std::lock_guard<std::mutex> lk(S->mu);
         std::vector<Request*> keep;
         for (size_t i = 0; i < act.size(); ++i) {
@@ -234,14 +280,17 @@ void run_loop(atpm_server* S) {
                 retire(S, r, st);
                 continue;
             }
-            const int64_t fs = tick_facet_steps(r->solve, before[i], after[i]);
+            const int* p = S->prog_host + i * rec;
+            const int rev = p[0], active = p[1], status = p[4];
+            const int64_t fs = tick_facet_steps(r->solve, r->last_rev, rev, p + 5, W);
+            r->last_rev = rev;
             r->facet_steps += fs;
             S->done_facet_steps += fs;
-            r->solve->last_nrev = after[i].rev;
+            r->solve->last_nrev = rev;
             atpm_status rs = ATPM_OK;
-            if (status[i] & atpm::ST_NONFINITE) rs = ATPM_E_NONFINITE;
-            else if (status[i] & (atpm::ST_NEWTON_CAP | atpm::ST_TC_TIMEOUT)) rs = ATPM_E_ITERATION;
-            if (!after[i].active || rs || r->cancelled) {
+            if (status & atpm::ST_NONFINITE) rs = ATPM_E_NONFINITE;
+            else if (status & (atpm::ST_NEWTON_CAP | atpm::ST_TC_TIMEOUT)) rs = ATPM_E_ITERATION;
+            if (!active || rs || r->cancelled) {
                 S->resident -= r->footprint;
                 retire(S, r, r->cancelled ? ATPM_E_CANCELLED : rs);
                 if (!r->status) {
@@ -277,6 +326,10 @@ ATPM_API atpm_status atpm_server_create(atpm_context* ctx, int32_t precision, in
     S->budget = budget_bytes;
     S->max_active = max_active;
     S->revs_per_tick = revs_per_tick;
+    {
+        const char* e = std::getenv("ATPM_SERVER_POOL");
+        S->pooling = !(e && e[0] == '0');
+    }
     cudaSetDevice(ctx->device);
     if (cudaStreamCreateWithFlags(&S->run_st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->setup_st, cudaStreamNonBlocking) != cudaSuccess) {
@@ -367,10 +420,16 @@ ATPM_API atpm_status atpm_server_wait(atpm_server* S, int64_t id, double timeout
     const auto deadline = clock_t_::now() + std::chrono::duration<double>(timeout_s);
     if (!S->cv_done.wait_until(lk, deadline, [&] { return r->done; }))
         return atpm::fail_status(ATPM_E_STATE, "wait: timed out (request still running)");
-    if (r->status) return atpm::fail_status(r->status, "request failed");
-    if (stemp1) std::memcpy(stemp1, r->stemp1.data(), r->stemp1.size() * 4);
-    if (nrev) *nrev = r->nrev;
-    if (latency_s) *latency_s = r->t_done - r->t_submit;
+    // the result is handed over once: the request (and its host copy of the
+    // temperatures) is forgotten, so a long stream does not accumulate them
+    const atpm_status rs = r->status;
+    if (!rs) {
+        if (stemp1) std::memcpy(stemp1, r->stemp1.data(), r->stemp1.size() * 4);
+        if (nrev) *nrev = r->nrev;
+        if (latency_s) *latency_s = r->t_done - r->t_submit;
+    }
+    S->all.erase(it);
+    if (rs) return atpm::fail_status(rs, "request failed");
     return ATPM_OK;
 }
 
@@ -403,9 +462,14 @@ ATPM_API atpm_status atpm_server_destroy(atpm_server* S) {
     }
     if (S->loop.joinable()) S->loop.join();
     cudaSetDevice(S->ctx->device);
-    for (auto& e : S->shapes)
+    for (auto& e : S->shapes) {
+        for (atpm_solve* x : e->pool) atpm_solve_destroy(x);
+        e->pool.clear();
         if (e->proto) atpm_solve_destroy(e->proto);
-    if (S->table) cudaFree(S->table);
+    }
+    atpm::batch_plan_free(S->plan);
+    if (S->prog_dev) cudaFree(S->prog_dev);
+    if (S->prog_host) cudaFreeHost(S->prog_host);
     if (S->run_st) cudaStreamDestroy(S->run_st);
     if (S->setup_st) cudaStreamDestroy(S->setup_st);
     atpm_status st = S->loop_error;

@@ -872,6 +872,32 @@ int launch_fill_initial(const DevSolve& s, const void* mean, const PowTab& pq, s
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+// Progress of every solve of a batch for one read-back: its control word,
+// status word and the convergence counts of its last `window` revolutions
+// (record of 5 + window ints per solve)
+__global__ void k_progress(Batch b, int window, int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n) return;
+    const DevSolve& s = b.tab[i];
+    int* o = out + (size_t)i * (5 + window);
+    const Ctl c = *s.ctl;
+    o[0] = c.rev;
+    o[1] = c.active;
+    o[2] = c.converged;
+    o[3] = c.numconv;
+    o[4] = *s.status;
+    for (int j = 0; j < window; ++j) {
+        const int r = c.rev - window + j;
+        o[5 + j] = (r >= 0 && r < s.revcap) ? s.counts[r] : 0;
+    }
+}
+
+int launch_progress(const Batch& b, int window, int* out, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    k_progress<<<(b.n + 127) / 128, 128, 0, st>>>(b, window, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 int launch_energy_balance(const DevSolve& s, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const int g = (s.nf + 127) / 128;

@@ -532,7 +532,7 @@ class Server:
 
     def wait(self, rid: int, shape_id: int, timeout_s: float = 600.0):
         nf, ntau = self._shapes[shape_id]
-        out = np.zeros((nf, ntau), np.float32)
+        out = np.empty((nf, ntau), np.float32)
         nrev, lat = C.c_int32(), C.c_double()
         _ck(load().atpm_server_wait(self.h, rid, timeout_s, _p(out), C.byref(nrev), C.byref(lat)))
         return out, nrev.value, lat.value

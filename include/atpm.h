@@ -352,7 +352,10 @@ ATPM_API atpm_status atpm_server_add_shape(atpm_server* s, const atpm_shape* sha
                                            int32_t* shape_id);
 ATPM_API atpm_status atpm_server_submit(atpm_server* s, int32_t shape_id, float thermal_inertia, int64_t* request_id);
 ATPM_API atpm_status atpm_server_cancel(atpm_server* s, int64_t request_id);
-/* Wait up to timeout_s for a request; stemp1 [nf][ntau] (may be NULL). */
+/* Wait up to timeout_s for a request; stemp1 [nf][ntau] (may be NULL).  A
+ * wait that finds the request finished hands its result over and forgets
+ * the request (a later wait on the same id is ATPM_E_INVALID); a wait that
+ * times out (ATPM_E_STATE) leaves it to a later wait. */
 ATPM_API atpm_status atpm_server_wait(atpm_server* s, int64_t request_id, double timeout_s, float* stemp1,
                                       int32_t* nrev, double* latency_s);
 /* Latency percentiles (submit to result) and facet-steps/s of completed requests. */
