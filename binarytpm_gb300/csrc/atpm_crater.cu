@@ -174,7 +174,13 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
     const int j = threadIdx.x;
     const bool act = j < nsf;
     const float alb = c.albedo[f];
-    const float m1 = A::div(A::mul(c.ti[f], A::sqrt_(A::div(A::mul(2.0f, c.PI), c.rot_period))), dz);
+    // the facet body's revolutions per model period scale the time step and
+    // the skin factor (175706/Run-04/thermal_GPU.cu:448-450, 539); with none
+    // given the expressions are the synchronous module's (GPU_code.cu:392-393)
+    const float w2pi = c.numrevs ? A::mul(A::mul(2.0f, c.PI), c.numrevs[f]) : A::mul(2.0f, c.PI);
+    const float m0f = c.numrevs ? A::div(A::div(w2pi, (float)ntau), A::mul(dz, dz)) : m0;
+    const float m1 = A::div(A::mul(c.ti[f], A::sqrt_(A::div(w2pi, c.rot_period))), dz);
+    const float esw = A::mul(c.ir_abs, es);  // IR_ABS * EPSSIGMA (thermal_GPU.cu:521): es when ir_abs = 1
     const float oma = A::sub(1.0f, alb);
     float T[NX + 1];
     float* tp = c.temp + (size_t)f * (NX + 1) * nsf;
@@ -206,7 +212,7 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
 #pragma unroll
             for (int i = 1; i < NX; ++i) {
                 const float t1 = T[i];
-                T[i] = A::add(t1, A::mul(m0, A::add(A::sub(T[i + 1], A::mul(2.0f, t1)), t0)));
+                T[i] = A::add(t1, A::mul(m0f, A::add(A::sub(T[i + 1], A::mul(2.0f, t1)), t0)));
                 t0 = t1;
             }
             T[NX] = T[NX - 1];
@@ -214,7 +220,7 @@ __global__ void __launch_bounds__(128) k_crater_revolution(CraterDev c, PowTab p
         // boundary_condition (GPU_code.cu:418-490)
         if (act) {
             c.stemp0[o] = old;
-            W[j] = A::mul(es, cpow4<MODE>(p4, old, c.status));
+            W[j] = A::mul(esw, cpow4<MODE>(p4, old, c.status));
         }
         __syncthreads();
         if (act) {
@@ -290,12 +296,13 @@ __global__ void __launch_bounds__(128) k_crater_equilibrium(CraterDev c, PowTab 
     const int j = threadIdx.x;
     const bool act = j < nsf;
     const float oma = A::sub(1.0f, c.albedo[f]);
+    const float esw = A::mul(c.ir_abs, es);
     for (int s = 0; s < ntau; ++s) {
         const size_t o = (size_t)f * ntau * nsf + (size_t)s * nsf + j;
         if (act) {
             const float old = c.stemp1[o];
             c.stemp0[o] = old;
-            W[j] = A::mul(es, cpow4<MODE>(p4, old, c.status));
+            W[j] = A::mul(esw, cpow4<MODE>(p4, old, c.status));
         }
         __syncthreads();
         if (act) {
@@ -342,7 +349,7 @@ __global__ void k_crater_init_self(CraterDev c, PowTab p4, float es, const float
     extern __shared__ float sm[];
     const int f = blockIdx.x, j = threadIdx.x, nsf = c.nsf;
     float* w = sm;
-    if (j < nsf) w[j] = __fmul_rn(es, cpow4_exact(p4, t0[(size_t)f * nsf + j], c.status));
+    if (j < nsf) w[j] = __fmul_rn(__fmul_rn(c.ir_abs, es), cpow4_exact(p4, t0[(size_t)f * nsf + j], c.status));
     __syncthreads();
     if (j >= nsf) return;
     float sh = 0.0f;

@@ -20,6 +20,7 @@ struct atpm_crater {
     cudaStream_t st = nullptr;
     void* mem = nullptr;
     float* scratch = nullptr;  // 2 x nf x nsf (initialisation)
+    float* numrevs = nullptr;  // [nf] revolutions per model period (non-synchronous binaries), once set
     float PI = 0.0f, rot = 0.0f;
     bool have_model = false;
     CraterDev d{};
@@ -145,6 +146,8 @@ ATPM_API atpm_status atpm_crater_create(atpm_context* ctx, int32_t nf, int32_t n
     cudaMemcpy((void*)d.cmult, mult, sizeof mult, cudaMemcpyHostToDevice);
     c->PI = 4.0f * std::atan(1.0f);
     d.PI = c->PI;
+    d.numrevs = nullptr;
+    d.ir_abs = 1.0f;
     *out = c;
     return ATPM_OK;
 }
@@ -154,10 +157,34 @@ ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c) {
     cudaSetDevice(c->ctx->device);
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->mem) cudaFree(c->mem);
+    if (c->numrevs) cudaFree(c->numrevs);
     if (c->st) cudaStreamDestroy(c->st);
     atpm_context* ctx = c->ctx;
     delete c;
     atpm_context_release(ctx);
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_set_revolutions(atpm_crater* c, const float* numrevs) {
+    if (!c) return atpm::fail_status(ATPM_E_INVALID, "null crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    if (!numrevs) {
+        c->d.numrevs = nullptr;
+        return ATPM_OK;
+    }
+    for (int f = 0; f < c->nf; ++f)
+        if (!(numrevs[f] > 0.0f) || !std::isfinite(numrevs[f]))
+            return atpm::fail_status(ATPM_E_INVALID, "crater_set_revolutions: revolutions must be positive");
+    if (!c->numrevs) CC(cudaMalloc((void**)&c->numrevs, (size_t)c->nf * 4), "allocation");
+    CC(cudaMemcpy(c->numrevs, numrevs, (size_t)c->nf * 4, cudaMemcpyHostToDevice), "copy");
+    c->d.numrevs = c->numrevs;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_set_ir_absorptivity(atpm_crater* c, float ir_abs) {
+    if (!c || !(ir_abs >= 0.0f) || !std::isfinite(ir_abs))
+        return atpm::fail_status(ATPM_E_INVALID, "crater_set_ir_absorptivity: bad arguments");
+    c->d.ir_abs = ir_abs;
     return ATPM_OK;
 }
 

@@ -302,6 +302,11 @@ struct CraterDev {
     const float* ctri;       // [nsf][2][3]
     const float* cmult;      // [100][2] trivector multipliers
     float PI, rot_period;
+    // non-synchronous binaries (175706/Run-04/thermal_GPU.cu): revolutions of
+    // each facet's body per model period (null: 1 for every facet) and the
+    // IR absorptivity of crater self-heating (1 unless set)
+    const float* numrevs;    // [nf] or null
+    float ir_abs;
     // per facet
     uint8_t* conv;           // sfc_converged
     const float* albedo;

@@ -320,6 +320,15 @@ ATPM_API atpm_status atpm_crater_get_array(atpm_crater* c, int32_t which, void* 
 ATPM_API atpm_status atpm_crater_set_array_strided(atpm_crater* c, int32_t which, const void* base,
                                                    uint64_t facet_stride);
 ATPM_API atpm_status atpm_crater_get_array_strided(atpm_crater* c, int32_t which, void* base, uint64_t facet_stride);
+/* Non-synchronous binaries (the 175706 program's module,
+ * 175706/Run-04/thermal_GPU.cu): each facet's body turns numrevs[f] times
+ * per model period, which scales that facet's crater time step and skin
+ * factor (thermal_GPU.cu:448-450, 539); NULL returns every facet to one
+ * turn, the synchronous module's expressions.  The IR absorptivity scales
+ * the crater sub-facets' emission seen by the others (thermal_GPU.cu:521,
+ * 390, 615); 1 unless set. */
+ATPM_API atpm_status atpm_crater_set_revolutions(atpm_crater* c, const float* numrevs /* [nf] or NULL */);
+ATPM_API atpm_status atpm_crater_set_ir_absorptivity(atpm_crater* c, float ir_abs);
 /* GPU_sfcpartialshadow (909-921): every step in one launch */
 ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c);
 /* GPU_single_scattering / GPU_multiple_scattering (927-949) */
