@@ -14,6 +14,15 @@
 // the Visibility driver's GPU module (3905/Visibility/NominalPole/
 // GPU_code.cu:146-283), whose partial-visibility kernel is the same
 // sfcpartialshadow toward the observer.
+//
+// With -DREF_NONSYNC_MODULE it provides the 27 symbols of the non-synchronous
+// binary program's module instead (175706/Run-04/thermal_GPU.cu:698-1279):
+// the same kernels over flat [facet][step][sub-facet] arrays, with each
+// facet's revolution count in the time step and skin factor
+// (thermal_GPU.cu:448-450, 539) and the IR absorptivity on the sub-facets'
+// mutual emission (thermal_GPU.cu:390, 521, 615).  The synchronous module is
+// the case of one revolution and absorptivity 1, whose products are exact, so
+// one set of kernels serves both.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -69,6 +78,8 @@ float c_PI;
 float c_rot_period;
 float* vf_D = nullptr;
 Facet_Properties* FP_D = nullptr;
+float* NR_D = nullptr;      // per-facet revolution counts (non-synchronous module)
+float c_ir_abs = 1.0f;      // IR absorptivity (non-synchronous module)
 Roughness_Shadow* RS_D = nullptr;
 Roughness_Illumination* RI_D = nullptr;
 Roughness_Globalillumination* RGI_D = nullptr;
@@ -149,6 +160,7 @@ void k_multiple_scattering(int b, float solar, float acc, int step) {
 
 // GPU_code.cu:328-371
 void k_initialise_temperatures(int b, float ES) {
+    const float IR = c_ir_abs;
     float albedo = FP_D[b].albedo;
     float st0[SFCNUMFACE];
     for (int t = 0; t < SFCNUMFACE; ++t) {
@@ -160,7 +172,7 @@ void k_initialise_temperatures(int b, float ES) {
     }
     for (int t = 0; t < SFCNUMFACE; ++t) {
         float sh = 0.0f;
-        for (int i = 0; i != SFCNUMFACE; ++i) sh = sh + (ES * powf(st0[i], 4.0f) * vf_D[(i * SFCNUMFACE) + t]);
+        for (int i = 0; i != SFCNUMFACE; ++i) sh = sh + (IR * ES * powf(st0[i], 4.0f) * vf_D[(i * SFCNUMFACE) + t]);
         float temp = 0.0f;
         for (int s = 0; s != NTAU; ++s)
             temp = temp + ((1.0f / NTAU) * (((1.0f - albedo) * RI_D[b].sfc_illumination[s][t]) +
@@ -171,10 +183,14 @@ void k_initialise_temperatures(int b, float ES) {
     }
 }
 
-// GPU_code.cu:377-412 (the out-of-range read of row NX+1 at line 403 is not reproduced)
+// facet b's turns per model period: 1 in the synchronous module
+float revs(int b) { return NR_D ? NR_D[b] : 1.0f; }
+
+// GPU_code.cu:377-412 (the out-of-range read of row NX+1 at line 403 is not
+// reproduced); non-synchronous: thermal_GPU.cu:430-478
 void k_finite_difference(int b) {
     if (FP_D[b].sfc_converged) return;
-    float DZ = 8.0f / NX, DTAU = (2.0f * c_PI) / NTAU, M0 = DTAU / (DZ * DZ);
+    float DZ = 8.0f / NX, DTAU = (2.0f * c_PI * revs(b)) / NTAU, M0 = DTAU / (DZ * DZ);
     for (int t = 0; t < SFCNUMFACE; ++t) {
         float (*T)[SFCNUMFACE] = RT_D[b].sfc_temp;
         float t0 = T[0][t], t1 = T[1][t], t2 = T[2][t];
@@ -187,16 +203,17 @@ void k_finite_difference(int b) {
     }
 }
 
-// GPU_code.cu:418-490
+// GPU_code.cu:418-490; non-synchronous: thermal_GPU.cu:485-574
 void k_boundary_condition(int b, float ES, float TACC, int step) {
     if (FP_D[b].sfc_converged) return;
-    float albedo = FP_D[b].albedo, ti = FP_D[b].thermal_inertia;
+    const float IR = c_ir_abs;
+    float albedo = FP_D[b].albedo, ti = FP_D[b].thermal_inertia, nr = revs(b);
     float stemp[SFCNUMFACE];
     Roughness_Temperatures& R = RT_D[b];
     for (int t = 0; t < SFCNUMFACE; ++t) {
         stemp[t] = R.sfc_stemp1[step][t];
         R.sfc_stemp0[step][t] = stemp[t];
-        stemp[t] = ES * powf(stemp[t], 4.0f);
+        stemp[t] = IR * ES * powf(stemp[t], 4.0f);
     }
     for (int t = 0; t < SFCNUMFACE; ++t) {
         float TR0 = R.sfc_temp[0][t], TR1 = TR0, temp = R.sfc_temp[1][t];
@@ -204,7 +221,7 @@ void k_boundary_condition(int b, float ES, float TACC, int step) {
         float inc = RGH_D[b].sfc_globalheating[step][t];
         for (int i = 0; i != SFCNUMFACE; ++i) inc = inc + (stemp[i] * vf_D[(i * SFCNUMFACE) + t]);
         float DT = 1.0f, DZ = 8.0f / NX;
-        float M1 = ti * sqrtf(2.0f * c_PI / c_rot_period) / DZ;
+        float M1 = ti * sqrtf(2.0f * c_PI * nr / c_rot_period) / DZ;
         float M2 = ((1.0f - albedo) * ill) + inc;
         for (int it = 0; DT >= TACC && it < 1000; ++it) {
             float SBC = M2 + (M1 * (temp - TR0)) - (ES * TR0 * TR0 * TR0 * TR0);
@@ -218,16 +235,17 @@ void k_boundary_condition(int b, float ES, float TACC, int step) {
     }
 }
 
-// GPU_code.cu:496-548
+// GPU_code.cu:496-548; non-synchronous: thermal_GPU.cu:581-641
 void k_inst_equilibrium(int b, float ES, int step) {
     if (FP_D[b].sfc_converged) return;
+    const float IR = c_ir_abs;
     float albedo = FP_D[b].albedo;
     float stemp[SFCNUMFACE];
     Roughness_Temperatures& R = RT_D[b];
     for (int t = 0; t < SFCNUMFACE; ++t) {
         stemp[t] = R.sfc_stemp1[step][t];
         R.sfc_stemp0[step][t] = stemp[t];
-        stemp[t] = ES * powf(stemp[t], 4.0f);
+        stemp[t] = IR * ES * powf(stemp[t], 4.0f);
     }
     for (int t = 0; t < SFCNUMFACE; ++t) {
         float inc = RGH_D[b].sfc_globalheating[step][t];
@@ -265,6 +283,130 @@ void GPU_sfcpartialshadow(Roughness_Shadow* RS_H) {
 #pragma omp parallel for schedule(static)
         for (int b = 0; b < ASTNUMFACE; ++b) k_sfcpartialshadow(b, step);
     }
+}
+}
+#elif defined(REF_NONSYNC_MODULE)
+namespace {
+void set_constants(const GPU_Surface& S_H);
+void run_steps(void (*k)(int, float, int), float x) {
+    for (int step = 0; step != NTAU; ++step) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < ASTNUMFACE; ++b) k(b, x, step);
+    }
+}
+}
+// ---- the 27 entry points of the non-synchronous module
+// (175706/Run-04/thermal_GPU.cu:698-1279): flat arrays in the layout of the
+// synchronous module's per-facet structs, copied field by field ----
+extern "C" {
+void set_cuda_device() {}
+
+void initialise_GPU_constants(float rot_period_H, float viewfactors_H[SFCNUMFACE][SFCNUMFACE], GPU_Surface S_H) {
+    c_PI = 4.0f * atanf(1.0f);
+    c_rot_period = rot_period_H;
+    if (!vf_D) vf_D = alloc<float>(SFCNUMFACE * SFCNUMFACE);
+    std::memcpy(vf_D, viewfactors_H, sizeof(float) * SFCNUMFACE * SFCNUMFACE);
+    set_constants(S_H);
+}
+void initialise_GPU_facet_properties_arrays() {
+    FP_D = alloc<Facet_Properties>(ASTNUMFACE);
+    NR_D = alloc<float>(ASTNUMFACE);
+}
+void initialise_GPU_shadow_arrays() { RS_D = alloc<Roughness_Shadow>(ASTNUMFACE); }
+void initialise_GPU_illumination_arrays() { RI_D = alloc<Roughness_Illumination>(ASTNUMFACE); }
+void initialise_GPU_globalillumination_arrays() { RGI_D = alloc<Roughness_Globalillumination>(ASTNUMFACE); }
+void initialise_GPU_globalheating_arrays() { RGH_D = alloc<Roughness_Globalheating>(ASTNUMFACE); }
+void initialise_GPU_temperature_arrays() { RT_D = alloc<Roughness_Temperatures>(ASTNUMFACE); }
+void freeup_GPU_shadow_arrays() { std::free(RS_D); RS_D = nullptr; }
+void freeup_GPU_globalillumination_arrays() { std::free(RGI_D); RGI_D = nullptr; }
+void freeup_GPU_globalheating_arrays() { std::free(RGH_D); RGH_D = nullptr; }
+void freeup_GPU_temperature_arrays() { std::free(RT_D); RT_D = nullptr; }
+
+void set_GPU_facet_properties(bool* conv, float* albedo, float* ti, float* numrevs) {
+    for (int b = 0; b < ASTNUMFACE; ++b) {
+        FP_D[b].sfc_converged = conv[b];
+        FP_D[b].albedo = albedo[b];
+        FP_D[b].thermal_inertia = ti[b];
+        NR_D[b] = numrevs[b];
+    }
+}
+void obtain_GPU_facet_properties(bool* conv, float* albedo, float* ti, float* numrevs) {
+    for (int b = 0; b < ASTNUMFACE; ++b) {
+        conv[b] = FP_D[b].sfc_converged;
+        albedo[b] = FP_D[b].albedo;
+        ti[b] = FP_D[b].thermal_inertia;
+        numrevs[b] = NR_D[b];
+    }
+}
+void load_GPU_globalillumination(float* H) { std::memcpy(RGI_D, H, sizeof(Roughness_Globalillumination) * ASTNUMFACE); }
+void load_GPU_globalheating(float* H) { std::memcpy(RGH_D, H, sizeof(Roughness_Globalheating) * ASTNUMFACE); }
+
+void GPU_sfcpartialshadow(int* shadow, float* sfc_shadow, float* sfc_illumvector, float* sfc_illumangle) {
+    const size_t ns = (size_t)NTAU * SFCNUMFACE;
+    for (int b = 0; b < ASTNUMFACE; ++b) {
+        std::memcpy(RS_D[b].shadow, shadow + (size_t)b * NTAU, sizeof(int) * NTAU);
+        std::memcpy(RS_D[b].sfc_shadow, sfc_shadow + b * ns, sizeof(float) * ns);
+        std::memcpy(RS_D[b].sfc_illumvector, sfc_illumvector + (size_t)b * NTAU * 3, sizeof(float) * NTAU * 3);
+        std::memcpy(RS_D[b].sfc_illumangle, sfc_illumangle + b * ns, sizeof(float) * ns);
+    }
+    for (int step = 0; step != NTAU; ++step) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < ASTNUMFACE; ++b) k_sfcpartialshadow(b, step);
+    }
+}
+void obtain_GPU_roughness_shadows(int* shadow, float* sfc_shadow, float* sfc_illumvector, float* sfc_illumangle) {
+    const size_t ns = (size_t)NTAU * SFCNUMFACE;
+    for (int b = 0; b < ASTNUMFACE; ++b) {
+        std::memcpy(shadow + (size_t)b * NTAU, RS_D[b].shadow, sizeof(int) * NTAU);
+        std::memcpy(sfc_shadow + b * ns, RS_D[b].sfc_shadow, sizeof(float) * ns);
+        std::memcpy(sfc_illumvector + (size_t)b * NTAU * 3, RS_D[b].sfc_illumvector, sizeof(float) * NTAU * 3);
+        std::memcpy(sfc_illumangle + b * ns, RS_D[b].sfc_illumangle, sizeof(float) * ns);
+    }
+}
+void obtain_GPU_roughness_temperatures(float* stemp0, float* stemp1, float* temp) {
+    const size_t ns = (size_t)NTAU * SFCNUMFACE, nd = (size_t)(NX + 1) * SFCNUMFACE;
+    for (int b = 0; b < ASTNUMFACE; ++b) {
+        std::memcpy(stemp0 + b * ns, RT_D[b].sfc_stemp0, sizeof(float) * ns);
+        std::memcpy(stemp1 + b * ns, RT_D[b].sfc_stemp1, sizeof(float) * ns);
+        std::memcpy(temp + b * nd, RT_D[b].sfc_temp, sizeof(float) * nd);
+    }
+}
+// thermal_GPU.cu:1102-1118 copies back the global-illumination array
+void obtain_GPU_roughness_illumination(float* H) {
+    std::memcpy(H, RGI_D, sizeof(Roughness_Globalillumination) * ASTNUMFACE);
+}
+
+void GPU_single_scattering(float solar) { run_steps(k_single_scattering, solar); }
+void GPU_multiple_scattering(float solar, float acc) {
+    for (int step = 0; step != NTAU; ++step) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < ASTNUMFACE; ++b) k_multiple_scattering(b, solar, acc, step);
+    }
+}
+void GPU_zero_temperatures() {
+    for (int b = 0; b < ASTNUMFACE; ++b) std::memset(&RT_D[b], 0, sizeof(Roughness_Temperatures));
+}
+void GPU_initialise_temperatures(float EPS, float SIGMA, float IR_ABS) {
+    float ES = EPS * SIGMA;
+    c_ir_abs = IR_ABS;
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < ASTNUMFACE; ++b) k_initialise_temperatures(b, ES);
+}
+void GPU_inertia_difference(float EPS, float SIGMA, float IR_ABS, float TACC) {
+    float ES = EPS * SIGMA, TACC2 = TACC / 10.0f;
+    c_ir_abs = IR_ABS;
+    for (int step = 0; step != NTAU; ++step) {
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < ASTNUMFACE; ++b) { k_finite_difference(b); k_boundary_condition(b, ES, TACC2, step); }
+    }
+}
+void GPU_inst_equilibrium(float EPS, float SIGMA, float IR_ABS) {
+    c_ir_abs = IR_ABS;
+    run_steps(k_inst_equilibrium, EPS * SIGMA);
+}
+void GPU_converged(float TACC) {
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < ASTNUMFACE; ++b) k_converged(b, TACC);
 }
 }
 #else

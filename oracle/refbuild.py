@@ -447,21 +447,58 @@ static void __oracle_rev(Asteroid& A, int rev) {
 }
 '''
 
+# With the crater model on: per part, the crater forcing the module returns
+# (sub-facet shadow fractions, Sun angles, and what the program stores as the
+# sub-facet total illumination) appended in facet order, and the per-revolution
+# crater convergence counts.
+_NONSYNC_ROUGH_HOOKS = r'''
+static void __oracle_dump_rough_forcing(Asteroid& A) {
+	FILE* fp = fopen("oracle_rough_forcing.bin", "ab");
+	for (int i = STARTROUGHFACE; i != ENDROUGHFACE + 1; ++i)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = ((A.beginf() + i)->beginsf() + j)->rtnshadow(s); fwrite(&v, 4, 1, fp); }
+	for (int i = STARTROUGHFACE; i != ENDROUGHFACE + 1; ++i)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = ((A.beginf() + i)->beginsf() + j)->rtnillumangle(s); fwrite(&v, 4, 1, fp); }
+	for (int i = STARTROUGHFACE; i != ENDROUGHFACE + 1; ++i)
+		for (int j = 0; j != SFCNUMFACE; ++j)
+			for (int s = 0; s != NTAU; ++s) { float v = ((A.beginf() + i)->beginsf() + j)->rtntotalillumination(s); fwrite(&v, 4, 1, fp); }
+	fclose(fp);
+}
+static void __oracle_rough_rev(Asteroid& A, int rev) {
+	FILE* fp = fopen("oracle_rough_revs.txt", "a");
+	fprintf(fp, "%s %d %d\n", part.c_str(), rev, A.rtnsfcnumconverged());
+	fclose(fp);
+}
+'''
+
 
 def patch_nonsync(cfg: dict) -> str:
     """The reference's non-synchronous binary Thermal program
-    (175706/Run-04/thermal.cpp) for one configuration: one part, roughness
-    off, a fixed thermal inertia, per-revolution convergence counts logged;
-    it writes its full-precision temperatures itself
-    (binary_writeglobaltemperature, thermal.cpp:3291-3316)."""
+    (175706/Run-04/thermal.cpp) for one configuration: a fixed thermal
+    inertia (0: instantaneous equilibrium), per-revolution convergence counts
+    logged; it writes its full-precision temperatures itself
+    (binary_writeglobaltemperature, thermal.cpp:3291-3316).  Roughness off:
+    one part.  With ``roughness`` the crater model runs over ``parts`` parts
+    (thermal.cpp:4380-4401; parts after the first read the shape's shadows,
+    illumination and temperatures back from the files the first wrote) and
+    the per-part crater temperature maps are stitched into one file
+    (stitch_temperatures, thermal.cpp:104-244)."""
     src = (REF_ROOT / NONSYNC_SRC).read_text(errors="replace")
     c = cfg
-    for name, val in (("ASTNUMVTX", c["nv"]), ("ASTNUMFACE", c["nf"]), ("NUMROUGHFACE", c["nf"]), ("NUMPARTS", 1),
+    rough = int(c.get("roughness", 0))
+    parts = int(c.get("parts", 1)) if rough else 1
+    if c["nf"] % parts:
+        raise ValueError("the facet count must split evenly into parts")
+    instant = 1 if c["thermal_inertia"] == 0.0 else 0
+    for name, val in (("ASTNUMVTX", c["nv"]), ("ASTNUMFACE", c["nf"]), ("NUMROUGHFACE", c["nf"] // parts),
+                      ("NUMPARTS", parts),
                       ("PRINUMVTX", c["prinumvtx"]), ("PRINUMFACE", c["prinumface"]),
                       ("NUMPRIREV", c["prirevs"]), ("NUMSECREV", c["secrevs"]), ("NTAU", c["ntau"]), ("NX", c["nx"]),
-                      ("fixed_thermal_inertia", 1), ("instant_equib_model", 0), ("roughness_thermal_model", 0),
+                      ("fixed_thermal_inertia", 1), ("instant_equib_model", instant),
+                      ("roughness_thermal_model", rough),
                       ("load_shape_selfheating", c["selfheating"]), ("multiple_scattering", 1),
-                      ("write_roughness_temperature", 0)):
+                      ("write_roughness_temperature", rough)):
         src = _sub_const(src, name, str(val))
     src = _sub_const(src, "shape_filename", '"%s"' % c.get("shape", "shape"))
     src = _sub_const(src, "polar0", _d(c["polar"][0]))
@@ -481,26 +518,110 @@ def patch_nonsync(cfg: dict) -> str:
                         "while (A.rtnconverged()==0 && rev<ORACLE_REVCAP) {")
     j = src.find("while (A.rtnconverged()==0 && rev<ORACLE_REVCAP) {", i)
     src = _replace_from(src, j, "rev=rev+1;", "__oracle_rev(A, rev);\n\t\t\t\trev=rev+1;")
-    # the per-part roughness maps are not written: nothing to stitch
-    src = _replace_from(src, i, "\tstitch_temperatures();", "")
-    return src
+    if not rough:
+        # the per-part roughness maps are not written: nothing to stitch
+        return _replace_from(src, i, "\tstitch_temperatures();", "")
+    src = src[:i] + _NONSYNC_ROUGH_HOOKS + "\n" + src[i:]
+    i = src.find("void single_model(Asteroid &A, Surface &S) {")
+    src = _insert_after(src, i, "retrieve_GPU_roughness_illumination(A);", "\n\t\t__oracle_dump_rough_forcing(A);")
+    src = _replace_from(src, i, "while (A.rtnsfcconverged()==0 && rev<301) {",
+                        "while (A.rtnsfcconverged()==0 && rev<ORACLE_REVCAP) {")
+    j = src.find("while (A.rtnsfcconverged()==0 && rev<ORACLE_REVCAP) {", i)
+    return _replace_from(src, j, "rev=rev+1;", "__oracle_rough_rev(A, rev);\n\t\t\t\trev=rev+1;")
 
 
-def build_nonsync(cfg: dict, threads: int = 1, revcap: int = 301) -> Path:
-    """Reference non-synchronous Thermal program, scratch copy, compiled with
-    stand-ins for its (unused) roughness GPU module."""
+def _nonsync_module_defines(cfg: dict) -> list[str]:
+    parts = int(cfg.get("parts", 1))
+    return [f"-DREF_ASTNUMFACE={cfg['nf'] // parts}", f"-DREF_NTAU={cfg['ntau']}", f"-DREF_NX={cfg['nx']}"]
+
+
+def nonsync_source(cfg: dict) -> Path:
+    """Write (once) the scratch copy of the non-synchronous program for ``cfg``."""
     d = OUT_ROOT / _tag("nonsync", cfg)
     src_path = d / "thermal.cpp"
-    exe = d / ("nonsync_t%d_r%d" % (threads, revcap))
-    if exe.exists():
-        return exe
-    d.mkdir(parents=True, exist_ok=True)
     if not src_path.exists():
         if not (REF_ROOT / NONSYNC_SRC).exists():
             raise RuntimeError("reference sources unavailable and no scratch copy in " + str(d))
+        d.mkdir(parents=True, exist_ok=True)
         src_path.write_text(patch_nonsync(cfg))
+    return src_path
+
+
+def build_nonsync(cfg: dict, threads: int = 1, revcap: int = 301) -> Path:
+    """Reference non-synchronous Thermal program, scratch copy.  Roughness
+    off: linked with stand-ins for its (unused) GPU module.  Roughness on:
+    linked with the CPU restatement of that module (oracle/ref_gpu_cpu.cpp
+    with REF_NONSYNC_MODULE)."""
+    src_path = nonsync_source(cfg)
+    exe = src_path.parent / ("nonsync_t%d_r%d" % (threads, revcap))
+    if exe.exists():
+        return exe
+    if cfg.get("roughness"):
+        module = ["-DREF_NONSYNC_MODULE", *_nonsync_module_defines(cfg), str(HERE / "ref_gpu_cpu.cpp")]
+    else:
+        module = [str(HERE / "ref_nonsync_gpu_stub.cpp")]
     subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % threads, "-DORACLE_REVCAP=%d" % revcap, str(src_path),
-                    str(HERE / "ref_nonsync_gpu_stub.cpp"), "-o", str(exe)], check=True)
+                    *module, "-o", str(exe)], check=True)
+    return exe
+
+
+def build_nonsync_shim(cfg: dict, lib_dir: Path, include_dir: Path, shim: Path, precision: str = "REFERENCE",
+                       threads: int = 1, revcap: int = 301) -> Path:
+    """The non-synchronous program with its GPU module replaced by
+    binarytpm_gb300/driver/atpm_ref_nonsync_gpu_shim.cpp over libatpm."""
+    src_path = nonsync_source(cfg)
+    tag = "" if precision == "REFERENCE" else "_" + precision.lower()
+    exe = src_path.parent / ("nonsync_shim%s_t%d_r%d" % (tag, threads, revcap))
+    subprocess.run(["g++", *CXXFLAGS, *_nonsync_module_defines(cfg), "-DORACLE_THREADS=%d" % threads,
+                    "-DORACLE_REVCAP=%d" % revcap, "-DATPM_REF_GPU_PRECISION=ATPM_" + precision,
+                    "-I", str(include_dir), str(src_path), str(shim), "-L", str(lib_dir), "-latpm",
+                    "-Wl,-rpath," + str(lib_dir), "-o", str(exe)], check=True)
+    return exe
+
+
+NONSYNC_GPU_MODULE_SRC = "175706/Run-04/thermal_GPU.cu"
+
+
+def nonsync_gpu_module_source(cfg: dict) -> Path:
+    """Scratch copy of the non-synchronous program's own GPU module
+    (thermal_GPU.cu) with the program's sizes.  Two allocations get a few
+    floats of slack, nothing else changes: finite_difference reads depth row
+    NX+1 of the last facet (thermal_GPU.cu:468, one row past sfc_temp_D) and
+    sfcpartialshadow reads a 4th Sun-vector component (thermal_GPU.cu:195, one
+    float past sfc_illumvector_D at the last facet's last step); neither value
+    is used."""
+    src_path = nonsync_source(cfg)
+    out = src_path.parent / "thermal_GPU.cu"
+    if not out.exists():
+        if not (REF_ROOT / NONSYNC_GPU_MODULE_SRC).exists():
+            raise RuntimeError("reference sources unavailable and no scratch GPU module in " + str(out.parent))
+        src = (REF_ROOT / NONSYNC_GPU_MODULE_SRC).read_text(errors="replace")
+        src = _sub_const(src, "ASTNUMFACE", str(cfg["nf"] // int(cfg.get("parts", 1))))
+        src = _sub_const(src, "NTAU", str(cfg["ntau"]))
+        src = _sub_const(src, "NX", str(cfg["nx"]))
+        for alloc, pad in (("cudaMalloc((void **)&sfc_temp_D, size);", "SFCNUMFACE"),
+                           ("cudaMalloc((void **)&sfc_illumvector_D, size);", "4")):
+            if src.count(alloc) != 1:
+                raise RuntimeError("allocation not found: " + alloc)
+            src = src.replace(alloc, alloc.replace("size);", "size + %s * sizeof(float));" % pad))
+        out.write_text(src)
+    return out
+
+
+def build_nonsync_refgpu(cfg: dict, threads: int = 1, revcap: int = 301, cuda_home: str = "/usr/local/cuda") -> Path:
+    """The non-synchronous program linked with its own GPU module (scratch
+    copy of thermal_GPU.cu, nvcc for sm_103a with nvcc's defaults).  Runs only
+    on a GPU host."""
+    src_path = nonsync_source(cfg)
+    cu = nonsync_gpu_module_source(cfg)
+    d = src_path.parent
+    obj = d / "thermal_gpu_sm103a.o"
+    exe = d / ("nonsync_refgpu_t%d_r%d" % (threads, revcap))
+    subprocess.run([cuda_home + "/bin/nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w",
+                    "-c", str(cu), "-o", str(obj)], check=True)
+    subprocess.run(["g++", *CXXFLAGS, "-DORACLE_THREADS=%d" % threads, "-DORACLE_REVCAP=%d" % revcap,
+                    str(src_path), str(obj), "-L", cuda_home + "/lib64", "-lcudart",
+                    "-Wl,-rpath," + cuda_home + "/lib64", "-o", str(exe)], check=True)
     return exe
 
 

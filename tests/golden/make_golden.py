@@ -54,6 +54,16 @@ CASES = {
     "nonsync_sh_s2s1": dict(kind="nonsync", mesh=("binary", 2, 1), ntau=72, nx=8, ti=[200.0], prirevs=3, secrevs=1,
                             pole=BINARY_POLE, polar=(1.0, 0.0, 0.0), period_h=11.9, albedo=0.02, tacc=0.005,
                             selfheating=1, ir_abs=0.9),
+    # the same program with its crater model on (its GPU module over flat
+    # arrays, per-facet revolution counts, IR absorptivity 0.9), the 160
+    # facets split into 5 parts of 32 (the third part holds facets of both
+    # bodies); TI 200, and TI 0 (instantaneous equilibrium)
+    "nonsync_rough_s1s1": dict(kind="nonsync", rough=True, parts=5, mesh=("binary", 1, 1), ntau=72, nx=8,
+                               ti=[200.0], prirevs=3, secrevs=1, pole=BINARY_POLE, polar=(1.0, 0.0, 0.0),
+                               period_h=11.9, albedo=0.02, tacc=0.005, selfheating=1, ir_abs=0.9),
+    "nonsync_rough0_s1s1": dict(kind="nonsync", rough=True, parts=5, mesh=("binary", 1, 1), ntau=72, nx=8,
+                                ti=[0.0], prirevs=3, secrevs=1, pole=BINARY_POLE, polar=(1.0, 0.0, 0.0),
+                                period_h=11.9, albedo=0.02, tacc=0.005, selfheating=1, ir_abs=0.9),
     # crater partial visibility toward the observer (Visibility's GPU module)
     "vis_rough_s1s1": dict(kind="visibility", rough=True, mesh=("binary", 1, 1), ntau=48,
                            pole=BINARY_POLE, observer=(1.2, 0.1, 0.3)),
@@ -141,7 +151,34 @@ def nonsync_cfg(name: str) -> dict:
     return dict(nv=len(v), nf=len(f), prinumvtx=pv, prinumface=pf, prirevs=c["prirevs"], secrevs=c["secrevs"],
                 ntau=c["ntau"], nx=c["nx"], polar=c["polar"], rot=c["pole"], EPS=0.9,
                 rotation_period=c["period_h"] * 3600.0, bond_albedo=c["albedo"], thermal_inertia=c["ti"][0],
-                TACC=c["tacc"], scattering_accuracy=1e-4, IR_ABS=c["ir_abs"], selfheating=c["selfheating"])
+                TACC=c["tacc"], scattering_accuracy=1e-4, IR_ABS=c["ir_abs"], selfheating=c["selfheating"],
+                **(dict(roughness=1, parts=c["parts"]) if c.get("rough") else {}))
+
+
+def nonsync_rough_files(name: str) -> list[str]:
+    """Files a non-synchronous crater run writes whose bytes the parity tests
+    compare: the crater forcing and convergence counts of every part, each
+    part's crater temperature map and the stitched map."""
+    c = CASES[name]
+    ti = "%g" % c["ti"][0]
+    out = ["oracle_rough_forcing.bin", "oracle_rough_revs.txt", "shape_roughness_temperature(%s).dat" % ti]
+    out += ["shape_roughness_temperature_part_%d(%s).dat" % (k, ti) for k in range(1, c["parts"] + 1)]
+    return out
+
+
+def write_nonsync_inputs(wd: Path, name: str, fix) -> None:
+    """Input files of a non-synchronous run from its fixture: the shape, its
+    view-factor lists (empty without self-heating) and the crater files."""
+    c = CASES[name]
+    v, f = fix["vertices"], fix["facets"]
+    if c["selfheating"]:
+        write_thermal_inputs(wd, v, f, fix["dep_ptr"], fix["dep_idx"], fix["dep_vf"], fix["dep_vec"],
+                             fix["photovectors"])
+    else:
+        z = np.zeros(len(f) + 1, np.int32)
+        write_thermal_inputs(wd, v, f, z, z[:0], np.zeros(0, np.float32))
+    if c.get("rough"):
+        write_crater_files(wd, crater_texts_from(fix))
 
 
 def visibility_cfg(name: str, threads: int = 1) -> dict:
@@ -167,6 +204,10 @@ def prepare_sources() -> None:
             refbuild.thermal_source(thermal_cfg(name))
             if c.get("rough"):
                 refbuild.gpu_module_source(thermal_cfg(name))
+        if c["kind"] == "nonsync":
+            refbuild.nonsync_source(nonsync_cfg(name))
+            if c.get("rough"):
+                refbuild.nonsync_gpu_module_source(nonsync_cfg(name))
 
 
 def run_case(name: str, c: dict, threads: int = 8) -> dict:
@@ -205,11 +246,23 @@ def run_case(name: str, c: dict, threads: int = 8) -> dict:
             if c["selfheating"]:
                 out["dep_vec"] = formats.read_float_stream(wd / "shape_selfheating_vector_list.txt", 3 * len(idx))
                 out["photovectors"] = formats.read_float_stream(wd / "shape_photovectors.txt", 3 * nf)
-                write_thermal_inputs(wd, v, f, ptr, idx, vf, out["dep_vec"], out["photovectors"])
-            else:
-                z = np.zeros(nf + 1, np.int32)
-                write_thermal_inputs(wd, v, f, z, z[:0], np.zeros(0, np.float32))
+            if c.get("rough"):
+                texts = refbuild.crater_files()
+                out["crater_names"] = np.array(list(texts))
+                out["crater_texts"] = np.array(list(texts.values()))
+            write_nonsync_inputs(wd, name, out)
             refbuild.run(refbuild.build_nonsync(cfg), wd)
+            if c.get("rough"):
+                import hashlib
+                names = nonsync_rough_files(name)
+                out["files"] = np.array(names)
+                out["sha256"] = np.array([hashlib.sha256((wd / n).read_bytes()).hexdigest() for n in names])
+                rr = np.loadtxt(wd / "oracle_rough_revs.txt", ndmin=2)
+                out["rough_parts"] = rr[:, 0].astype(np.int32)
+                out["rough_counts"] = rr[:, 2].astype(np.int32)
+                T = np.fromfile(wd / ("shape_roughness_temperature(%g).dat" % c["ti"][0]), dtype=np.float32)
+                T = T[61 * 3 + 100 * 3:].reshape(nf, 100, c["ntau"])
+                out["rough_stemp1_first_last"] = np.stack([T[0], T[-1]])   # one facet of each body
             raw = np.fromfile(wd / ("shape_temperature(%g).dat" % c["ti"][0]), dtype=np.uint8)
             off = len(v) * 24 + nf * 12
             out["stemp1"] = raw[off:].view(np.float32).reshape(nf, c["ntau"]).copy()

@@ -55,11 +55,14 @@ def test_no_gpu_is_an_error_not_a_fallback():
 @pytest.mark.parametrize("header,shim,count,defines", [
     ("atpm_ref_gpu.h", "atpm_ref_gpu_shim.cpp", 27, ["-DREF_ASTNUMFACE=4", "-DREF_NTAU=8", "-DREF_NX=8"]),
     ("atpm_ref_vis_gpu.h", "atpm_ref_vis_gpu_shim.cpp", 6, ["-DREF_ASTNUMFACE=4", "-DREF_NTAU=8"]),
+    ("atpm_ref_nonsync_gpu.h", "atpm_ref_nonsync_gpu_shim.cpp", 27,
+     ["-DREF_ASTNUMFACE=4", "-DREF_NTAU=8", "-DREF_NX=8"]),
 ])
 def test_reference_gpu_module_shim_defines_every_symbol(tmp_path, header, shim, count, defines):
     """Each shim in binarytpm_gb300/driver defines, with C linkage, every
     function its header declares (the Thermal driver's 27-entry roughness
-    module, the Visibility driver's 6-entry crater-visibility module)."""
+    module, the Visibility driver's 6-entry crater-visibility module, the
+    non-synchronous program's 27-entry flat-array module)."""
     hdr = (ROOT / "include" / header).read_text()
     body = hdr[hdr.index('extern "C" {'):]
     declared = set(re.findall(r"\bvoid\s+(\w+)\s*\(", body))

@@ -73,6 +73,30 @@ def test_crater_oracle_reproduces_golden_digests(tmp_path):
     assert ref["rough_counts"][-1] == prob.nf
 
 
+@pytest.mark.parametrize("name", ["nonsync_rough_s1s1", "nonsync_rough0_s1s1"])
+def test_nonsync_crater_oracle_reproduces_golden_digests(tmp_path, name):
+    """The non-synchronous program with its crater model on (5 parts, per-facet
+    revolution counts 3 and 1, IR absorptivity 0.9), linked with the CPU
+    restatement of its GPU module, writes the bytes the golden digests record;
+    every part's crater facets converge."""
+    import hashlib
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden
+    from oracle import refbuild
+
+    _, ref = golden(name)
+    make_golden.write_nonsync_inputs(tmp_path, name, ref)
+    refbuild.run(refbuild.build_nonsync(make_golden.nonsync_cfg(name)), tmp_path)
+    for fname, want in zip(ref["files"], ref["sha256"]):
+        assert hashlib.sha256((tmp_path / str(fname)).read_bytes()).hexdigest() == str(want), fname
+    parts, counts = ref["rough_parts"], ref["rough_counts"]
+    assert sorted(set(parts.tolist())) == [1, 2, 3, 4, 5]
+    assert all(counts[parts == k][-1] == 32 for k in range(1, 6))
+
+
 def test_crater_visibility_oracle_reproduces_golden_digest(tmp_path):
     """The reference Visibility driver with crater visibility on, linked with
     the CPU restatement of its GPU module, writes the golden bytes."""
