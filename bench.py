@@ -782,8 +782,8 @@ def _tile_stats(prob, slices=False):
 
 def _roofline(kern, n, prob, hbm, bf16, kind):
     """Dominant kernel of the revolution loop: the self-heating product
-    (k_spmm_tc, tensor-core tiles plus the FP32 sparse remainder in its
-    epilogue).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
+    (k_spmm_tc over the tensor-core tiles, then k_spmm_rem over the FP32
+    sparse remainder; timed together).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
     BF16 + 4 B index) + 8 F NTAU bytes per solve, is ~52 FLOP/B, below the
     GB300 ridge (~290), so the bound is HBM: achieved = algorithmic bytes per
     launch (view factors once, shared by the batch's clones; W read and Q
@@ -816,7 +816,7 @@ def _roofline(kern, n, prob, hbm, bf16, kind):
                "note": "algorithmic bytes = nnz x 6 B + solves x 8 B x F x NTAU; executed tensor FLOP count the "
                        f"zero padding of the issued 128x16 K slices ({sl} of the {4 * tiles} in {tiles} tiles; "
                        f"{sl_lo} in the {lo} tiles with residual) and the hi/lo products; {rem} of {prob.nnz} "
-                       f"entries (cells with < {_tc_min_entries()} entries) are summed in FP32 in the epilogue"}
+                       f"entries (cells with < {_tc_min_entries()} entries) are summed in FP32 by k_spmm_rem"}
     c = kern.get("conduction")
     if c and c["ms"]:
         nx = prob.nx

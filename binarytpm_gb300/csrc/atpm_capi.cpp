@@ -270,12 +270,15 @@ void build_maps(int nf, int ntau, int solve, std::vector<int4>& w, std::vector<i
 }
 
 // FAST conduction variant: ATPM_COND_VARIANT in {1,2,3} (minimum resident
-// blocks per SM given to the register allocator), default 3 (fastest on
-// GB300 for NX = 56: 2.09 -> 1.52 ms per batched revolution)
+// blocks per SM given to the register allocator; 3 was the fastest of them
+// on GB300 for NX = 56: 2.09 -> 1.52 ms per batched revolution) or 4 (the
+// facet-range sweep as pairs of facets on the packed FP32 instructions, the
+// list and warp forms as in 3: 18.1 -> 16.8 ms per 6-revolution step of the
+// 8-inertia binary batch).  All four give bit-identical results.  Default 4.
 int cond_variant() {
     const char* e = std::getenv("ATPM_COND_VARIANT");
-    if (e && e[0] >= '1' && e[0] <= '3' && e[1] == 0) return e[0] - '0';
-    return 3;
+    if (e && e[0] >= '1' && e[0] <= '4' && e[1] == 0) return e[0] - '0';
+    return 4;
 }
 
 // Newton iteration cap of the surface boundary condition (ATPM_NEWTON_CAP,
@@ -639,6 +642,9 @@ uint64_t tune_key(const Batch& b) {
            ((uint64_t)(b.nq > 0) << 32);
 }
 
+// revolutions the autotuner times, one conduction variant each
+constexpr int kTuneRevs = 4;
+
 atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64_t* launches, int* tuned) {
     atpm_context* c = s0->ctx;
     const uint64_t key = tune_key(b);
@@ -653,18 +659,19 @@ atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64
     }
     atpm_tune_choice ch;
     const int smax = b.nq > 0 ? tc_max_stages(b.tc_nmax) : 0;
-    if (maxcap < 3) {  // too short to time: defaults
-        b.cond_variant = 3;
+    if (maxcap < kTuneRevs) {  // too short to time: defaults
+        b.cond_variant = cond_variant();
         b.tc_stages = 0;
         return ATPM_OK;
     }
     // candidates per revolution: conduction variant v, pipeline depth d
-    const int cand_v[3] = {1, 2, 3};
-    const int cand_d[3] = {smax, smax > 2 ? smax - 1 : smax, smax};
-    cudaEvent_t ev[12];
-    for (int i = 0; i < 12; ++i) CK(cudaEventCreate(&ev[i]));
+    const int cand_v[kTuneRevs] = {1, 2, 3, 4};
+    const int cand_d[kTuneRevs] = {smax, smax > 2 ? smax - 1 : smax, smax, smax};
+    cudaEvent_t ev[4 * kTuneRevs];
+    for (int i = 0; i < 4 * kTuneRevs; ++i) CK(cudaEventCreate(&ev[i]));
     int rc = 0;
-    for (int r = 0; r < 3 && !rc; ++r) {
+    int64_t nlaunch = 0;
+    for (int r = 0; r < kTuneRevs && !rc; ++r) {
         b.cond_variant = cand_v[r];
         b.tc_stages = cand_d[r];
         rc |= launch_revolution_part(b, 0, s0->st);
@@ -676,23 +683,24 @@ atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64
         rc |= launch_revolution_part(b, 3, s0->st);
         rc |= launch_revolution_part(b, 4, s0->st);
         cudaEventRecord(ev[4 * r + 3], s0->st);
+        nlaunch += kernels_per_revolution(b);
     }
     cudaError_t e = cudaStreamSynchronize(s0->st);
-    float tc[3] = {0, 0, 0}, cd[3] = {0, 0, 0};
-    for (int r = 0; r < 3 && e == cudaSuccess && !rc; ++r) {
+    float tc[kTuneRevs] = {}, cd[kTuneRevs] = {};
+    for (int r = 0; r < kTuneRevs && e == cudaSuccess && !rc; ++r) {
         cudaEventElapsedTime(&tc[r], ev[4 * r], ev[4 * r + 1]);
         cudaEventElapsedTime(&cd[r], ev[4 * r + 1], ev[4 * r + 2]);
     }
-    for (int i = 0; i < 12; ++i) cudaEventDestroy(ev[i]);
+    for (int i = 0; i < 4 * kTuneRevs; ++i) cudaEventDestroy(ev[i]);
     if (rc) return fail(ATPM_E_CUDA, "revolution launch (autotune): %s", cudaGetErrorString(cudaGetLastError()));
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "autotune: %s", cudaGetErrorString(e));
     int best = 0;
-    for (int r = 1; r < 3; ++r)
+    for (int r = 1; r < kTuneRevs; ++r)
         if (cd[r] < cd[best]) best = r;
     ch.cond_variant = cand_v[best];
     // depth smax ran in revolutions 0 and 2, smax - 1 in revolution 1
     ch.tc_stages = (smax > 2 && tc[1] < 0.5f * (tc[0] + tc[2])) ? smax - 1 : 0;
-    for (int r = 0; r < 3; ++r) ch.cond_ms[r] = cd[r];
+    for (int r = 0; r < kTuneRevs; ++r) ch.cond_ms[r] = cd[r];
     ch.tc_ms[0] = 0.5f * (tc[0] + tc[2]);
     ch.tc_ms[1] = tc[1];
     {
@@ -701,8 +709,8 @@ atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64
     }
     b.cond_variant = ch.cond_variant;
     b.tc_stages = ch.tc_stages;
-    *done_revs = 3;
-    *launches += 3 * kernels_per_revolution(b);
+    *done_revs = kTuneRevs;
+    *launches += nlaunch;
     *tuned = 1;
     return ATPM_OK;
 }

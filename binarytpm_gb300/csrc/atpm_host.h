@@ -14,9 +14,9 @@
 
 // launch configuration chosen by the autotuner for one kind of batch
 struct atpm_tune_choice {
-    int cond_variant = 3;  // FAST conduction register/occupancy variant
+    int cond_variant = 4;  // FAST conduction variant (1-3 register budgets, 4 paired facets)
     int tc_stages = 0;     // tensor-core pipeline depth (0: deepest)
-    float cond_ms[3] = {0, 0, 0};
+    float cond_ms[4] = {0, 0, 0, 0};
     float tc_ms[2] = {0, 0};
 };
 

@@ -221,16 +221,29 @@ __device__ __forceinline__ void column_revolution(const DevSolve& sv, const Batc
 // FAST + tensor-core self-heating: eps*sigma*T^4 of the new surface
 // temperature goes straight into the hi/lo BF16 tiles the next revolution's
 // product reads (atpm_spmm_tc.cu), so no separate pass re-reads stemp1.
+// FAST arithmetic is written with explicitly rounded operations (the _rn
+// intrinsics are never contracted into a multiply-add), so the scalar, the
+// warp-per-facet and the paired forms of the sweep round alike, operation by
+// operation, whatever the compiler schedules.
+// eps sigma T^4 (with the IR absorptivity folded into es_w)
+__device__ __forceinline__ float fast_w(float es_w, float t) {
+    const float t2 = __fmul_rn(t, t);
+    return __fmul_rn(es_w, __fmul_rn(t2, t2));
+}
+// the BF16 pair of W: hi = bf16(w), lo = bf16(w - hi)
+__device__ __forceinline__ __nv_bfloat16 w_lo(float w, __nv_bfloat16 hi) {
+    return __float2bfloat16_rn(__fsub_rn(w, __bfloat162float(hi)));
+}
+
 __device__ __forceinline__ void store_w(const DevSolve& sv, int f, int s, float t) {
     const int N = sv.tc_n;
-    const float t2 = t * t;
-    const float w = sv.es_w * (t2 * t2);
+    const float w = fast_w(sv.es_w, t);
     __nv_bfloat16* W = static_cast<__nv_bfloat16*>(sv.Wb);
     const size_t base = ((size_t)(f >> 6) * sv.tc_nchunks + s / N) * (size_t)2 * N * 64;
     const uint32_t o = swz((uint32_t)(s % N), (uint32_t)(f & 63));
     const __nv_bfloat16 hi = __float2bfloat16_rn(w);
     W[base + o] = hi;
-    W[base + (size_t)N * 64 + o] = __float2bfloat16_rn(w - __bfloat162float(hi));
+    W[base + (size_t)N * 64 + o] = w_lo(w, hi);
     if (sv.W32) sv.W32[(size_t)f * sv.w32_ld + s] = w;
 }
 
@@ -264,17 +277,19 @@ constexpr int kFastPrefetch = 8;  // steps of forcing / flux / previous temperat
 // (up + dn) - 2 t is formed as one fma: 2 t is exact, so this is the
 // rounding of the plain expression
 __device__ __forceinline__ float ftcs_node(float r, float up, float dn, float t) {
-    return fmaf(r, fmaf(-2.0f, t, up + dn), t);
+    return __fmaf_rn(r, __fmaf_rn(-2.0f, t, __fadd_rn(up, dn)), t);
 }
 
+// one Newton step on theta_0: sbc = (m1 (t1 - th) + a) - es TR^4 with the
+// emission folded into one multiply-add
 __device__ __forceinline__ float newton_fast(float th, float Tref, float t1, float a, float m1, float es, float es4,
                                              float& DT) {
-    const float TR = Tref + th;
-    const float t2 = TR * TR;
-    const float sbc = fmaf(m1, t1 - th, a) - es * (t2 * t2);
-    const float sbcd = fmaf(es4, t2 * TR, m1);
-    const float th1 = th + __fdividef(sbc, sbcd);
-    DT = fabsf(th1 - th);
+    const float TR = __fadd_rn(Tref, th);
+    const float t2 = __fmul_rn(TR, TR);
+    const float sbc = __fmaf_rn(-es, __fmul_rn(t2, t2), __fmaf_rn(m1, __fsub_rn(t1, th), a));
+    const float sbcd = __fmaf_rn(es4, __fmul_rn(t2, TR), m1);
+    const float th1 = __fadd_rn(th, __fdividef(sbc, sbcd));
+    DT = fabsf(__fsub_rn(th1, th));
     return th1;
 }
 
@@ -299,7 +314,7 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     const uint32_t kc = (uint32_t)(f & 63) >> 3, k7 = (uint32_t)f & 7u;
     int wn = 0;
 #pragma unroll
-    for (int i = 0; i <= NX; ++i) T[i] = temp[(size_t)i * nf + f] - Tref;
+    for (int i = 0; i <= NX; ++i) T[i] = __fsub_rn(temp[(size_t)i * nf + f], Tref);
     bool hot = false;
     int flags = 0;
     const int cap = sv.newton_cap;
@@ -332,7 +347,7 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
         S0[o] = old;
         const float t1 = T[1];
         T[1] = ftcs_node(r, T[2], T[0], t1);
-        const float a = fmaf(oma, e, q);
+        const float a = __fmaf_rn(oma, e, q);
         // Newton iterations 1 and 2 on theta_0 (T_0 = Tref + theta_0)
         float DT;
         float th1 = newton_fast(T[0], Tref, T[1], a, m1, es, es4, DT);
@@ -352,15 +367,14 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
             ++it;
         }
         T[0] = th1;
-        const float Tsurf = Tref + th1;
+        const float Tsurf = __fadd_rn(Tref, th1);
         S1[o] = Tsurf;
         if (Wb) {
-            const float t2s = Tsurf * Tsurf;
-            const float w = sv.es_w * (t2s * t2s);
+            const float w = fast_w(sv.es_w, Tsurf);
             const uint32_t off = (uint32_t)wn * 64u + ((kc ^ ((uint32_t)wn & 7u)) << 3) + k7;
             const __nv_bfloat16 hi = __float2bfloat16_rn(w);
             Wb[wrow + off] = hi;
-            Wb[wrow + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
+            Wb[wrow + (size_t)N * 64 + off] = w_lo(w, hi);
             if (++wn == N) { wn = 0; wrow += chunk; }
             if (w32row) {
                 w8[s & 7][lt] = w;
@@ -372,7 +386,7 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
             }
         }
         T[NX] = T[NX - 1];
-        hot = hot || (fabsf(Tsurf - old) >= tacc);
+        hot = hot || (fabsf(__fsub_rn(Tsurf, old)) >= tacc);
         // refill the slot just read (its words are consumed) with step s + D
         if (s + D < ntau) {
             const size_t od = o + (size_t)D * nf;
@@ -386,10 +400,178 @@ __device__ __forceinline__ void column_revolution_fast(const DevSolve& sv, int f
     cp_async_wait<0>();
     if (w32row)  // the steps after the last full group of 8
         for (int s = ntau & ~7; s < ntau; ++s) w32row[s] = w8[s & 7][lt];
-    if (!isfinite(T[0] + Tref)) flags |= ST_NONFINITE;
+    if (!isfinite(__fadd_rn(T[0], Tref))) flags |= ST_NONFINITE;
 #pragma unroll
-    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = Tref + T[i];
+    for (int i = 0; i <= NX; ++i) temp[(size_t)i * nf + f] = __fadd_rn(Tref, T[i]);
     sv.hot[f] = hot ? 1 : 0;
+    if (flags) atomicOr(sv.status, flags);
+}
+
+// FAST, two adjacent facets per thread.  The sweep is issue-bound, so the
+// pair is advanced with the packed FP32 instructions (fma/add/mul .f32x2):
+// each lane of a pair is the scalar sweep's operation sequence with the same
+// roundings, so both facets end bit-identical to column_revolution_fast.  The
+// two facets' words sit side by side in every [step][facet] and
+// [depth][facet] array (f even, nf even), so their loads and stores are
+// 8-byte accesses and the two W tile entries one BF16x2 store.  The Newton
+// solve runs while either lane still needs a step; a lane that has stopped
+// keeps its value (per-lane select), so each facet takes its own iterations.
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// a - b with one rounding (b * -1 is exact), the value of __fsub_rn(a, b)
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+
+__device__ __forceinline__ float2 ftcs_node2(float2 r, float2 up, float2 dn, float2 t) {
+    return f2fma(r, f2fma(make_float2(-2.0f, -2.0f), t, f2add(up, dn)), t);
+}
+
+// newton_fast on both lanes (nes = -es)
+__device__ __forceinline__ float2 newton_fast2(float2 th, float2 Tref, float2 t1, float2 a, float2 m1, float2 nes,
+                                               float2 es4, float2& DT) {
+    const float2 TR = f2add(Tref, th);
+    const float2 t2 = f2mul(TR, TR);
+    const float2 sbc = f2fma(nes, f2mul(t2, t2), f2fma(m1, f2sub(t1, th), a));
+    const float2 sbcd = f2fma(es4, f2mul(t2, TR), m1);
+    const float2 th1 = f2add(th, make_float2(__fdividef(sbc.x, sbcd.x), __fdividef(sbc.y, sbcd.y)));
+    const float2 d = f2sub(th1, th);
+    DT = make_float2(fabsf(d.x), fabsf(d.y));
+    return th1;
+}
+
+__device__ __forceinline__ void cp_async8(float2* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
+template <int NX>
+__device__ __forceinline__ void column_revolution_fast2(const DevSolve& sv, int f) {
+    const int nf = sv.nf, ntau = sv.ntau;
+    const bool sec0 = f >= sv.fsplit, sec1 = f + 1 >= sv.fsplit;
+    const float2 r = make_float2(sec0 ? sv.r2 : sv.r, sec1 ? sv.r2 : sv.r);
+    const float2 m1 = make_float2(sec0 ? sv.m1_2 : sv.m1, sec1 ? sv.m1_2 : sv.m1);
+    const float2 oma = make_float2(sv.oma, sv.oma), nes = make_float2(-sv.es, -sv.es),
+                 es4 = make_float2(sv.es4, sv.es4), esw = make_float2(sv.es_w, sv.es_w);
+    const float tacc = sv.tacc, tacc10 = sv.tacc10;
+    float* temp = static_cast<float*>(sv.temp);
+    const float* __restrict__ E = static_cast<const float*>(sv.E);
+    const float* __restrict__ Q = static_cast<const float*>(sv.Q);
+    float* __restrict__ S0 = static_cast<float*>(sv.stemp0);
+    float* __restrict__ S1 = static_cast<float*>(sv.stemp1);
+    float2 T[NX + 1];
+    const float2 Tref = *reinterpret_cast<const float2*>(temp + (size_t)NX * nf + f);
+    __nv_bfloat16* Wb = static_cast<__nv_bfloat16*>(sv.Wb);
+    const int N = sv.tc_n;
+    const size_t chunk = (size_t)2 * N * 64;
+    size_t wrow = Wb ? (size_t)(f >> 6) * sv.tc_nchunks * chunk : 0;
+    const uint32_t kc = (uint32_t)(f & 63) >> 3, k7 = (uint32_t)f & 7u;  // f even: f + 1 is the next BF16
+    int wn = 0;
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) T[i] = f2sub(*reinterpret_cast<const float2*>(temp + (size_t)i * nf + f), Tref);
+    bool hot0 = false, hot1 = false;
+    int flags = 0;
+    const int cap = sv.newton_cap;
+    constexpr int D = kFastPrefetch;
+    __shared__ float2 pre2[D][3][64];
+    __shared__ float2 w8p[8][64];
+    float* W32 = Wb ? sv.W32 : nullptr;
+    float* w32r0 = W32 ? W32 + (size_t)f * sv.w32_ld : nullptr;
+    float* w32r1 = W32 ? w32r0 + sv.w32_ld : nullptr;
+    const int lt = threadIdx.x;
+    for (int j = 0; j < D; ++j) {
+        if (j < ntau) {
+            const size_t oj = (size_t)j * nf + f;
+            cp_async8(&pre2[j][0][lt], E + oj);
+            cp_async8(&pre2[j][1][lt], Q + oj);
+            cp_async8(&pre2[j][2][lt], S1 + oj);
+        }
+        cp_async_commit();
+    }
+    size_t o = (size_t)f;
+    int slot = 0;
+    for (int s = 0; s < ntau; ++s, o += nf) {
+        cp_async_wait<D - 1>();
+        const float2 e = pre2[slot][0][lt], q = pre2[slot][1][lt], old = pre2[slot][2][lt];
+        *reinterpret_cast<float2*>(S0 + o) = old;
+        const float2 t1 = T[1];
+        T[1] = ftcs_node2(r, T[2], T[0], t1);
+        const float2 a = f2fma(oma, e, q);
+        float2 DT;
+        float2 th1 = newton_fast2(T[0], Tref, T[1], a, m1, nes, es4, DT);
+        {
+            const bool n0 = DT.x >= tacc10, n1 = DT.y >= tacc10;
+            if (n0 || n1) {
+                float2 d2;
+                const float2 t = newton_fast2(th1, Tref, T[1], a, m1, nes, es4, d2);
+                if (n0) { th1.x = t.x; DT.x = d2.x; }
+                if (n1) { th1.y = t.y; DT.y = d2.y; }
+            }
+        }
+        float2 tm = t1;
+#pragma unroll
+        for (int i = 2; i < NX; ++i) {
+            const float2 ti = T[i];
+            T[i] = ftcs_node2(r, T[i + 1], tm, ti);
+            tm = ti;
+        }
+        for (int it = 2;; ++it) {
+            const bool n0 = DT.x >= tacc10, n1 = DT.y >= tacc10;
+            if (!n0 && !n1) break;
+            if (it >= cap) { flags |= ST_NEWTON_CAP; break; }
+            float2 d2;
+            const float2 t = newton_fast2(th1, Tref, T[1], a, m1, nes, es4, d2);
+            if (n0) { th1.x = t.x; DT.x = d2.x; }
+            if (n1) { th1.y = t.y; DT.y = d2.y; }
+        }
+        T[0] = th1;
+        const float2 Tsurf = f2add(Tref, th1);
+        *reinterpret_cast<float2*>(S1 + o) = Tsurf;
+        if (Wb) {
+            const float2 t2s = f2mul(Tsurf, Tsurf);
+            const float2 w = f2mul(esw, f2mul(t2s, t2s));
+            const uint32_t off = (uint32_t)wn * 64u + ((kc ^ ((uint32_t)wn & 7u)) << 3) + k7;
+            const __nv_bfloat162 hi = __floats2bfloat162_rn(w.x, w.y);
+            const float2 lo = f2sub(w, __bfloat1622float2(hi));
+            *reinterpret_cast<__nv_bfloat162*>(Wb + wrow + off) = hi;
+            *reinterpret_cast<__nv_bfloat162*>(Wb + wrow + (size_t)N * 64 + off) = __floats2bfloat162_rn(lo.x, lo.y);
+            if (++wn == N) { wn = 0; wrow += chunk; }
+            if (w32r0) {
+                w8p[s & 7][lt] = w;
+                if ((s & 7) == 7) {
+                    float4* d0 = reinterpret_cast<float4*>(w32r0 + (s - 7));
+                    float4* d1 = reinterpret_cast<float4*>(w32r1 + (s - 7));
+                    d0[0] = make_float4(w8p[0][lt].x, w8p[1][lt].x, w8p[2][lt].x, w8p[3][lt].x);
+                    d0[1] = make_float4(w8p[4][lt].x, w8p[5][lt].x, w8p[6][lt].x, w8p[7][lt].x);
+                    d1[0] = make_float4(w8p[0][lt].y, w8p[1][lt].y, w8p[2][lt].y, w8p[3][lt].y);
+                    d1[1] = make_float4(w8p[4][lt].y, w8p[5][lt].y, w8p[6][lt].y, w8p[7][lt].y);
+                }
+            }
+        }
+        T[NX] = T[NX - 1];
+        const float2 dT = f2sub(Tsurf, old);
+        hot0 = hot0 || (fabsf(dT.x) >= tacc);
+        hot1 = hot1 || (fabsf(dT.y) >= tacc);
+        if (s + D < ntau) {
+            const size_t od = o + (size_t)D * nf;
+            cp_async8(&pre2[slot][0][lt], E + od);
+            cp_async8(&pre2[slot][1][lt], Q + od);
+            cp_async8(&pre2[slot][2][lt], S1 + od);
+        }
+        cp_async_commit();
+        if (++slot == D) slot = 0;
+    }
+    cp_async_wait<0>();
+    if (w32r0)
+        for (int s = ntau & ~7; s < ntau; ++s) {
+            w32r0[s] = w8p[s & 7][lt].x;
+            w32r1[s] = w8p[s & 7][lt].y;
+        }
+    const float2 t0 = f2add(T[0], Tref);
+    if (!isfinite(t0.x) || !isfinite(t0.y)) flags |= ST_NONFINITE;
+#pragma unroll
+    for (int i = 0; i <= NX; ++i) *reinterpret_cast<float2*>(temp + (size_t)i * nf + f) = f2add(Tref, T[i]);
+    sv.hot[f] = hot0 ? 1 : 0;
+    sv.hot[f + 1] = hot1 ? 1 : 0;
     if (flags) atomicOr(sv.status, flags);
 }
 
@@ -425,8 +607,8 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
     const int N = sv.tc_n;
     const int na = 2 * lane, nb = 2 * lane + 1;
     const float Tref = temp[(size_t)NX * nf + f];
-    float Ta = na <= NX ? temp[(size_t)na * nf + f] - Tref : 0.0f;
-    float Tb = nb <= NX ? temp[(size_t)nb * nf + f] - Tref : 0.0f;
+    float Ta = na <= NX ? __fsub_rn(temp[(size_t)na * nf + f], Tref) : 0.0f;
+    float Tb = nb <= NX ? __fsub_rn(temp[(size_t)nb * nf + f], Tref) : 0.0f;
     bool hot = false;
     int flags = 0;
     const int cap = sv.newton_cap;
@@ -437,7 +619,7 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
     float ca = 0.0f, co = 0.0f;
     if (lane < ntau) {
         const size_t o = (size_t)lane * nf + f;
-        ca = fmaf(oma, E[o], Q[o]);
+        ca = __fmaf_rn(oma, E[o], Q[o]);
         co = S1[o];
     }
     for (int s0 = 0; s0 < ntau; s0 += 32) {
@@ -484,9 +666,9 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
             t2_u = t2n;
             t3_u = t3n;
             a = a_next;
-            const float Tsurf = Tref + th1;
+            const float Tsurf = __fadd_rn(Tref, th1);
             if (lane == j) ts = Tsurf;
-            hot = hot || (fabsf(Tsurf - old) >= tacc);
+            hot = hot || (fabsf(__fsub_rn(Tsurf, old)) >= tacc);
         }
         if (lane < nstep) {
             const int s = s0 + lane;
@@ -494,27 +676,26 @@ __device__ __forceinline__ void column_revolution_warp(const DevSolve& sv, int f
             S0[o] = co;
             S1[o] = ts;
             if (Wb) {
-                const float t2s = ts * ts;
-                const float w = sv.es_w * (t2s * t2s);
+                const float w = fast_w(sv.es_w, ts);
                 const size_t base = ((size_t)(f >> 6) * sv.tc_nchunks + s / N) * (size_t)2 * N * 64;
                 const uint32_t off = swz((uint32_t)(s % N), (uint32_t)(f & 63));
                 const __nv_bfloat16 hi = __float2bfloat16_rn(w);
                 Wb[base + off] = hi;
-                Wb[base + (size_t)N * 64 + off] = __float2bfloat16_rn(w - __bfloat162float(hi));
+                Wb[base + (size_t)N * 64 + off] = w_lo(w, hi);
                 if (sv.W32) sv.W32[(size_t)f * sv.w32_ld + s] = w;  // 32 lanes: one 128-byte row segment
             }
         }
-        ca = fmaf(oma, ne, nq);
+        ca = __fmaf_rn(oma, ne, nq);
         co = no;
     }
-    if (!isfinite(th_u + Tref)) flags |= ST_NONFINITE;
+    if (!isfinite(__fadd_rn(th_u, Tref))) flags |= ST_NONFINITE;
     if (lane == 0) Ta = th_u;  // node 0 lives in the uniform copy during the sweep
     if constexpr ((NX & 1) == 0) {
         const float bot = __shfl_sync(FULL, Tb, (NX - 1) >> 1);  // node NX-1
         if (lane == (NX >> 1)) Ta = bot;
     }
-    if (na <= NX) temp[(size_t)na * nf + f] = Tref + Ta;
-    if (nb <= NX) temp[(size_t)nb * nf + f] = Tref + Tb;
+    if (na <= NX) temp[(size_t)na * nf + f] = __fadd_rn(Tref, Ta);
+    if (nb <= NX) temp[(size_t)nb * nf + f] = __fadd_rn(Tref, Tb);
     if (lane == 0) {
         sv.hot[f] = hot ? 1 : 0;
         if (flags) atomicOr(sv.status, flags);
@@ -601,6 +782,17 @@ __device__ __forceinline__ void column_equilibrium(const DevSolve& sv, const Bat
     sv.hot[f] = hot ? 1 : 0;
 }
 
+// the solve sweeps its list of active facets this revolution (at most half
+// of them active, freeze protocol, list built for this revolution)
+__device__ __forceinline__ bool list_mode(const Batch& b, const DevSolve& sv) {
+    const int rev = sv.ctl->rev;
+    return b.warp_tail && sv.freeze && rev >= 7 && sv.act_cnt[2 + (rev & 1)] == rev && 2 * sv.act_cnt[rev & 1] <= sv.nf;
+}
+// the facet-range sweep of this solve runs as pairs (variant 4, even facet count)
+__device__ __forceinline__ bool pairs_here(const Batch& b, const DevSolve& sv) {
+    return b.cond_variant == 4 && (sv.nf & 1) == 0;
+}
+
 // MINB: minimum resident blocks per SM requested from the register allocator
 // (FAST only; the variants trade registers for occupancy, picked at run time)
 template <int MODE, int NX, int MINB = 1>
@@ -615,8 +807,7 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
             // list of active facets instead of its facet range, so active
             // facets fill whole warps and the remaining blocks exit
             const int rev = sv.ctl->rev;
-            if (b.warp_tail && sv.freeze && rev >= 7 && sv.act_cnt[2 + (rev & 1)] == rev &&
-                2 * sv.act_cnt[rev & 1] <= sv.nf) {
+            if (list_mode(b, sv)) {
                 const int k = fb.y + threadIdx.x;
                 if (k >= sv.act_cnt[rev & 1]) return;
                 column_revolution_fast<NX>(sv, sv.act_list[(size_t)(rev & 1) * sv.nf + k]);
@@ -626,6 +817,11 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
     }
     const int f = fb.y + threadIdx.x;
     if (f >= sv.nf) return;
+    if constexpr (MODE == MODE_FAST) {
+        // k_conduction_pairs sweeps the pairs whose facets are both active;
+        // a facet whose partner is frozen is swept here
+        if (sv.ti != 0.0f && pairs_here(b, sv) && !(sv.freeze && sv.conv[f ^ 1])) return;
+    }
     const bool inst = (MODE == MODE_FP64) ? (sv.ti_d == 0.0) : (sv.ti == 0.0f);
     if (inst) { column_equilibrium<MODE>(sv, b, f); return; }
     if (sv.freeze && sv.conv[f]) return;
@@ -633,6 +829,22 @@ __global__ void __launch_bounds__(128, MINB) k_conduction(Batch b) {
         column_revolution_fast<NX>(sv, f);
     }
     else column_revolution<MODE, NX>(sv, b, f);
+}
+
+// FAST conduction variant 4: the facet-range sweep (every revolution before
+// the active-list and warp-per-facet forms take over) as pairs of adjacent
+// facets, 64 threads per 128-facet block.  Only pairs with both facets
+// active are swept here: k_conduction, launched beside it, takes a facet
+// whose partner is frozen (the freeze flags do not change during the sweep),
+// and every facet of a solve with an odd facet count.
+template <int NX>
+__global__ void __launch_bounds__(64, 4) k_conduction_pairs(Batch b) {
+    const int2 fb = b.fmap[blockIdx.x];
+    const DevSolve& sv = b.tab[fb.x];
+    if (!sv.ctl->active || sv.ti == 0.0f || !pairs_here(b, sv) || warp_tail_now(b) || list_mode(b, sv)) return;
+    const int f = fb.y + 2 * threadIdx.x;
+    if (f >= sv.nf || (sv.freeze && (sv.conv[f] || sv.conv[f + 1]))) return;
+    column_revolution_fast2<NX>(sv, f);
 }
 
 // -------------------------------------------------------------- convergence
@@ -785,7 +997,18 @@ static int launch_rev_part(const Batch& b, int part, cudaStream_t st) {
         case 1: if (b.nw > 0) k_selfheat_q<MODE><<<b.nw, dim3(32, 32), 0, st>>>(b); break;
         case 2:
             if (MODE == MODE_FAST) k_tail_mode<<<1, 32, 0, st>>>(b);
-            if (MODE == MODE_FAST && b.cond_variant == 3) {
+            if (MODE == MODE_FAST && b.cond_variant == 4) {
+                switch (b.nx) {
+#define NX_CASE(n)                                                \
+    case n:                                                       \
+        k_conduction<MODE, n, 3><<<b.nfb, 128, 0, st>>>(b);       \
+        k_conduction_pairs<n><<<b.nfb, 64, 0, st>>>(b);           \
+        break;
+                    NX_LIST(NX_CASE)
+#undef NX_CASE
+                    default: return 1;
+                }
+            } else if (MODE == MODE_FAST && b.cond_variant == 3) {
                 switch (b.nx) {
 #define NX_CASE(n) case n: k_conduction<MODE, n, 3><<<b.nfb, 128, 0, st>>>(b); break;
                     NX_LIST(NX_CASE)
@@ -838,7 +1061,8 @@ int kernels_per_revolution(const Batch& b) {
     const bool tc = b.mode == MODE_FAST && b.nq > 0;
     // k_tc_compact + k_spmm_tc (+ k_spmm_rem), or W + Q
     const int selfheat = tc ? 2 + (b.rem_nmb > 0 ? 1 : 0) : (b.nw > 0 ? 2 : 0);
-    const int conduction = b.mode == MODE_FAST ? 3 : 1;  // + k_tail_mode, k_conduction_warp
+    // + k_tail_mode, k_conduction_warp (+ k_conduction_pairs)
+    const int conduction = b.mode == MODE_FAST ? (b.cond_variant == 4 ? 4 : 3) : 1;
     return selfheat + conduction + 2;                    // + k_converge, k_advance
 }
 

@@ -1,8 +1,11 @@
-"""The autotuner's knobs (conduction register variant, tensor-core pipeline
-depth) change launch configurations only: a FAST batch gives bit-identical
-temperatures and convergence counts with the tuner on, off, and with each
-variant forced; the first batch of a kind times the candidates on its first
-three revolutions and later batches of that kind reuse the choice."""
+"""The autotuner's knobs (conduction variant: register/occupancy variants 1-3
+and the paired-facet sweep 4; tensor-core pipeline depth) change launch
+configurations only: a FAST batch gives bit-identical temperatures and
+convergence counts with the tuner on, off, and with each variant forced
+(the run goes to convergence, so the active-list and warp-per-facet forms
+and pairs with one frozen facet are exercised too); the first batch of a
+kind times the candidates on its first four revolutions and later batches of
+that kind reuse the choice."""
 import os
 
 import numpy as np
@@ -44,12 +47,12 @@ def test_autotune_choices_do_not_change_results(gpu_ctx):
     prob, ref = golden("binary_s3s1")
     ctx = lib.Context(0)   # a fresh context: nothing tuned yet
     t0, c0, cfg0 = _batch(ctx, prob, ref, {"ATPM_AUTOTUNE": "1"})
-    assert cfg0[2] and cfg0[0] in (1, 2, 3)
+    assert cfg0[2] and cfg0[0] in (1, 2, 3, 4)
     t1, c1, cfg1 = _batch(ctx, prob, ref, {"ATPM_AUTOTUNE": "1"})
     assert not cfg1[2] and cfg1[:2] == cfg0[:2]
     assert np.array_equal(t0.view(np.uint32), t1.view(np.uint32))
     assert all(np.array_equal(a, b) for a, b in zip(c1, c0))
-    for v in ("1", "2", "3"):
+    for v in ("1", "2", "3", "4"):
         t, cnt, cfg = _batch(ctx, prob, ref, {"ATPM_AUTOTUNE": "0", "ATPM_COND_VARIANT": v})
         assert cfg[0] == int(v) and not cfg[2]
         assert np.array_equal(t.view(np.uint32), t0.view(np.uint32))
