@@ -415,6 +415,8 @@ def main():
     ap.add_argument("--prepare", action="store_true", help="write the reference scratch copy and exit")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving run (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving run (1/s)")
+    ap.add_argument("--sweep-solves", type=int, default=256,
+                    help="solves in the batched-sweep run (mixed sizes, albedos, inertias; 0: skip)")
     ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
     ap.add_argument("--precision-stress", type=int, default=0, metavar="SUBDIV",
                     help="run the precision-stress configuration with this primary subdivision (6: 81,920 facets)")
@@ -497,7 +499,7 @@ def main():
     cond_v, tc_depth, _ = s0.last_run_config()
     launch_config = {"conduction_variant": cond_v, "tc_pipeline_depth": tc_depth,
                      "chosen_by": "autotuner: the first batch of this kind (a warm-up step) timed the candidates "
-                                  "on its first 3 revolutions; results do not depend on the choice"}
+                                  "on its first 4 revolutions; results do not depend on the choice"}
 
     # per-kernel durations of one instrumented (all-active) revolution
     kern = lib.profile_revolution(solves)
@@ -521,6 +523,7 @@ def main():
 
     serve = serving(ctx, args.serve_requests, args.serve_rate) if args.serve_requests > 0 else None
     vis = None if args.no_visibility else visibility(ctx)
+    sweep = batched_sweep(ctx, args.sweep_solves) if args.sweep_solves > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -549,6 +552,7 @@ def main():
                         "what": f"serving: submit to result, Poisson arrivals {serve['arrival_rate_per_s']}/s, "
                                 f"{serve['requests']} requests"} if serve else None),
         "serving": serve,
+        "batched_sweep": sweep,
         "visibility": vis,
         "energy_balance_fp64": energy,
         "kernels_ms": kern,
@@ -753,6 +757,101 @@ def serving(ctx, n_requests: int, rate: float, seed: int = 5):
             "shape_registration_s": register_s, "mix": mix,
             "what": "continuous batching, HBM-budget admission (160 GB, 128 slots, 8 revolutions per tick), "
                     "state resident on the device, solves pooled per shape"}
+
+
+CRATER_FIXTURE = ROOT / "tests" / "golden" / "rough_s1s1.npz"  # carries the reference's crater model files
+
+
+def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: int = 1280):
+    """The batched-sweep configuration: ``n_solves`` binary solves advanced in
+    one batch (every kernel launch spans all of them).  Each solve: a primary
+    icosphere of subdivision 3, 4 or 5 (1,280 / 5,120 / 20,480 facets,
+    equally likely) with a subdivision-3 secondary, thermal inertia
+    log-uniform in [10, 2000] SI, Bond albedo uniform in [0.01, 0.2] (its own
+    scattering), NX = 48, NTAU = 720, FAST, revolutions 0-5 of the reference
+    protocol.  Each solve is a device clone of its shape's prototype (shared
+    view-factor tiles), with its own albedo and scattering.
+
+    Roughness (hemispherical craters of 100 sub-facets, the reference's crater
+    model; each solve draws a covering fraction in [0, 1] that weights the
+    rough flux against the smooth one): one solve of each primary size runs
+    the crater model natively -- its forcing from the solve on the device,
+    partial shadows, scattering, global heating from the batch's final
+    temperatures, starting temperatures, then ``rough_revs`` crater
+    revolutions -- in parts of ``part`` facets through one crater object,
+    timed as sub-facet-steps/s."""
+    from binarytpm_gb300 import formats, lib, workloads
+
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    protos = {}
+    for p in (3, 4, 5):
+        prob = workloads.binary_problem(ctx, p_subdiv=p, s_subdiv=3, nx=48)
+        s = lib.Solve(ctx, prob, precision=lib.FAST, revcap=HEADLINE_REVS)
+        s.geometry_shadow()
+        protos[p] = (prob, s)
+    subs = rng.integers(3, 6, size=n_solves)
+    tis = np.exp(rng.uniform(np.log(10.0), np.log(2000.0), size=n_solves))
+    albs = rng.uniform(0.01, 0.2, size=n_solves)
+    fracs = rng.uniform(0.0, 1.0, size=n_solves)
+    solves = []
+    for p, ti, a in zip(subs, tis, albs):
+        c = protos[int(p)][1].clone()
+        c.set_albedo(float(a))
+        c.scattering()
+        c.set_thermal_inertia(float(ti))
+        c.initialise_temperatures()
+        solves.append(c)
+    setup_s = time.perf_counter() - t0
+    counts = lib.batch_run(solves)
+    ms, launches, fs = solves[0].last_run_stats()
+    out = {"solves": n_solves, "nx": 48, "ntau": 720, "revolutions_per_solve": HEADLINE_REVS,
+           "mix": {f"primary_subdiv{p}": int((subs == p).sum()) for p in (3, 4, 5)},
+           "facets": int(sum(protos[int(p)][0].nf for p in subs)),
+           "facet_steps": int(fs), "device_ms": ms, "facet_steps_per_s": fs / (ms / 1e3),
+           "gpu_launches": int(launches), "setup_s": setup_s,
+           "all_active": all(len(c) == HEADLINE_REVS for c in counts)}
+    # roughness: one solve of each primary size, crater model in parts
+    fx = np.load(CRATER_FIXTURE)
+    texts = {str(k): str(v) for k, v in zip(fx["crater_names"], fx["crater_texts"])}
+    cv, cf, V = formats.crater_model(texts["new_crater2.txt"], texts["new_crater2_selfheating_list.txt"])
+    crater = lib.Crater(ctx, part, 720, 48, precision=lib.FAST)
+    crater.set_surface(cv, cf, V, 11.9 * 3600.0)
+    forcing_s, rev_s, sub_steps, sampled = 0.0, 0.0, 0, []
+    for p in (3, 4, 5):
+        i = int(np.flatnonzero(subs == p)[0])
+        s, prob = solves[i], protos[p][0]
+        alb = np.full(part, albs[i], np.float32)
+        for f0 in range(0, prob.nf, part):
+            tf = time.perf_counter()
+            crater.forcing(s, f0, prob.meta["dep_vec"])
+            crater.set_properties(np.zeros(part, np.uint8), alb, np.full(part, tis[i], np.float32))
+            crater.partial_shadow()
+            crater.scattering(s.solar(), prob.scattering_accuracy, multiple=True)
+            crater.global_heating(s, f0)
+            crater.initialise_temperatures(prob.emissivity, 5.67e-8)
+            tr = time.perf_counter()
+            for _ in range(rough_revs):
+                crater.inertia_difference(prob.emissivity, 5.67e-8, prob.tacc)
+            crater.update_converged(prob.tacc)
+            rev_s += time.perf_counter() - tr
+            forcing_s += tr - tf
+            sub_steps += part * 100 * 720 * rough_revs
+        sampled.append({"primary_subdiv": p, "facets": prob.nf, "thermal_inertia": float(tis[i]),
+                        "albedo": float(albs[i]), "roughness_fraction": float(fracs[i])})
+    crater.close()
+    out["rough"] = {"sampled": sampled, "part_facets": part, "revolutions": rough_revs,
+                    "sub_facet_steps": sub_steps, "sub_facet_steps_per_s": sub_steps / rev_s,
+                    "forcing_s": forcing_s,
+                    "what": "crater model run natively per part of the sampled solves: forcing on the device from "
+                            "the solve (sub-facet geometry, global view factors, illumination and heating), partial "
+                            "shadows, scattering, starting temperatures (forcing_s), then crater revolutions "
+                            "(host clock around synchronous calls)"}
+    for s in solves:
+        s.close()
+    for _, s in protos.values():
+        s.close()
+    return out
 
 
 FP64_TI = [200.0, 2000.0]

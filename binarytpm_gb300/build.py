@@ -21,7 +21,7 @@ LIB = PKG / "libatpm.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["atpm_thermal.cu", "atpm_scatter.cu", "atpm_geom.cu", "atpm_viewfactor.cu", "atpm_spmm_tc.cu", "atpm_crater.cu", "atpm_flux.cu"]
+CU_SOURCES = ["atpm_thermal.cu", "atpm_scatter.cu", "atpm_geom.cu", "atpm_viewfactor.cu", "atpm_spmm_tc.cu", "atpm_crater.cu", "atpm_crater_forcing.cu", "atpm_flux.cu"]
 CPP_SOURCES = ["atpm_capi.cpp", "atpm_powtab.cpp", "atpm_vfapi.cpp", "atpm_server.cpp", "atpm_crater_api.cpp"]
 
 

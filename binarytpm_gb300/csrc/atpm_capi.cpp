@@ -1259,6 +1259,45 @@ ATPM_API atpm_status atpm_geometry_shadow(atpm_solve* s) {
     return ATPM_OK;
 }
 
+// The crater model's Sun vectors and facet shadow flags of facets f0 ..
+// f0 + nfc - 1 into device arrays, from the solve's geometry parameters and
+// shadows (asteroidgeometry, main.cpp:894-1030): the vertex positions of every
+// step are recomputed, as atpm_geometry_shadow does, into a scratch buffer.
+extern "C++" {
+atpm_status atpm::solve_crater_sun(atpm_solve* s, int f0, int nfc, float* sun, int* shadow, cudaStream_t st) {
+    const atpm_params& P = s->P;
+    const int ntau = P.ntau;
+    GeomWork g{};
+    std::vector<double> rot, rot2;
+    geometry_tables(P, g.tm, g.car, rot, s->revs_p);
+    geometry_tables(P, g.tm, g.car, rot2, s->revs_s);
+    rot.insert(rot.end(), rot2.begin(), rot2.end());
+    g.vsplit = s->sec_vertex >= 0 ? s->sec_vertex : s->nv;
+    if (s->has_position)
+        for (int k = 0; k < 3; ++k) g.car[k] = s->position[k];
+    const size_t hp = align256((size_t)s->nv * ntau * 24);
+    void* tmp = nullptr;
+    CK(cudaMallocAsync(&tmp, hp + rot.size() * 8, st));
+    g.hp = static_cast<double*>(tmp);
+    g.rot = reinterpret_cast<double*>(static_cast<char*>(tmp) + hp);
+    g.rot2 = g.rot + 2 * (size_t)ntau;
+    cudaError_t e = cudaMemcpyAsync((void*)g.rot, rot.data(), rot.size() * 8, cudaMemcpyHostToDevice, st);
+    int rc = e == cudaSuccess ? launch_crater_sun(s->ds, g, f0, nfc, sun, shadow, st) : 0;
+    cudaFreeAsync(tmp, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);  // `rot` must outlive the copy
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "crater geometry upload: %s", cudaGetErrorString(e));
+    if (rc) return fail(ATPM_E_CUDA, "crater geometry launch: %s", cudaGetErrorString(cudaGetLastError()));
+    if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "crater geometry: %s", cudaGetErrorString(e2));
+    return ATPM_OK;
+}
+}  // extern "C++"
+
+ATPM_API atpm_status atpm_solve_solar(const atpm_solve* s, float* solar) {
+    if (!s || !solar) return fail(ATPM_E_INVALID, "null argument");
+    *solar = s->ds.solar;
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_scattering(atpm_solve* s) {
     if (!s) return fail(ATPM_E_INVALID, "null solve");
     CK(cudaSetDevice(s->ctx->device));
@@ -1328,6 +1367,19 @@ ATPM_API atpm_status atpm_set_thermal_inertia(atpm_solve* s, float ti) {
     CK(cudaMemsetAsync(s->ds.counts, 0, (size_t)s->P.revcap * 4, s->st));
     CK(reset_active_lists(s));
     CK(cudaStreamSynchronize(s->st));
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_set_albedo(atpm_solve* s, float albedo) {
+    if (!s) return fail(ATPM_E_INVALID, "null solve");
+    if (!(albedo >= 0.0f && albedo < 1.0f)) return fail(ATPM_E_INVALID, "albedo %g", (double)albedo);
+    CK(cudaSetDevice(s->ctx->device));
+    s->P.albedo = albedo;
+    set_scalars(s, s->ti);
+    atpm_status r = upload_table(s);
+    if (r) return r;
+    // the scattered illumination depends on the albedo: scatter again
+    s->have_forcing = false;
     return ATPM_OK;
 }
 

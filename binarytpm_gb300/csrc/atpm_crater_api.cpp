@@ -23,6 +23,15 @@ struct atpm_crater {
     float* numrevs = nullptr;  // [nf] revolutions per model period (non-synchronous binaries), once set
     float PI = 0.0f, rot = 0.0f;
     bool have_model = false;
+    // forcing from a solve (atpm_crater_forcing): sub-facet normals, the
+    // part's list entries' sub-facet view factors and direction vectors,
+    // and which solve and facet range they belong to
+    float* cnorm = nullptr;    // [nsf][3]
+    float* gvf = nullptr;      // [entries][nsf]
+    float* vec = nullptr;      // [entries][3]
+    size_t gvf_cap = 0;        // entries allocated
+    const atpm_solve* fsolve = nullptr;
+    int ff0 = -1;
     CraterDev d{};
 };
 
@@ -158,10 +167,120 @@ ATPM_API atpm_status atpm_crater_destroy(atpm_crater* c) {
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->mem) cudaFree(c->mem);
     if (c->numrevs) cudaFree(c->numrevs);
+    if (c->cnorm) cudaFree(c->cnorm);
+    if (c->gvf) cudaFree(c->gvf);
+    if (c->vec) cudaFree(c->vec);
     if (c->st) cudaStreamDestroy(c->st);
     atpm_context* ctx = c->ctx;
     delete c;
     atpm_context_release(ctx);
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_set_surface(atpm_crater* c, int32_t nsv, const float* vertices,
+                                             const int32_t* facets, const float* viewfactors, float rot_period) {
+    if (!c || nsv < 3 || nsv > 128 || !vertices || !facets || (!viewfactors && c->nx != 0))
+        return atpm::fail_status(ATPM_E_INVALID, "crater_set_surface: bad arguments");
+    for (int i = 0; i < 3 * c->nsf; ++i)
+        if (facets[i] < 0 || facets[i] >= nsv) return atpm::fail_status(ATPM_E_INVALID, "crater_set_surface: facet index");
+    // surfacegeometry (3905/Thermal/NominalPole/main.cpp:822-868), in float:
+    // edge vectors, unit normal, and the sub-point grid's two vectors
+    // (-edge 2 / m, edge 1 / m, m = 10)
+    const int nsf = c->nsf;
+    std::vector<float> tri((size_t)nsf * 6), nrm((size_t)nsf * 3);
+    for (int j = 0; j < nsf; ++j) {
+        const float* a = vertices + 3 * facets[3 * j];
+        const float* b = vertices + 3 * facets[3 * j + 1];
+        const float* e = vertices + 3 * facets[3 * j + 2];
+        float n0[3], n1[3], nv[3];
+        for (int k = 0; k < 3; ++k) {
+            n0[k] = b[k] - a[k];
+            n1[k] = e[k] - a[k];
+        }
+        nv[0] = (n0[1] * n1[2]) - (n0[2] * n1[1]);
+        nv[1] = (n0[2] * n1[0]) - (n0[0] * n1[2]);
+        nv[2] = (n0[0] * n1[1]) - (n0[1] * n1[0]);
+        const float n = std::sqrt((nv[0] * nv[0]) + (nv[1] * nv[1]) + (nv[2] * nv[2]));
+        for (int k = 0; k < 3; ++k) {
+            nrm[3 * j + k] = nv[k] / n;
+            tri[6 * j + k] = -1.0f * n1[k] / 10.0f;
+            tri[6 * j + 3 + k] = n0[k] / 10.0f;
+        }
+    }
+    atpm_status r = atpm_crater_set_model(c, nsv, vertices, facets, tri.data(), viewfactors, rot_period);
+    if (r) return r;
+    if (!c->cnorm) CC(cudaMalloc((void**)&c->cnorm, (size_t)nsf * 12), "allocation");
+    CC(cudaMemcpy(c->cnorm, nrm.data(), (size_t)nsf * 12, cudaMemcpyHostToDevice), "copy");
+    c->d.cnorm = c->cnorm;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_forcing(atpm_solve* s, atpm_crater* c, int32_t f0, const float* dep_vec) {
+    if (!s || !c || f0 < 0 || f0 + c->nf > s->nf || c->ntau != s->P.ntau)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_forcing: the crater must cover facets f0 .. f0+nf-1 of the solve");
+    if (!c->cnorm) return atpm::fail_status(ATPM_E_STATE, "crater_forcing: set the crater surface first");
+    if (s->rs != 4) return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_forcing: FP32 solves (REFERENCE or FAST)");
+    if (!s->have_forcing) return atpm::fail_status(ATPM_E_STATE, "crater_forcing: run the solve's geometry and scattering first");
+    if (s->ctx->device != c->ctx->device) return atpm::fail_status(ATPM_E_INVALID, "crater_forcing: different devices");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    CC(cudaStreamSynchronize(s->st), "solve stream");
+    CraterDev& d = c->d;
+    atpm_status r = solve_crater_sun(s, f0, c->nf, const_cast<float*>(d.illumvec), const_cast<int*>(d.shadow), c->st);
+    if (r) return r;
+    if (launch_crater_surface(d, const_cast<float*>(d.illumangle), c->st))
+        return atpm::fail_status(ATPM_E_CUDA, "crater_forcing: surface launch");
+    // the part's list entries
+    std::vector<int32_t> ptr(2);
+    CC(cudaMemcpy(ptr.data(), s->ds.dep_ptr + f0, 4, cudaMemcpyDeviceToHost), "list bounds");
+    CC(cudaMemcpy(ptr.data() + 1, s->ds.dep_ptr + f0 + c->nf, 4, cudaMemcpyDeviceToHost), "list bounds");
+    const size_t ne = (size_t)(ptr[1] - ptr[0]);
+    if (ne > 0 && !dep_vec) return atpm::fail_status(ATPM_E_INVALID, "crater_forcing: the list entries' vectors are needed");
+    if (ne > c->gvf_cap) {
+        if (c->gvf) cudaFree(c->gvf);
+        if (c->vec) cudaFree(c->vec);
+        c->gvf = nullptr;
+        c->vec = nullptr;
+        c->gvf_cap = 0;
+        CC(cudaMalloc((void**)&c->gvf, ne * c->nsf * 4), "allocation");
+        CC(cudaMalloc((void**)&c->vec, ne * 12), "allocation");
+        c->gvf_cap = ne;
+    }
+    if (ne > 0) {
+        CC(cudaMemcpyAsync(c->vec, dep_vec + 3 * (size_t)ptr[0], ne * 12, cudaMemcpyHostToDevice, c->st), "vectors");
+        if (launch_crater_gvf(d, s->ds.vert, s->ds.fac, s->ds.dep_ptr, s->ds.dep_vf, f0, c->vec, c->gvf, c->st))
+            return atpm::fail_status(ATPM_E_CUDA, "crater_forcing: view-factor launch");
+    }
+    // global illumination: the dependent facets' scattered illumination x
+    // albedo (a shadow-only crater holds arrays 0-3 only)
+    if (c->nx != 0 &&
+        launch_crater_gsum(d, s->ds.dep_ptr, s->ds.dep_idx, f0, c->gvf, static_cast<const float*>(s->ds.Efm),
+                           s->P.ntau, 0, s->ds.alb, 0.0f, 0.0f, const_cast<float*>(d.RGI), c->st))
+        return atpm::fail_status(ATPM_E_CUDA, "crater_forcing: global illumination launch");
+    CC(cudaStreamSynchronize(c->st), "forcing");
+    c->fsolve = s;
+    c->ff0 = f0;
+    return ATPM_OK;
+}
+
+ATPM_API atpm_status atpm_crater_global_heating(atpm_solve* s, atpm_crater* c, int32_t f0) {
+    if (!s || !c) return atpm::fail_status(ATPM_E_INVALID, "crater_global_heating: null argument");
+    if (c->fsolve != s || c->ff0 != f0)
+        return atpm::fail_status(ATPM_E_STATE, "crater_global_heating: run atpm_crater_forcing for this solve and f0 first");
+    if (c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "crater_global_heating: shadow-only crater");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    CC(cudaStreamSynchronize(s->st), "solve stream");
+    // the dependent facets' surface temperatures, facet-major
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    float* tfm = nullptr;
+    CC(cudaMallocAsync((void**)&tfm, nt * 4, c->st), "allocation");
+    int rc = launch_transpose_sf(static_cast<const float*>(s->ds.stemp1), s->P.ntau, s->nf, tfm, c->st);
+    // load_GPU_roughness_globalheating (main.cpp:2072-2103): EPS x SIGMA x T^4
+    if (!rc)
+        rc = launch_crater_gsum(c->d, s->ds.dep_ptr, s->ds.dep_idx, f0, c->gvf, tfm, s->P.ntau, 1, 0.0f,
+                                (float)s->P.emissivity, 5.67e-8f, const_cast<float*>(c->d.RGH), c->st);
+    cudaFreeAsync(tfm, c->st);
+    CC(cudaStreamSynchronize(c->st), "global heating");
+    if (rc) return atpm::fail_status(ATPM_E_CUDA, "crater_global_heating: launch");
     return ATPM_OK;
 }
 

@@ -505,6 +505,61 @@ int launch_shadow_culled(const DevSolve& s, const GeomWork& g, bool all_pairs, s
     return rc;
 }
 
+// The Sun direction in every facet's local frame, the crater model's input
+// (asteroidgeometry, 3905/Thermal/NominalPole/main.cpp:967-1030): frame rows
+// = the first edge (unit), normal x edge, the unit normal; the vector is
+// -frame . heliocentric midpoint, scaled to length 10^4 and rounded to float.
+// The facet's final shadow flag (self-shadow and astshadow) goes beside it.
+// Facets f0 .. f0 + nfc - 1; outputs [nfc][ntau][3] and [nfc][ntau].
+__global__ void __launch_bounds__(256) k_crater_sun(GeomArgs a, int f0, int nfc, float* sun, int* shadow) {
+    const int ntau = a.s.ntau;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nfc * ntau) return;
+    const int fl = (int)(i / ntau), s = (int)(i % ntau), f = f0 + fl;
+    const int* fv = a.s.fac + 3 * f;
+    const double* h0 = a.g.hp + ((size_t)fv[0] * ntau + s) * 3;
+    const double* h1 = a.g.hp + ((size_t)fv[1] * ntau + s) * 3;
+    const double* h2 = a.g.hp + ((size_t)fv[2] * ntau + s) * 3;
+    double hm[3], n[3], nc0[3], nc1[3], y[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        hm[k] = DDIV(DADD(DADD(h0[k], h1[k]), h2[k]), 3.0);
+        nc0[k] = DSUB(h1[k], h0[k]);
+        nc1[k] = DSUB(h2[k], h0[k]);
+    }
+    const double t = __dsqrt_rn(DADD(DADD(DMUL(hm[0], hm[0]), DMUL(hm[1], hm[1])), DMUL(hm[2], hm[2])));
+    n[0] = DSUB(DMUL(nc0[1], nc1[2]), DMUL(nc0[2], nc1[1]));
+    n[1] = DSUB(DMUL(nc0[2], nc1[0]), DMUL(nc0[0], nc1[2]));
+    n[2] = DSUB(DMUL(nc0[0], nc1[1]), DMUL(nc0[1], nc1[0]));
+    const double nn = __dsqrt_rn(DADD(DADD(DMUL(n[0], n[0]), DMUL(n[1], n[1])), DMUL(n[2], n[2])));
+    const double x = __dsqrt_rn(DADD(DADD(DMUL(nc0[0], nc0[0]), DMUL(nc0[1], nc0[1])), DMUL(nc0[2], nc0[2])));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        n[k] = DDIV(n[k], nn);
+        nc0[k] = DDIV(nc0[k], x);
+    }
+    y[0] = DSUB(DMUL(n[1], nc0[2]), DMUL(n[2], nc0[1]));
+    y[1] = DSUB(DMUL(n[2], nc0[0]), DMUL(n[0], nc0[2]));
+    y[2] = DSUB(DMUL(n[0], nc0[1]), DMUL(n[1], nc0[0]));
+    const double* row[3] = {nc0, y, n};
+    float* out = sun + ((size_t)fl * ntau + s) * 3;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double iv = -DADD(DADD(DMUL(row[k][0], hm[0]), DMUL(row[k][1], hm[1])), DMUL(row[k][2], hm[2]));
+        out[k] = (float)DDIV(DMUL(10000.0, iv), t);
+    }
+    shadow[(size_t)fl * ntau + s] = a.s.shadow[(size_t)f * ntau + s];
+}
+
+int launch_crater_sun(const DevSolve& s, const GeomWork& g, int f0, int nfc, float* sun, int* shadow, stream_t stv) {
+    cudaStream_t st = static_cast<cudaStream_t>(stv);
+    GeomArgs a{s, g};
+    const long long nvt = (long long)s.nv * s.ntau, nct = (long long)nfc * s.ntau;
+    k_geom_vertices<<<(unsigned)((nvt + 255) / 256), 256, 0, st>>>(a);
+    k_crater_sun<<<(unsigned)((nct + 255) / 256), 256, 0, st>>>(a, f0, nfc, sun, shadow);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     GeomArgs a{s, g};

@@ -111,6 +111,9 @@ void batch_plan_free(BatchPlan& plan);
 // dst (a clone of src's shape) takes src's parameters and device state
 // again by device copies, without allocating
 atpm_status solve_refresh(atpm_solve* dst, atpm_solve* src);
+// the crater model's Sun vectors [nfc][ntau][3] and facet shadows [nfc][ntau]
+// of facets f0 .. f0 + nfc - 1 (device arrays), on stream st (synchronised)
+atpm_status solve_crater_sun(atpm_solve* s, int f0, int nfc, float* sun, int* shadow, cudaStream_t st);
 atpm_status fail_status(atpm_status s, const char* msg);
 }  // namespace atpm
 

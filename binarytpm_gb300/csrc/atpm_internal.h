@@ -188,6 +188,10 @@ struct GeomWork {
     unsigned long long* tests;  // [64] exact ray-triangle tests of the culled drivers (or null)
 };
 int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t st);
+// vertex positions of every step (into g.hp), then the crater model's Sun
+// vector [nfc][ntau][3] and the facet shadow flags [nfc][ntau] of facets
+// f0 .. f0 + nfc - 1
+int launch_crater_sun(const DevSolve& s, const GeomWork& g, int f0, int nfc, float* sun, int* shadow, stream_t st);
 int launch_shadow_deplist(const DevSolve& s, const GeomWork& g, stream_t st);
 int launch_shadow_allpairs(const DevSolve& s, const GeomWork& g, stream_t st);
 // the same flags with the projected-box cull in front of the exact test
@@ -301,6 +305,7 @@ struct CraterDev {
     const int* cfac;         // [nsf][3]
     const float* ctri;       // [nsf][2][3]
     const float* cmult;      // [100][2] trivector multipliers
+    const float* cnorm;      // [nsf][3] sub-facet unit normals (atpm_crater_set_surface), or null
     float PI, rot_period;
     // non-synchronous binaries (175706/Run-04/thermal_GPU.cu): revolutions of
     // each facet's body per model period (null: 1 for every facet) and the
@@ -331,6 +336,14 @@ struct CraterDev {
 int crater_launch(int what, const CraterDev& c, const PowTab& p4, const PowTab& pq, const float* fargs, void* p0,
                   void* p1, stream_t st);
 bool crater_nx_supported(int nx);
+// the crater's forcing from a solve (atpm_crater_forcing.cu)
+int launch_crater_surface(const CraterDev& c, float* illumangle, stream_t st);
+int launch_crater_gvf(const CraterDev& c, const double* vert, const int* fac, const int* dep_ptr,
+                      const float* dep_vf, int f0, const float* vec, float* gvf, stream_t st);
+int launch_crater_gsum(const CraterDev& c, const int* dep_ptr, const int* dep_idx, int f0, const float* gvf,
+                       const float* X, int ntau_x, int heat, float alb, float eps, float sigma, float* out,
+                       stream_t st);
+int launch_transpose_sf(const float* in, int ntau, int nf, float* out, stream_t st);
 
 // pow exception tables (atpm_powtab.cpp)
 struct HostPowTab {

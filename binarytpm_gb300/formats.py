@@ -111,3 +111,26 @@ def write_shadow(path, v, f, shadow) -> None:
 def read_values_after_header(path, nv: int, nf: int, dtype=np.float64):
     tok = open(path).read().split()
     return np.array(tok[3 * nv + 3 * nf:], dtype=dtype)
+
+
+def crater_model(mesh_text: str, list_text: str, nsv: int = 61, nsf: int = 100):
+    """The crater (roughness) model from the text of its two files, as the
+    reference reads them (Surface::readmodel / readselfheating,
+    3905/Thermal/NominalPole/main.cpp:641-668): float vertices [nsv][3],
+    facets [nsf][3] and the dense view-factor matrix the driver hands its GPU
+    module, V[d][i] = view factor of sub-facet i's entry for sub-facet d and
+    V[i][i] = 0 (load_GPU_constants, main.cpp:1951-2001)."""
+    tok = mesh_text.split()
+    v = np.array(tok[:3 * nsv], dtype=np.float64).astype(np.float32).reshape(nsv, 3)
+    f = np.array(tok[3 * nsv:3 * nsv + 3 * nsf], dtype=np.int32).reshape(nsf, 3)
+    V = np.zeros((nsf, nsf), np.float32)
+    lines = list_text.splitlines()
+    for i in range(nsf):
+        t = lines[i].split()
+        n = int(t[0])
+        dep = np.array(t[1:1 + n], dtype=np.int64)
+        vf = np.array(t[1 + n:1 + 2 * n], dtype=np.float64).astype(np.float32)
+        V[dep, i] = vf
+        V[i, i] = 0.0
+    return v, f, V
+

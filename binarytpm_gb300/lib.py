@@ -117,6 +117,11 @@ _SIGS = {
     "atpm_crater_get_array_strided": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_uint64]),
     "atpm_disk_flux_rough": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]),
+    "atpm_crater_set_surface": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float]),
+    "atpm_crater_forcing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "atpm_crater_global_heating": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "atpm_solve_solar": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "atpm_set_albedo": (C.c_int, [C.c_void_p, C.c_float]),
 }
 
 
@@ -419,6 +424,16 @@ class Solve:
         _ck(load().atpm_last_run_config(self.h, C.byref(v), C.byref(d), C.byref(t)))
         return v.value, d.value, bool(t.value)
 
+    def set_albedo(self, albedo: float):
+        """Change the Bond albedo (scatter again before the next revolution)."""
+        _ck(load().atpm_set_albedo(self.h, float(albedo)))
+
+    def solar(self) -> float:
+        """The solar flux at the body, W/m^2."""
+        v = C.c_float()
+        _ck(load().atpm_solve_solar(self.h, C.byref(v)))
+        return float(v.value)
+
     def last_shadow_stats(self):
         """(device ms, rays, exact ray-triangle tests or -1) of the last
         geometry_shadow's shadow drivers."""
@@ -577,6 +592,25 @@ class Crater:
         vf = np.ascontiguousarray(viewfactors, np.float32)
         _ck(load().atpm_crater_set_model(self.h, len(v), _p(v), _p(f), _p(t), _p(vf), float(rotation_period_s)))
 
+    def set_surface(self, vertices, facets, viewfactors, rotation_period_s: float):
+        """The crater model from its mesh (sub-point grid vectors and sub-facet
+        normals derived on the host as the reference's surfacegeometry does);
+        viewfactors: dense V[i][j] (``crater_viewfactors``)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        f = np.ascontiguousarray(facets, np.int32)
+        vf = np.ascontiguousarray(viewfactors, np.float32)
+        _ck(load().atpm_crater_set_surface(self.h, len(v), _p(v), _p(f), _p(vf), float(rotation_period_s)))
+
+    def forcing(self, solve: "Solve", f0: int = 0, dep_vec=None):
+        """Arrays 0-3 and 5 for facets f0 .. f0+nf-1 of ``solve``, computed on
+        the device; dep_vec: the solve's list entries' direction vectors [nnz][3]."""
+        d = None if dep_vec is None else np.ascontiguousarray(np.asarray(dep_vec, np.float32).reshape(-1, 3))
+        _ck(load().atpm_crater_forcing(solve.h, self.h, int(f0), _p(d)))
+
+    def global_heating(self, solve: "Solve", f0: int = 0):
+        """Array 6 from the solve's current surface temperatures."""
+        _ck(load().atpm_crater_global_heating(solve.h, self.h, int(f0)))
+
     def set_properties(self, converged=None, albedo=None, thermal_inertia=None):
         c = None if converged is None else np.ascontiguousarray(converged, np.uint8)
         a = None if albedo is None else np.ascontiguousarray(albedo, np.float32)
@@ -608,6 +642,14 @@ class Crater:
 
     # strided-transfer slots of the temperature arrays ([nf][ntau][nsf], depth [nf][nx+1][nsf])
     STEMP0, STEMP1, DEPTH = 7, 8, 9
+
+    def get_temperatures(self):
+        """(stemp0, stemp1, depth): [nf][ntau][nsf] twice and [nf][nx+1][nsf]."""
+        s0 = np.zeros((self.nf, self.ntau, self.nsf), np.float32)
+        s1 = np.zeros((self.nf, self.ntau, self.nsf), np.float32)
+        d = np.zeros((self.nf, self.nx + 1, self.nsf), np.float32)
+        _ck(load().atpm_crater_get_temperatures(self.h, _p(s0), _p(s1), _p(d)))
+        return s0, s1, d
 
     def set_temperatures(self, stemp1, stemp0=None):
         """Sub-facet surface temperatures [nf][ntau][nsf] (and the previous

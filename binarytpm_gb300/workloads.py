@@ -24,20 +24,23 @@ from . import problem as P
 BATCH_TI = [25.0, 50.0, 100.0, 200.0, 400.0, 800.0, 1400.0, 2000.0]
 
 
-def _lists(ctx, v, f):
+def _lists(ctx, v, f, with_vectors=False):
     from . import lib
 
     ptr, idx, vf, vec, photo = lib.viewfactors(ctx, v, f, refine=True)
-    return ptr, idx, vf
+    return (ptr, idx, vf, vec) if with_vectors else (ptr, idx, vf)
 
 
 def binary_problem(ctx, p_subdiv=5, s_subdiv=3, ntau=720, nx=56, seed=2) -> P.Problem:
+    """The synchronous binary; meta["dep_vec"] keeps the list entries'
+    direction vectors (the crater forcing needs them)."""
     v, f = P.binary_mesh(p_subdiv, s_subdiv, seed)
-    ptr, idx, vf = _lists(ctx, v, f)
+    ptr, idx, vf, vec = _lists(ctx, v, f, with_vectors=True)
     return P.Problem(vertices=v, facets=f.astype(np.int32), dep_ptr=ptr, dep_idx=idx, dep_vf=vf,
                      ntau=ntau, nx=nx, polar=(1.0, 0.0, 0.0), pole=P.BINARY_POLE,
                      rotation_period_s=11.9 * 3600.0, albedo=0.02, emissivity=0.9,
-                     thermal_inertia=200.0, tacc=0.005, name=f"binary_s{p_subdiv}s{s_subdiv}")
+                     thermal_inertia=200.0, tacc=0.005, name=f"binary_s{p_subdiv}s{s_subdiv}",
+                     meta={"dep_vec": np.asarray(vec, np.float32).reshape(-1, 3)})
 
 
 def stress_problem(ctx, p_subdiv=6, s_subdiv=4, ntau=720, nx=56, seed=3) -> P.Problem:

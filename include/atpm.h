@@ -150,6 +150,13 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
                                     int32_t* counts);
 
 /* Host copies of the solve's state ([nf][ntau] facet-major). */
+/* A solve's Bond albedo (the reference's bond_albedo, main.cpp:38), e.g. for a
+ * clone that shares its source's shape and shadows: the scattered
+ * illumination depends on it, so atpm_scattering runs again before the
+ * next revolution. */
+ATPM_API atpm_status atpm_set_albedo(atpm_solve* s, float albedo);
+/* the solar flux at the body (A.rtnsolar(), main.cpp:905), W/m^2 */
+ATPM_API atpm_status atpm_solve_solar(const atpm_solve* s, float* solar);
 ATPM_API atpm_status atpm_get_shadow(atpm_solve* s, int32_t* out);
 ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out);
 ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0);
@@ -328,6 +335,30 @@ ATPM_API atpm_status atpm_crater_get_array_strided(atpm_crater* c, int32_t which
  * the crater sub-facets' emission seen by the others (thermal_GPU.cu:521,
  * 390, 615); 1 unless set. */
 ATPM_API atpm_status atpm_crater_set_revolutions(atpm_crater* c, const float* numrevs /* [nf] or NULL */);
+/* The crater model from its mesh alone (the shim path gets the derived
+ * vectors from the driver instead): vertices [nsv][3], facets [nsf][3] and
+ * view factors V[i][j] as for atpm_crater_set_model; the sub-point grid
+ * vectors and the sub-facet unit normals are derived as surfacegeometry does
+ * (3905/Thermal/NominalPole/main.cpp:822-868).  Needed by atpm_crater_forcing. */
+ATPM_API atpm_status atpm_crater_set_surface(atpm_crater* c, int32_t nsv, const float* vertices,
+                                             const int32_t* facets, const float* viewfactors, float rot_period);
+/* The crater's forcing for facets f0 .. f0 + nf - 1 of a solve (a part, in
+ * the reference's terms), computed on the device from the solve's geometry,
+ * shadows and scattered illumination (after atpm_geometry_shadow and
+ * atpm_scattering; REFERENCE or FAST solves): the facet shadows and local
+ * Sun vectors (asteroidgeometry, main.cpp:1019-1030), each sub-facet's Sun
+ * angle and starting shadow (surfacegeometry, 873-885), the sub-facet view
+ * factors of the solve's list entries (calculate_surface_global_viewfactors,
+ * 1053-1181) and the global illumination (2033-2065) -- arrays 0-3 and 5.
+ * dep_vec: the solve's list entries' direction vectors [nnz][3] (the
+ * _selfheating_vector_list.txt vectors; NULL when the part has no entries).
+ * A REFERENCE crater on a REFERENCE solve gives the arrays the reference
+ * driver builds on the host, bit for bit. */
+ATPM_API atpm_status atpm_crater_forcing(atpm_solve* s, atpm_crater* c, int32_t f0, const float* dep_vec);
+/* The global heating (array 6) from the solve's current surface temperatures
+ * (load_GPU_roughness_globalheating, main.cpp:2069-2103), with the view
+ * factors of the last atpm_crater_forcing on the same solve and f0. */
+ATPM_API atpm_status atpm_crater_global_heating(atpm_solve* s, atpm_crater* c, int32_t f0);
 ATPM_API atpm_status atpm_crater_set_ir_absorptivity(atpm_crater* c, float ir_abs);
 /* GPU_sfcpartialshadow (909-921): every step in one launch */
 ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c);
