@@ -205,3 +205,31 @@ def test_precision_stress_concave_binary_small(gpu_ctx):
     err = workloads.fast_vs_fp64(gpu_ctx, prob, [50.0, 800.0], 40, sh, il)
     assert err["max_temperature_error_K"] < 0.01, err
     assert err["max_rel_flux_error_12um"] < 1e-5, err
+
+
+@pytest.mark.parametrize("precision", ["FAST", "REFERENCE"])
+def test_albedo_change_on_a_clone_matches_a_fresh_solve(gpu_ctx, precision):
+    """atpm_set_albedo on a clone of a prepared solve, then scattering again:
+    the scattered illumination and a revolution's temperatures are those of
+    a solve created with that albedo."""
+    from binarytpm_gb300 import lib
+
+    prob, _ = golden("binary_s3s1")
+    p = getattr(lib, precision)
+    s0 = lib.Solve(gpu_ctx, prob, precision=p, revcap=4)
+    s0.geometry_shadow()
+    s0.scattering()
+    c = s0.clone()
+    c.set_albedo(0.13)
+    c.scattering()
+    f = lib.Solve(gpu_ctx, prob.with_(albedo=0.13), precision=p, revcap=4)
+    f.geometry_shadow()
+    f.scattering()
+    assert np.array_equal(c.illumination().view(np.uint32), f.illumination().view(np.uint32))
+    for x in (c, f):
+        x.set_thermal_inertia(200.0)
+        x.initialise_temperatures()
+        x.run()
+    assert np.array_equal(c.surface_temperature()[0].view(np.uint32), f.surface_temperature()[0].view(np.uint32))
+    for x in (s0, c, f):
+        x.close()
