@@ -498,8 +498,9 @@ def main():
 
     cond_v, tc_depth, _ = s0.last_run_config()
     launch_config = {"conduction_variant": cond_v, "tc_pipeline_depth": tc_depth,
-                     "chosen_by": "autotuner: the first batch of this kind (a warm-up step) timed the candidates "
-                                  "on its first 4 revolutions; results do not depend on the choice"}
+                     "chosen_by": "autotuner: the first batch of this kind (a warm-up step) ran its first 5 revolutions "
+                                  "with one candidate each, both batch groups together, and timed each "
+                                  "revolution whole; results do not depend on the choice"}
 
     # per-kernel durations of one instrumented (all-active) revolution
     kern = lib.profile_revolution(solves)
@@ -530,7 +531,7 @@ def main():
         cpu = cpu_baseline(prob)
 
     hbm, bf16, kind = _peaks()
-    roof = _roofline(kern, len(tis), prob, hbm, bf16, kind)
+    roof = _roofline(kern, len(tis), prob, hbm, bf16, kind, cond_v)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -856,9 +857,13 @@ def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: 
 
 FP64_TI = [200.0, 2000.0]
 CONV_ERR_TI = [200.0, 2000.0]
-# executed instructions per facet-step of k_conduction<FAST,56> (ncu,
-# profiles/conduction_and_spmm_binary_s4s3_fast.md)
-COND_INSTR_PER_FACET_STEP = 327
+# executed instructions per facet-step of the FAST sweep by conduction
+# variant (ncu: profiles/conduction_and_spmm_binary_s4s3_fast.md for the
+# scalar k_conduction<FAST,56>, profiles/conduction_pairs_binary_s4s3_8solves.md
+# for the paired k_conduction_pairs<56>)
+COND_INSTR_PER_FACET_STEP = {1: 327, 2: 327, 3: 327, 4: 188}
+COND_KERNEL = {1: "k_conduction<FAST,56,1>", 2: "k_conduction<FAST,56,2>", 3: "k_conduction<FAST,56,3>",
+               4: "k_conduction_pairs<56>"}
 ACC_REVS = 40
 
 
@@ -879,7 +884,7 @@ def _tile_stats(prob, slices=False):
     return len(tiles), int(has_lo.sum()), rem, len(sk), int(has_lo[sk // 4].sum())
 
 
-def _roofline(kern, n, prob, hbm, bf16, kind):
+def _roofline(kern, n, prob, hbm, bf16, kind, cond_variant=4):
     """Dominant kernel of the revolution loop: the self-heating product
     (k_spmm_tc over the tensor-core tiles, then k_spmm_rem over the FP32
     sparse remainder; timed together).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
@@ -919,21 +924,28 @@ def _roofline(kern, n, prob, hbm, bf16, kind):
     c = kern.get("conduction")
     if c and c["ms"]:
         nx = prob.nx
-        bytes_ = c["facet_steps"] * 20 + c["active_facets"] * 2 * (nx + 1) * 4
+        # per facet-step: E, Q and stemp read, E and stemp written (20 B), W
+        # as BF16 hi/lo tile entries (4 B) and as FP32 (4 B); the depth column
+        # read and written once per facet
+        bytes_ = c["facet_steps"] * 28 + c["active_facets"] * 2 * (nx + 1) * 4
         gbs = bytes_ / (c["ms"] / 1e3) / 1e9
         traffic = None
         tf = ROOT / "profiles" / "conduction_fast_nx56_traffic.json"
         if tf.exists():
-            traffic = json.loads(tf.read_text())["dram_bytes_per_facet_step"] * c["facet_steps"]
+            per = json.loads(tf.read_text()).get("by_variant", {}).get(str(cond_variant))
+            if per:
+                traffic = per["dram_bytes_per_facet_step"] * c["facet_steps"]
         # FP32 issue: one warp instruction per SM sub-partition per clock
         issue_peak = 152 * 4 * 32 * 2.07e9
-        instr = COND_INSTR_PER_FACET_STEP * c["facet_steps"]
-        out["conduction"] = {"kernel": "k_conduction<FAST,56>", "bound": "fp32_issue",
+        ipfs = COND_INSTR_PER_FACET_STEP[cond_variant]
+        instr = ipfs * c["facet_steps"]
+        out["conduction"] = {"kernel": COND_KERNEL[cond_variant], "bound": "fp32_issue",
                              "achieved": instr / (c["ms"] / 1e3) / 1e12, "peak": issue_peak / 1e12,
                              "unit": "T thread-instructions/s",
                              "frac": instr / (c["ms"] / 1e3) / issue_peak,
-                             "instructions_per_facet_step": COND_INSTR_PER_FACET_STEP,
-                             "minimum_instructions_per_facet_step": 230,
+                             "instructions_per_facet_step": ipfs,
+                             # scalar: 55 nodes x 3 FP32 ops + Newton; paired: half of that per facet
+                             "minimum_instructions_per_facet_step": 115 if cond_variant == 4 else 230,
                              "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
                                      "algorithmic_bytes": bytes_, "traffic": traffic},
                              "note": "issue peak = 152 SMs x 4 sub-partitions x 32 lanes x 2.07 GHz (nominal); "
@@ -955,35 +967,56 @@ def e2e_run(ctx, prob, tis, steps):
                                         for k in ("vertices", "facets", "dep_ptr", "dep_idx", "dep_vf")})
     outs = [lib.host_buffer((prob.nf, prob.ntau), np.float32) for _ in tis]
     vals, h2d, d2h = [], 0, 0
-    for _ in range(steps):
+    phases = {}
+
+    def mark(name, t):
+        # phase boundaries of the one extra, untimed job (synchronised there)
+        if split:
+            torch.cuda.synchronize()
+            now = time.perf_counter()
+            phases[name] = round((now - t) * 1e3, 3)
+            return now
+        return t
+
+    for j in range(steps + 1):
+        split = j == steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        t = t0
         s0 = lib.Solve(ctx, prob, precision=lib.FAST, revcap=HEADLINE_REVS)
+        t = mark("solve_create_h2d", t)
         s0.geometry_shadow()
+        t = mark("geometry_shadow", t)
         s0.scattering()
+        t = mark("scattering", t)
         # one prepared shape, cloned on the device for the other inertias
         solves = [s0] + [s0.clone() for _ in tis[1:]]
         for s, ti in zip(solves, tis):
             s.set_thermal_inertia(ti)
             s.initialise_temperatures()
+        t = mark("clones_initial_temperatures", t)
         lib.batch_run(solves)
+        t = mark("batched_revolutions", t)
         fs = solves[0].last_run_stats()[2]
         # the stage's result: every facet's surface temperature at every step
         temps = [s.result_temperature(out=o) for s, o in zip(solves, outs)]
         torch.cuda.synchronize()
+        t = mark("temperatures_d2h", t)
         dt = time.perf_counter() - t0
-        vals.append(fs / dt)
+        if not split:
+            vals.append(fs / dt)
         shape_bytes = prob.vertices.nbytes + prob.facets.nbytes + prob.dep_ptr.nbytes + prob.dep_idx.nbytes + prob.dep_vf.nbytes
         h2d = shape_bytes
         d2h = sum(t.nbytes for t in temps)
         for s in solves:
             s.close()
     return {"value": statistics.median(vals), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h),
+            "d2h_bytes_per_step": int(d2h), "phases_ms": phases,
             "what": "C-ABI job from host arrays: solve create (H2D), geometry+shadowing+scattering, "
                     "device clones for the other inertias, the timed workload's batched revolutions, "
                     "surface temperatures (the Thermal stage's result) D2H; "
-                    "inputs and read-back buffers page-locked, allocated once before the timed jobs"}
+                    "inputs and read-back buffers page-locked, allocated once before the timed jobs; "
+                    "phases_ms: host time of each phase in one more job, synchronised between phases"}
 
 
 if __name__ == "__main__":

@@ -628,88 +628,111 @@ atpm_status capture_graph(atpm_solve* s, const Batch& b, cudaGraphExec_t* out) {
 }
 
 // Autotuner for FAST batches.  Its knobs change launch configurations only,
-// never results: the conduction kernel's register/occupancy variant
-// (k_conduction<FAST, NX, 1|2|3>: one source, three register budgets) and
-// the tensor-core pipeline depth.  The first time a kind of batch (precision,
-// NX, step chunk, size class) runs, its first three revolutions -- real
-// revolutions of the solve, each a different candidate -- are timed part by
-// part with events; the fastest conduction variant and pipeline depth are
-// kept in the context for every later batch of that kind.
-uint64_t tune_key(const Batch& b) {
+// never results: the conduction variant (k_conduction<FAST, NX, 1|2|3>: one
+// source, three register budgets; 4: the paired-facet sweep) and the
+// tensor-core pipeline depth.  The first time a kind of batch (precision,
+// NX, step chunk, size class, number of groups) runs, its first kTuneRevs
+// revolutions -- real revolutions of the solves, each with one candidate --
+// are launched for every group together, each group on its own stream as
+// the revolution loop launches them, and each revolution is timed whole,
+// from a common start to the end of the last group.  A variant that leaves
+// issue slots to the other group's product therefore shows up as the faster
+// revolution, which the sweep's own duration does not show.  The fastest
+// candidates are kept in the context for every later batch of that kind.
+uint64_t tune_key(const Batch& b, int groups) {
     int cls = 0;
     while ((1 << cls) < b.nfb && cls < 40) ++cls;  // facet blocks, power-of-two class
     return (uint64_t)b.mode | ((uint64_t)b.nx << 4) | ((uint64_t)b.tc_nmax << 12) | ((uint64_t)cls << 24) |
-           ((uint64_t)(b.nq > 0) << 32);
+           ((uint64_t)(b.nq > 0) << 32) | ((uint64_t)(groups > 1) << 33);
 }
 
-// revolutions the autotuner times, one conduction variant each
-constexpr int kTuneRevs = 4;
+// revolutions the autotuner times: conduction variants 1-4 at the deepest
+// tensor-core pipeline, then variant 4 one stage shallower
+constexpr int kTuneRevs = 5;
 
-atpm_status autotune(atpm_solve* s0, Batch& b, int maxcap, int* done_revs, int64_t* launches, int* tuned) {
+bool tune_log() {
+    const char* e = std::getenv("ATPM_TUNE_LOG");
+    return e && e[0] == '1';
+}
+
+atpm_status autotune(const std::vector<atpm_solve*>& leads, std::vector<Batch>& bs, const std::vector<int>& maxcap,
+                     std::vector<int>& done, int64_t* launches, int* tuned) {
+    atpm_solve* s0 = leads[0];
     atpm_context* c = s0->ctx;
-    const uint64_t key = tune_key(b);
+    const int ng = (int)bs.size();
+    const uint64_t key = tune_key(bs[0], ng);
+    auto apply = [&](int v, int d) {
+        for (Batch& b : bs) {
+            b.cond_variant = v;
+            b.tc_stages = d;
+        }
+    };
     {
         std::lock_guard<std::mutex> lk(c->mu);
         auto it = c->tune.find(key);
         if (it != c->tune.end()) {
-            b.cond_variant = it->second.cond_variant;
-            b.tc_stages = it->second.tc_stages;
+            apply(it->second.cond_variant, it->second.tc_stages);
             return ATPM_OK;
         }
     }
-    atpm_tune_choice ch;
-    const int smax = b.nq > 0 ? tc_max_stages(b.tc_nmax) : 0;
-    if (maxcap < kTuneRevs) {  // too short to time: defaults
-        b.cond_variant = cond_variant();
-        b.tc_stages = 0;
+    int mincap = maxcap[0];
+    for (int g = 1; g < ng; ++g) mincap = std::min(mincap, maxcap[g]);
+    if (mincap < kTuneRevs) {  // too short to time: defaults
+        apply(cond_variant(), 0);
         return ATPM_OK;
     }
-    // candidates per revolution: conduction variant v, pipeline depth d
-    const int cand_v[kTuneRevs] = {1, 2, 3, 4};
-    const int cand_d[kTuneRevs] = {smax, smax > 2 ? smax - 1 : smax, smax, smax};
-    cudaEvent_t ev[4 * kTuneRevs];
-    for (int i = 0; i < 4 * kTuneRevs; ++i) CK(cudaEventCreate(&ev[i]));
+    const int smax = bs[0].nq > 0 ? tc_max_stages(bs[0].tc_nmax) : 0;
+    const int cand_v[kTuneRevs] = {1, 2, 3, 4, 4};
+    const int cand_d[kTuneRevs] = {smax, smax, smax, smax, smax > 2 ? smax - 1 : smax};
+    // per revolution: start and end on the leader's stream, the end of every other group
+    const int nev = kTuneRevs * (1 + ng);
+    std::vector<cudaEvent_t> ev(nev, nullptr);
+    for (int i = 0; i < nev; ++i) CK(cudaEventCreate(&ev[i]));
+    auto ev_start = [&](int r) { return ev[r * (1 + ng)]; };
+    auto ev_end = [&](int r, int g) { return ev[r * (1 + ng) + 1 + g]; };  // g = 0: all groups done
     int rc = 0;
+    cudaError_t e = cudaSuccess;
     int64_t nlaunch = 0;
-    for (int r = 0; r < kTuneRevs && !rc; ++r) {
-        b.cond_variant = cand_v[r];
-        b.tc_stages = cand_d[r];
-        rc |= launch_revolution_part(b, 0, s0->st);
-        cudaEventRecord(ev[4 * r], s0->st);
-        rc |= launch_revolution_part(b, 1, s0->st);
-        cudaEventRecord(ev[4 * r + 1], s0->st);
-        rc |= launch_revolution_part(b, 2, s0->st);
-        cudaEventRecord(ev[4 * r + 2], s0->st);
-        rc |= launch_revolution_part(b, 3, s0->st);
-        rc |= launch_revolution_part(b, 4, s0->st);
-        cudaEventRecord(ev[4 * r + 3], s0->st);
-        nlaunch += kernels_per_revolution(b);
+    for (int r = 0; r < kTuneRevs && !rc && e == cudaSuccess; ++r) {
+        apply(cand_v[r], cand_d[r]);
+        e = cudaEventRecord(ev_start(r), s0->st);
+        for (int g = 1; g < ng && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(leads[g]->st, ev_start(r), 0);
+        for (int g = 0; g < ng && e == cudaSuccess && !rc; ++g) {
+            rc |= launch_revolution(bs[g], leads[g]->st);
+            nlaunch += kernels_per_revolution(bs[g]);
+        }
+        for (int g = 1; g < ng && e == cudaSuccess; ++g) {
+            e = cudaEventRecord(ev_end(r, g), leads[g]->st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(s0->st, ev_end(r, g), 0);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end(r, 0), s0->st);
     }
-    cudaError_t e = cudaStreamSynchronize(s0->st);
-    float tc[kTuneRevs] = {}, cd[kTuneRevs] = {};
-    for (int r = 0; r < kTuneRevs && e == cudaSuccess && !rc; ++r) {
-        cudaEventElapsedTime(&tc[r], ev[4 * r], ev[4 * r + 1]);
-        cudaEventElapsedTime(&cd[r], ev[4 * r + 1], ev[4 * r + 2]);
-    }
-    for (int i = 0; i < 4 * kTuneRevs; ++i) cudaEventDestroy(ev[i]);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s0->st);
+    float rv[kTuneRevs] = {};
+    for (int r = 0; r < kTuneRevs && e == cudaSuccess && !rc; ++r)
+        e = cudaEventElapsedTime(&rv[r], ev_start(r), ev_end(r, 0));
+    for (int i = 0; i < nev; ++i) cudaEventDestroy(ev[i]);
     if (rc) return fail(ATPM_E_CUDA, "revolution launch (autotune): %s", cudaGetErrorString(cudaGetLastError()));
     if (e != cudaSuccess) return fail(ATPM_E_CUDA, "autotune: %s", cudaGetErrorString(e));
-    int best = 0;
-    for (int r = 1; r < kTuneRevs; ++r)
-        if (cd[r] < cd[best]) best = r;
+    // variant 4 unless another revolution was faster; ties keep it
+    int best = 3;
+    for (int r = 0; r < 3; ++r)
+        if (rv[r] < rv[best]) best = r;
+    atpm_tune_choice ch;
     ch.cond_variant = cand_v[best];
-    // depth smax ran in revolutions 0 and 2, smax - 1 in revolution 1
-    ch.tc_stages = (smax > 2 && tc[1] < 0.5f * (tc[0] + tc[2])) ? smax - 1 : 0;
-    for (int r = 0; r < kTuneRevs; ++r) ch.cond_ms[r] = cd[r];
-    ch.tc_ms[0] = 0.5f * (tc[0] + tc[2]);
-    ch.tc_ms[1] = tc[1];
+    ch.tc_stages = (smax > 2 && rv[4] < rv[3]) ? smax - 1 : 0;
+    for (int r = 0; r < kTuneRevs; ++r) ch.rev_ms[r] = rv[r];
+    if (tune_log())
+        std::fprintf(stderr,
+                     "atpm autotune: %d group(s), revolution ms v1 %.4f v2 %.4f v3 %.4f v4 %.4f v4/depth-1 %.4f "
+                     "-> variant %d depth %d\n",
+                     ng, rv[0], rv[1], rv[2], rv[3], rv[4], ch.cond_variant, ch.tc_stages);
     {
         std::lock_guard<std::mutex> lk(c->mu);
         c->tune[key] = ch;
     }
-    b.cond_variant = ch.cond_variant;
-    b.tc_stages = ch.tc_stages;
-    *done_revs = kTuneRevs;
+    apply(ch.cond_variant, ch.tc_stages);
+    for (int g = 0; g < ng; ++g) done[g] = kTuneRevs;
     *launches += nlaunch;
     *tuned = 1;
     return ATPM_OK;
@@ -1537,16 +1560,16 @@ ATPM_API atpm_status atpm_batch_run(atpm_solve* const* solves, int32_t n, int32_
     if (e != cudaSuccess) { free_tmps(); return fail(ATPM_E_CUDA, "batch start: %s", cudaGetErrorString(e)); }
     if (bs[0].mode == MODE_FAST) {
         if (!autotune_enabled()) {
-            bs[0].cond_variant = cond_variant();
-            bs[0].tc_stages = 0;
+            for (Batch& b : bs) {
+                b.cond_variant = cond_variant();
+                b.tc_stages = 0;
+            }
         } else {
-            // group 0 tunes (if this kind of batch has not been), the others take its choice
-            atpm_status rt = autotune(s0, bs[0], maxcap[0], &done[0], &launches, &tuned);
+            // tunes every group together if this kind of batch has not been
+            std::vector<atpm_solve*> leads(ng);
+            for (int g = 0; g < ng; ++g) leads[g] = gs[g][0];
+            atpm_status rt = autotune(leads, bs, maxcap, done, &launches, &tuned);
             if (rt) { free_tmps(); return rt; }
-        }
-        for (int g = 1; g < ng; ++g) {
-            bs[g].cond_variant = bs[0].cond_variant;
-            bs[g].tc_stages = bs[0].tc_stages;
         }
     }
     std::vector<std::vector<Ctl>> ctl(ng);

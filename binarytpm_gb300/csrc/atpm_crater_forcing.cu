@@ -139,6 +139,12 @@ __global__ void __launch_bounds__(128) k_crater_gvf(CraterDev c, const double* v
         }
         float g = A::div(A::mul(A::mul(dep_vf[k], vis), angle), w[2]);
         if (g > 1.0f) g = 1.0f;
+        // FAST: an entry whose direction is not above the facet's plane (a
+        // grazing neighbour; its normal component can round to zero or
+        // below) contributes nothing instead of an unbounded quotient
+        if constexpr (MODE == MODE_FAST) {
+            if (!(w[2] > 0.0f)) g = 0.0f;
+        }
         gvf[(size_t)(k - k0) * nsf + j] = g;
     }
 }

@@ -16,8 +16,7 @@
 struct atpm_tune_choice {
     int cond_variant = 4;  // FAST conduction variant (1-3 register budgets, 4 paired facets)
     int tc_stages = 0;     // tensor-core pipeline depth (0: deepest)
-    float cond_ms[4] = {0, 0, 0, 0};
-    float tc_ms[2] = {0, 0};
+    float rev_ms[5] = {0, 0, 0, 0, 0};  // the timed revolutions, one per candidate
 };
 
 // A context lives while its creator's handle or any solve, server or crater

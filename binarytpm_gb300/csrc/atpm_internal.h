@@ -155,13 +155,13 @@ struct DevSolve {
     int tc_n, tc_nchunks, tc_nmb, tc_nkb;
     // sparse remainder of the view-factor lists (FAST): the entries of the
     // (128-row, 64-column) cells too sparse for a tensor-core tile, per row
-    // in list order (CSR, FP32 values), summed by the product's epilogue
-    // against W32, this solve's eps*sigma*T^4 facet-major in FP32
+    // in list order (CSR, FP32 values), summed by k_spmm_rem against W32,
+    // this solve's eps*sigma*T^4 facet-major in FP32
     const int* rem_ptr;      // [nf+1], or null when every entry is in a tile
     const int* rem_idx;      // [rem_nnz]
     const float* rem_vf;     // [rem_nnz]
     float* W32;              // [nf][w32_ld] FP32 (null without a remainder)
-    int w32_ld;              // row stride of W32: ntau rounded up to 8
+    int w32_ld;              // row stride of W32: ntau rounded up to 32 (the remainder's step chunks)
 };
 
 // element offset of (row, k) inside a 128-byte-swizzled K-major tile with 64

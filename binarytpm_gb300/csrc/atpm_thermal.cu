@@ -788,9 +788,19 @@ __device__ __forceinline__ bool list_mode(const Batch& b, const DevSolve& sv) {
     const int rev = sv.ctl->rev;
     return b.warp_tail && sv.freeze && rev >= 7 && sv.act_cnt[2 + (rev & 1)] == rev && 2 * sv.act_cnt[rev & 1] <= sv.nf;
 }
-// the facet-range sweep of this solve runs as pairs (variant 4, even facet count)
+// the facet-range sweep of this solve runs as pairs (variant 4, even facet
+// count) while at least 90 % of its facets are active: once facets freeze,
+// pairs split and their other halves would fall to the scalar sweep, so the
+// whole range goes back to it.  Both kernels read the same list count
+// (written by the previous revolution's convergence test), so exactly one
+// of them takes each facet.
 __device__ __forceinline__ bool pairs_here(const Batch& b, const DevSolve& sv) {
-    return b.cond_variant == 4 && (sv.nf & 1) == 0;
+    if (b.cond_variant != 4 || (sv.nf & 1)) return false;
+    const int rev = sv.ctl->rev;
+    // no count for this revolution (every facet active before revolution 7,
+    // or no lists kept): pairs; split pairs fall to the scalar sweep
+    if (!sv.freeze || rev < 7 || sv.act_cnt[2 + (rev & 1)] != rev) return true;
+    return 10 * sv.act_cnt[rev & 1] >= 9 * sv.nf;
 }
 
 // MINB: minimum resident blocks per SM requested from the register allocator

@@ -68,3 +68,27 @@ def test_selfheating_vectors_follow_the_list_rows(tmp_path):
     rows = p.read_text().split("\n")
     assert [len(r.split()) for r in rows[:3]] == [6, 0, 3]
     assert np.array_equal(formats.read_float_stream(p, 9), _g6_f32(vec.ravel()))
+
+
+def test_crater_model_parses_the_reference_crater_files():
+    """formats.crater_model reads the reference's crater mesh and its
+    self-heating list as the driver does: 61 float vertices, 100 facets, and
+    the dense V[d][i] with every sub-facet's 99 entries and a zero diagonal
+    (each sub-facet of the hemispherical bowl sees about half of the rest)."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_golden
+    from conftest import golden
+
+    from binarytpm_gb300 import formats
+
+    _, ref = golden("rough_s1s1")
+    texts = make_golden.crater_texts_from(ref)
+    v, f, V = formats.crater_model(texts["new_crater2.txt"], texts["new_crater2_selfheating_list.txt"])
+    assert v.shape == (61, 3) and v.dtype == np.float32
+    assert f.shape == (100, 3) and f.min() >= 0 and f.max() < 61
+    assert np.all(np.diag(V) == 0.0)
+    assert np.all((V > 0).sum(axis=0) == 99)
+    assert np.allclose(V.sum(axis=0), 0.5, atol=0.05)

@@ -4,8 +4,8 @@ configurations only: a FAST batch gives bit-identical temperatures and
 convergence counts with the tuner on, off, and with each variant forced
 (the run goes to convergence, so the active-list and warp-per-facet forms
 and pairs with one frozen facet are exercised too); the first batch of a
-kind times the candidates on its first four revolutions and later batches of
-that kind reuse the choice."""
+kind times the candidates on its first five revolutions (whole revolutions of
+both batch groups) and later batches of that kind reuse the choice."""
 import os
 
 import numpy as np
