@@ -483,16 +483,18 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
         for (int f = 0; f < nf; ++f) rptr[f + 1] += rptr[f];
         rnnz = (size_t)rptr[nf];
         if (rnnz) {
-            const size_t b_ridx = align256(rnnz * 4);
-            CK(cudaMalloc(&tc->rem_mem, b_rptr + 2 * b_ridx));
+            const size_t b_ridx = align256(rnnz * 4), b_rrow = align256(rnnz);
+            CK(cudaMalloc(&tc->rem_mem, b_rptr + 2 * b_ridx + b_rrow));
             char* p = static_cast<char*>(tc->rem_mem);
             CK(cudaMemcpyAsync(p, rptr.data(), (size_t)(nf + 1) * 4, cudaMemcpyHostToDevice, s->st));
             if (launch_rem_fill(s->ds, nkb, d_slot, reinterpret_cast<int*>(p), reinterpret_cast<int*>(p + b_rptr),
-                                reinterpret_cast<float*>(p + b_rptr + b_ridx), s->st))
+                                reinterpret_cast<float*>(p + b_rptr + b_ridx),
+                                reinterpret_cast<uint8_t*>(p + b_rptr + 2 * b_ridx), s->st))
                 return fail(ATPM_E_CUDA, "remainder fill: %s", cudaGetErrorString(cudaGetLastError()));
             s->ds.rem_ptr = reinterpret_cast<const int*>(p);
             s->ds.rem_idx = reinterpret_cast<const int*>(p + b_rptr);
             s->ds.rem_vf = reinterpret_cast<const float*>(p + b_rptr + b_ridx);
+            s->ds.rem_row = reinterpret_cast<const uint8_t*>(p + b_rptr + 2 * b_ridx);
             s->w32_bytes = align256((size_t)nf * w32_ld * 4);
             CK(cudaMalloc(&s->w32_mem, s->w32_bytes));
             CK(cudaMemsetAsync(s->w32_mem, 0, s->w32_bytes, s->st));

@@ -160,6 +160,7 @@ struct DevSolve {
     const int* rem_ptr;      // [nf+1], or null when every entry is in a tile
     const int* rem_idx;      // [rem_nnz]
     const float* rem_vf;     // [rem_nnz]
+    const uint8_t* rem_row;  // [rem_nnz] the entry's row within its 128-facet row block
     float* W32;              // [nf][w32_ld] FP32 (null without a remainder)
     int w32_ld;              // row stride of W32: ntau rounded up to 32 (the remainder's step chunks)
 };
@@ -248,7 +249,7 @@ int kernels_per_revolution(const Batch& b);          // kernels launch_revolutio
 int launch_tc_cells(const DevSolve& s, int nkb, unsigned* cmax, unsigned* cmask, unsigned* count, stream_t st);
 // the sparse remainder's per-row counts, then (rptr scanned) its lists in list order
 int launch_rem_count(const DevSolve& s, int nkb, const int* slot, int* count, stream_t st);
-int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf,
+int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf, uint8_t* rrow,
                     stream_t st);
 // cells whose tile needs the BF16 residual for some row's flux (need zeroed
 // by the caller); returns 1 when the shape is too large for the per-row maps

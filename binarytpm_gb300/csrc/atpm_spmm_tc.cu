@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(256) k_rem_count(DevSolve s, int nkb, const in
 }
 
 __global__ void __launch_bounds__(256) k_rem_fill(DevSolve s, int nkb, const int* slot, const int* rptr, int* ridx,
-                                                  float* rvf) {
+                                                  float* rvf, uint8_t* rrow) {
     const int f = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (f >= s.nf) return;  // warp-uniform
@@ -329,6 +329,7 @@ __global__ void __launch_bounds__(256) k_rem_fill(DevSolve s, int nkb, const int
             const int o = out + __popc(m & ((1u << lane) - 1u));
             ridx[o] = s.dep_idx[k];
             rvf[o] = s.dep_vf[k];
+            rrow[o] = (uint8_t)(f & 127);
         }
         out += __popc(m);
     }
@@ -341,11 +342,11 @@ int launch_rem_count(const DevSolve& s, int nkb, const int* slot, int* count, st
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
-int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf,
+int launch_rem_fill(const DevSolve& s, int nkb, const int* slot, const int* rptr, int* ridx, float* rvf, uint8_t* rrow,
                     stream_t stv) {
     cudaStream_t st = static_cast<cudaStream_t>(stv);
     const size_t threads = (size_t)s.nf * 32;
-    k_rem_fill<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, rptr, ridx, rvf);
+    k_rem_fill<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(s, nkb, slot, rptr, ridx, rvf, rrow);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
@@ -613,55 +614,111 @@ int tc_max_stages(int N) { return tc_stages(N); }
 
 // The sparse remainder of the product: the list entries of the cells too
 // sparse for a tensor-core tile, added to the tiles' Q in FP32.  One CTA per
-// (solve, 128-facet row block, 32-step chunk); a warp per facet row, lane j
-// on step s0 + j, so every entry is one coalesced 128-byte load of its
-// column facet's W32 row; entries accumulate in list order (four loads in
-// flight), the block's 128 x 32 sums go through shared memory, and Q is
-// updated along facets (coalesced).  Row blocks the tensor-core product
-// skips (all facets frozen) are skipped alike.
+// (solve, 128-facet row block, 32-step chunk), lane j of every warp on step
+// s0 + j, so each entry is one coalesced 128-byte load of its column facet's
+// W32 row.  The block's entries (rows in order, each row's in list order)
+// are cut into four contiguous ranges, one per warp; a warp reads 32
+// entries' column, value and row at once and keeps eight W32 loads in
+// flight across row boundaries, so the gather is not a chain of dependent
+// loads per row (a row holds ~3 remainder entries on average).  A row's sum
+// is the multiply-add chain over its entries in list order within each
+// warp's range; a row split between warps adds the warps' partial sums in
+// warp order after a barrier.  The block's 128 x 32 sums go through shared
+// memory and Q is updated along facets (coalesced).  Row blocks the
+// tensor-core product skips (all facets frozen) are skipped alike.
+// Earlier forms, a warp per facet row (one dependent index-then-W32 chain
+// per row: 1.80 ms for the product per batch revolution of the 8-inertia
+// binary), the same with the block's entries staged in shared memory first
+// (1.93 ms) and one CTA per row block looping over the chunks (2.43 ms),
+// were latency-bound.
 constexpr int REM_STEPS = 32;
+constexpr int REM_WARPS = 4;
+constexpr int REM_INFLIGHT = 8;
 
-__global__ void __launch_bounds__(128) k_spmm_rem(Batch b) {
+__global__ void __launch_bounds__(REM_WARPS * 32) k_spmm_rem(Batch b) {
     const DevSolve& sv = b.tab[blockIdx.z];
     const int rb = blockIdx.x, s0 = blockIdx.y * REM_STEPS;
     const int nf = sv.nf, ntau = sv.ntau;
     if (!sv.rem_ptr || rb * 128 >= nf || s0 >= ntau || !sv.ctl->active) return;
     const bool everyone = !sv.freeze || sv.ti == 0.0f;
     if (!everyone && !sv.rb_act[rb]) return;
+    const int f_lo = rb * 128, f_hi = min(nf, f_lo + 128);
+    const int e0 = __ldg(&sv.rem_ptr[f_lo]), e1 = __ldg(&sv.rem_ptr[f_hi]);
+    if (e0 == e1) return;  // no remainder entry in this block
     __shared__ float acc[128][REM_STEPS + 1];
-    __shared__ int any;
+    __shared__ float edge[REM_WARPS][REM_STEPS];
+    __shared__ int edge_row[REM_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) any = 0;
+    for (int i = threadIdx.x; i < 128 * (REM_STEPS + 1); i += blockDim.x) (&acc[0][0])[i] = 0.0f;
     __syncthreads();
     const float* W32 = sv.W32;
     const size_t ld = (size_t)sv.w32_ld;
     const int s = s0 + lane;  // W32 rows are padded to the chunk grid: s < w32_ld
-    for (int r = warp; r < 128; r += 4) {
-        const int f = rb * 128 + r;
-        float a = 0.0f;
-        if (f < nf) {
-            int k = __ldg(&sv.rem_ptr[f]);
-            const int k1 = __ldg(&sv.rem_ptr[f + 1]);
-            if (k < k1 && lane == 0) any = 1;
-            for (; k + 4 <= k1; k += 4) {
-                const int g0 = __ldg(&sv.rem_idx[k]), g1 = __ldg(&sv.rem_idx[k + 1]);
-                const int g2 = __ldg(&sv.rem_idx[k + 2]), g3 = __ldg(&sv.rem_idx[k + 3]);
-                const float w0 = W32[(size_t)g0 * ld + s], w1 = W32[(size_t)g1 * ld + s];
-                const float w2 = W32[(size_t)g2 * ld + s], w3 = W32[(size_t)g3 * ld + s];
-                a = fmaf(__ldg(&sv.rem_vf[k]), w0, a);
-                a = fmaf(__ldg(&sv.rem_vf[k + 1]), w1, a);
-                a = fmaf(__ldg(&sv.rem_vf[k + 2]), w2, a);
-                a = fmaf(__ldg(&sv.rem_vf[k + 3]), w3, a);
+    const int n = e1 - e0;
+    const int a0 = e0 + (int)(((long long)n * warp) / REM_WARPS);
+    const int a1 = e0 + (int)(((long long)n * (warp + 1)) / REM_WARPS);
+    // the warp's first row goes to its edge slot, every later row (which
+    // starts inside this range) straight to acc
+    int cur = -1;
+    bool first = true;
+    float a = 0.0f;
+    if (lane == 0) edge_row[warp] = -1;
+    for (int kb = a0; kb < a1; kb += 32) {
+        const int k = kb + lane;
+        const bool in = k < a1;
+        const int gk = in ? __ldg(&sv.rem_idx[k]) : 0;
+        const float vk = in ? __ldg(&sv.rem_vf[k]) : 0.0f;
+        const int rk = in ? (int)__ldg(&sv.rem_row[k]) : 0;
+        const int cnt = min(32, a1 - kb);
+        for (int j0 = 0; j0 < cnt; j0 += REM_INFLIGHT) {
+            float w[REM_INFLIGHT];
+#pragma unroll
+            for (int u = 0; u < REM_INFLIGHT; ++u) {
+                const int g = __shfl_sync(0xffffffffu, gk, (j0 + u) & 31);
+                w[u] = (j0 + u < cnt) ? W32[(size_t)g * ld + s] : 0.0f;
             }
-            for (; k < k1; ++k) a = fmaf(__ldg(&sv.rem_vf[k]), W32[(size_t)__ldg(&sv.rem_idx[k]) * ld + s], a);
+#pragma unroll
+            for (int u = 0; u < REM_INFLIGHT; ++u) {
+                const float v = __shfl_sync(0xffffffffu, vk, (j0 + u) & 31);
+                const int r = __shfl_sync(0xffffffffu, rk, (j0 + u) & 31);
+                if (j0 + u < cnt) {
+                    if (r != cur) {  // warp-uniform: the entry's row is the same on every lane
+                        if (cur >= 0) {
+                            if (first) {
+                                edge[warp][lane] = a;
+                                if (lane == 0) edge_row[warp] = cur;
+                                first = false;
+                            } else {
+                                acc[cur][lane] = a;
+                            }
+                        }
+                        cur = r;
+                        a = 0.0f;
+                    }
+                    a = fmaf(v, w[u], a);
+                }
+            }
         }
-        acc[r][lane] = a;
+    }
+    if (cur >= 0) {
+        if (first) {
+            edge[warp][lane] = a;
+            if (lane == 0) edge_row[warp] = cur;
+        } else {
+            acc[cur][lane] = a;
+        }
     }
     __syncthreads();
-    if (!any) return;  // no row of this block has a remainder entry
+    // the edge sums, in warp order
+    if (warp == 0)
+        for (int w = 0; w < REM_WARPS; ++w) {
+            const int r = edge_row[w];
+            if (r >= 0) acc[r][lane] = acc[r][lane] + edge[w][lane];
+        }
+    __syncthreads();
     float* Q = static_cast<float*>(sv.Q);
-    const int f = rb * 128 + threadIdx.x;
-    if (f >= nf || __ldg(&sv.rem_ptr[f]) == __ldg(&sv.rem_ptr[f + 1])) return;
+    const int f = f_lo + threadIdx.x;
+    if (f >= f_hi || __ldg(&sv.rem_ptr[f]) == __ldg(&sv.rem_ptr[f + 1])) return;
     for (int j = 0; j < REM_STEPS && s0 + j < ntau; ++j) {
         const size_t o = (size_t)(s0 + j) * nf + f;
         Q[o] = Q[o] + acc[threadIdx.x][j];
@@ -693,7 +750,7 @@ int launch_spmm_tc(const Batch& b, stream_t stv) {
     k_spmm_tc<<<grid, TC_THREADS, smem, st>>>(b);
     if (b.rem_nmb > 0) {
         const dim3 g((unsigned)b.rem_nmb, (unsigned)((b.rem_ntau + REM_STEPS - 1) / REM_STEPS), (unsigned)b.n);
-        k_spmm_rem<<<g, 128, 0, st>>>(b);
+        k_spmm_rem<<<g, REM_WARPS * 32, 0, st>>>(b);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
