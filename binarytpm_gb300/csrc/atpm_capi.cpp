@@ -2041,6 +2041,9 @@ ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q) {
     atpm_solve* one[1] = {s};
     atpm_status r = make_batch_for(one, 1, &b, &tmp);
     if (r) return r;
+    // every row block, frozen facets included: the flux of the current
+    // temperatures for every facet, not only the ones still advancing
+    CK(cudaMemsetAsync(s->ds.rb_act, 1, (size_t)(s->nf + 127) / 128, s->st));
     int rc = launch_revolution_part(b, 0, s->st);
     if (!rc) rc = launch_w_bf16_one(s->ds, s->st);
     if (!rc) rc = launch_revolution_part(b, 1, s->st);

@@ -175,7 +175,8 @@ ATPM_API atpm_status atpm_profile_revolution(atpm_solve* const* solves, int32_t 
                                              int64_t* facet_steps, int64_t* active_facets);
 /* Self-heating flux Q[s][f] = sum_g V[f][g] eps sigma T_g[s]^4 for the
  * current surface temperatures ([ntau][nf] step-major), through the solve's
- * own path (list-order gather, or the BF16 tensor-core product for FAST). */
+ * own path (list-order gather, or the BF16 tensor-core product for FAST),
+ * for every facet, frozen ones included. */
 ATPM_API atpm_status atpm_selfheating_flux(atpm_solve* s, float* q);
 /* Non-synchronous binary (the 175706 Thermal program,
  * 175706/Run-04/thermal.cpp:1347-1381, 860-869, 1925-1967): the first
