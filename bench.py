@@ -246,15 +246,17 @@ def activity(caps=(10, 25, 50, 75, 100, 150, 200, 250, 300)):
     print(json.dumps({"active_facets_per_solve": out, "thermal_inertia": tis, "nf": prob.nf}), flush=True)
 
 
-def profile_case(nsolves: int = 2):
+def profile_case(nsolves: int = 2, p_subdiv: int = 4):
     """A small, fast case of the same kernels for ncu --set full captures:
     the binary with a subdivision-4 primary (5,120 + 1,280 facets, NX = 56,
     NTAU = 720), ``nsolves`` FAST solves (thermal inertias from the batched
-    sweep), three instrumented revolutions."""
+    sweep), three instrumented revolutions.  With ``p_subdiv`` 5 it is the
+    headline binary (20,480 + 1,280 facets), for one-pass metric captures
+    (DRAM bytes and durations) at full size."""
     from binarytpm_gb300 import lib, workloads
 
     ctx = lib.Context(0)
-    prob = workloads.binary_problem(ctx, p_subdiv=4)
+    prob = workloads.binary_problem(ctx, p_subdiv=p_subdiv)
     s0 = lib.Solve(ctx, prob, precision=lib.FAST)
     s0.geometry_shadow()
     s0.scattering()
@@ -418,6 +420,8 @@ def main():
     ap.add_argument("--sweep-solves", type=int, default=256,
                     help="solves in the batched-sweep run (mixed sizes, albedos, inertias; 0: skip)")
     ap.add_argument("--profile-solves", type=int, default=2, help="solves in the --profile-case batch")
+    ap.add_argument("--profile-subdiv", type=int, default=4, choices=[4, 5],
+                    help="primary subdivision of the --profile-case binary (5: the headline binary)")
     ap.add_argument("--precision-stress", type=int, default=0, metavar="SUBDIV",
                     help="run the precision-stress configuration with this primary subdivision (6: 81,920 facets)")
     ap.add_argument("--activity", action="store_true",
@@ -432,7 +436,7 @@ def main():
         precision_stress(args.precision_stress)
         return
     if args.profile_case:
-        profile_case(args.profile_solves)
+        profile_case(args.profile_solves, args.profile_subdiv)
         return
     if args.activity:
         activity()
@@ -888,10 +892,11 @@ def _roofline(kern, n, prob, hbm, bf16, kind, cond_variant=4):
     """Dominant kernel of the revolution loop: the self-heating product
     (k_spmm_tc over the tensor-core tiles, then k_spmm_rem over the FP32
     sparse remainder; timed together).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
-    BF16 + 4 B index) + 8 F NTAU bytes per solve, is ~52 FLOP/B, below the
+    BF16 + 4 B index) + 8 F NTAU bytes per solve, is ~65 FLOP/B, below the
     GB300 ridge (~290), so the bound is HBM: achieved = algorithmic bytes per
     launch (view factors once, shared by the batch's clones; W read and Q
-    written per solve) / CUDA-event duration.  The tensor-pipe figures are
+    written per solve) / CUDA-event duration; traffic = both kernels' ncu
+    DRAM bytes per batch revolution, measured on the headline binary.  The tensor-pipe figures are
     beside it: algorithmic FLOP/s, and executed = every issued 128x16 K
     slice x step chunk x (2 or 3 BF16 products for the hi/lo compensation).
     The conduction sweep is reported beside it."""
