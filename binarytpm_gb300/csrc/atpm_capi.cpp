@@ -557,6 +557,7 @@ Batch make_batch(atpm_context* ctx, const DevSolve* tab, int n, const int4* wm, 
     b.sms = ctx->sm_count;
     b.rem_nmb = 0;
     b.rem_ntau = 0;
+    b.side = b.ev_fork = b.ev_join = nullptr;
     return b;
 }
 
@@ -568,6 +569,26 @@ void set_remainder_grid(Batch& b, atpm_solve* const* solves, int n) {
         if (!d.rem_ptr) continue;
         b.rem_nmb = std::max(b.rem_nmb, (d.nf + 127) / 128);
         b.rem_ntau = std::max(b.rem_ntau, d.ntau);
+    }
+    // the leader's side stream and events, so the remainder can run beside
+    // the product (without them it runs after it: same sums)
+    atpm_solve* s0 = solves[0];
+    if (b.rem_nmb > 0 && !s0->side_st) {
+        if (cudaStreamCreateWithFlags(&s0->side_st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s0->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s0->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            if (s0->side_st) cudaStreamDestroy(s0->side_st);
+            if (s0->ev_fork) cudaEventDestroy(s0->ev_fork);
+            if (s0->ev_join) cudaEventDestroy(s0->ev_join);
+            s0->side_st = nullptr;
+            s0->ev_fork = s0->ev_join = nullptr;
+        }
+    }
+    if (b.rem_nmb > 0 && s0->side_st) {
+        b.side = s0->side_st;
+        b.ev_fork = s0->ev_fork;
+        b.ev_join = s0->ev_join;
     }
 }
 
@@ -1113,6 +1134,12 @@ ATPM_API atpm_status atpm_solve_destroy(atpm_solve* s) {
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->side_st) {
+        cudaStreamSynchronize(s->side_st);
+        cudaStreamDestroy(s->side_st);
+    }
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->wmap) cudaFree(s->wmap);
     if (s->fmap) cudaFree(s->fmap);
     if (s->ds_dev) cudaFree(s->ds_dev);

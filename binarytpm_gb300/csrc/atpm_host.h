@@ -65,6 +65,11 @@ struct atpm_solve {
     size_t wb_bytes = 0;
     void* w32_mem = nullptr;  // this solve's FP32 W rows for the sparse remainder
     size_t w32_bytes = 0;
+    // the stream the sparse remainder of a batch this solve leads runs on
+    // beside the tensor-core product, and its fork / join events (made on
+    // first use)
+    cudaStream_t side_st = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // the last atpm_geometry_shadow's shadow drivers
     double last_shadow_ms = 0.0;
     int64_t last_shadow_rays = 0, last_shadow_tests = -1;

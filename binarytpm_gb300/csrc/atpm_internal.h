@@ -117,7 +117,8 @@ struct DevSolve {
     void* stemp1;            // [ntau][nf] R
     void* temp;              // [nx+1][nf] R
     void* Q;                 // [ntau][nf] R
-    void* W;                 // [nf][ntau] R
+    void* W;                 // [nf][ntau] R (FAST with tensor-core tiles: the sparse remainder's
+                             // sums, [ntau][nf] FP32, which k_rem_add adds to Q)
     uint8_t* conv;           // [nf] frozen (reference astconverged)
     uint8_t* hot;            // [nf] some |stemp1-stemp0| >= TACC this revolution
     // facets still active after each convergence test (FAST, freeze on),
@@ -233,6 +234,12 @@ struct Batch {
     int sms;                 // SMs of the device (persistent tensor-core grid)
     int rem_nmb, rem_ntau;   // largest row-block count / steps of the batch's solves with a
                              // sparse remainder (0: none; the remainder kernel's grid)
+    // host handles: a second stream on which the remainder runs beside the
+    // tensor-core product (forked and joined with the two events; null: the
+    // remainder runs after the product on the batch's stream)
+    void* side;
+    void* ev_fork;
+    void* ev_join;
 };
 // deepest tensor-core pipeline that fits shared memory for step chunk N
 int tc_max_stages(int N);

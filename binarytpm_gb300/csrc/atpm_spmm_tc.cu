@@ -624,7 +624,8 @@ int tc_max_stages(int N) { return tc_stages(N); }
 // is the multiply-add chain over its entries in list order within each
 // warp's range; a row split between warps adds the warps' partial sums in
 // warp order after a barrier.  The block's 128 x 32 sums go through shared
-// memory and Q is updated along facets (coalesced).  Row blocks the
+// memory into the remainder's own array (along facets, coalesced), which
+// k_rem_add adds to Q once the tensor-core product is complete.  Row blocks the
 // tensor-core product skips (all facets frozen) are skipped alike.
 // Earlier forms, a warp per facet row (one dependent index-then-W32 chain
 // per row: 1.80 ms for the product per batch revolution of the 8-inertia
@@ -716,12 +717,29 @@ __global__ void __launch_bounds__(REM_WARPS * 32) k_spmm_rem(Batch b) {
             if (r >= 0) acc[r][lane] = acc[r][lane] + edge[w][lane];
         }
     __syncthreads();
-    float* Q = static_cast<float*>(sv.Q);
+    float* R = static_cast<float*>(sv.W);
     const int f = f_lo + threadIdx.x;
     if (f >= f_hi || __ldg(&sv.rem_ptr[f]) == __ldg(&sv.rem_ptr[f + 1])) return;
+    for (int j = 0; j < REM_STEPS && s0 + j < ntau; ++j) R[(size_t)(s0 + j) * nf + f] = acc[threadIdx.x][j];
+}
+
+// Q += the remainder's sums, for the rows k_spmm_rem summed (same grid and
+// the same tests): runs once both the tensor-core product and the remainder
+// are complete, so the two can run side by side.
+__global__ void __launch_bounds__(128) k_rem_add(Batch b) {
+    const DevSolve& sv = b.tab[blockIdx.z];
+    const int rb = blockIdx.x, s0 = blockIdx.y * REM_STEPS;
+    const int nf = sv.nf, ntau = sv.ntau;
+    if (!sv.rem_ptr || rb * 128 >= nf || s0 >= ntau || !sv.ctl->active) return;
+    const bool everyone = !sv.freeze || sv.ti == 0.0f;
+    if (!everyone && !sv.rb_act[rb]) return;
+    const int f = rb * 128 + threadIdx.x;
+    if (f >= nf || __ldg(&sv.rem_ptr[f]) == __ldg(&sv.rem_ptr[f + 1])) return;
+    float* Q = static_cast<float*>(sv.Q);
+    const float* R = static_cast<const float*>(sv.W);
     for (int j = 0; j < REM_STEPS && s0 + j < ntau; ++j) {
         const size_t o = (size_t)(s0 + j) * nf + f;
-        Q[o] = Q[o] + acc[threadIdx.x][j];
+        Q[o] = Q[o] + R[o];
     }
 }
 
@@ -747,10 +765,28 @@ int launch_spmm_tc(const Batch& b, stream_t stv) {
     if (cudaMemsetAsync(b.tc_work, 0, 2 * sizeof(int), st) != cudaSuccess) return 2;
     k_tc_compact<<<(b.nq + 127) / 128, 128, 0, st>>>(b);
     const int grid = b.nq < b.sms ? b.nq : b.sms;  // one persistent CTA per SM
+    // The sparse remainder (latency-bound gathers) runs beside the product
+    // (latency-bound on its copy ring) on the side stream, into its own sums.
+    // Submitting the remainder first was measured faster on the 8-inertia
+    // binary (two batch groups): 16.1 against 17.2 ms for the 6-revolution
+    // step, 255.5 against 260.5 ms solved to convergence.
+    const dim3 g((unsigned)b.rem_nmb, (unsigned)((b.rem_ntau + REM_STEPS - 1) / REM_STEPS), (unsigned)b.n);
+    cudaStream_t side = static_cast<cudaStream_t>(b.side);
+    const bool fork = b.rem_nmb > 0 && side && b.ev_fork && b.ev_join;
+    if (fork) {
+        cudaEvent_t ef = static_cast<cudaEvent_t>(b.ev_fork), ej = static_cast<cudaEvent_t>(b.ev_join);
+        if (cudaEventRecord(ef, st) != cudaSuccess || cudaStreamWaitEvent(side, ef, 0) != cudaSuccess) return 2;
+        k_spmm_rem<<<g, REM_WARPS * 32, 0, side>>>(b);
+        if (cudaEventRecord(ej, side) != cudaSuccess) return 2;
+    }
     k_spmm_tc<<<grid, TC_THREADS, smem, st>>>(b);
     if (b.rem_nmb > 0) {
-        const dim3 g((unsigned)b.rem_nmb, (unsigned)((b.rem_ntau + REM_STEPS - 1) / REM_STEPS), (unsigned)b.n);
-        k_spmm_rem<<<g, REM_WARPS * 32, 0, st>>>(b);
+        if (fork) {
+            if (cudaStreamWaitEvent(st, static_cast<cudaEvent_t>(b.ev_join), 0) != cudaSuccess) return 2;
+        } else {
+            k_spmm_rem<<<g, REM_WARPS * 32, 0, st>>>(b);
+        }
+        k_rem_add<<<g, 128, 0, st>>>(b);
     }
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

@@ -1069,8 +1069,8 @@ int launch_revolution_part(const Batch& b, int part, stream_t stv) {
 
 int kernels_per_revolution(const Batch& b) {
     const bool tc = b.mode == MODE_FAST && b.nq > 0;
-    // k_tc_compact + k_spmm_tc (+ k_spmm_rem), or W + Q
-    const int selfheat = tc ? 2 + (b.rem_nmb > 0 ? 1 : 0) : (b.nw > 0 ? 2 : 0);
+    // k_tc_compact + k_spmm_tc (+ k_spmm_rem, k_rem_add), or W + Q
+    const int selfheat = tc ? 2 + (b.rem_nmb > 0 ? 2 : 0) : (b.nw > 0 ? 2 : 0);
     // + k_tail_mode, k_conduction_warp (+ k_conduction_pairs)
     const int conduction = b.mode == MODE_FAST ? (b.cond_variant == 4 ? 4 : 3) : 1;
     return selfheat + conduction + 2;                    // + k_converge, k_advance
