@@ -1003,8 +1003,9 @@ def e2e_run(ctx, prob, tis, steps):
         lib.batch_run(solves)
         t = mark("batched_revolutions", t)
         fs = solves[0].last_run_stats()[2]
-        # the stage's result: every facet's surface temperature at every step
-        temps = [s.result_temperature(out=o) for s, o in zip(solves, outs)]
+        # the stage's result: every facet's surface temperature at every step,
+        # the solves' copies overlapping
+        temps = lib.result_temperatures(solves, outs)
         torch.cuda.synchronize()
         t = mark("temperatures_d2h", t)
         dt = time.perf_counter() - t0

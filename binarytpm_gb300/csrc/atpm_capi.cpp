@@ -1719,6 +1719,34 @@ ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out) {
     return ATPM_OK;
 }
 
+ATPM_API atpm_status atpm_get_surface_temperatures(atpm_solve* const* solves, int32_t n, float* const* stemp1) {
+    if (!solves || !stemp1 || n < 0) return fail(ATPM_E_INVALID, "null argument");
+    for (int i = 0; i < n; ++i)
+        if (!solves[i] || !stemp1[i]) return fail(ATPM_E_INVALID, "null solve or output %d", i);
+    if (n == 0) return ATPM_OK;
+    CK(cudaSetDevice(solves[0]->ctx->device));
+    cudaError_t e = cudaSuccess;
+    int issued = 0;
+    for (; issued < n && e == cudaSuccess; ++issued) {
+        atpm_solve* s = solves[issued];
+        const size_t nt = s->P.ntau, nf = s->nf;
+        void* tmp = nullptr;
+        e = cudaMallocAsync(&tmp, nt * nf * 4, s->st);
+        if (e != cudaSuccess) break;
+        if (launch_transpose(s->ds.stemp1, (int)s->rs, tmp, 4, nt, nf, s->st)) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(stemp1[issued], tmp, nt * nf * 4, cudaMemcpyDeviceToHost, s->st);
+        cudaFreeAsync(tmp, s->st);
+    }
+    cudaError_t e2 = cudaSuccess;
+    for (int i = 0; i < issued; ++i) {
+        const cudaError_t ei = cudaStreamSynchronize(solves[i]->st);
+        if (e2 == cudaSuccess) e2 = ei;
+    }
+    if (e != cudaSuccess) return fail(ATPM_E_CUDA, "surface temperatures: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(ATPM_E_CUDA, "surface temperatures: %s", cudaGetErrorString(e2));
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0) {
     if (!s) return fail(ATPM_E_INVALID, "null solve");
     CK(cudaSetDevice(s->ctx->device));

@@ -101,11 +101,20 @@ __global__ void __launch_bounds__(256) k_geom_facets(GeomArgs a) {
     n[1] = DDIV(n[1], nn);
     n[2] = DDIV(n[2], nn);
     const double iv2 = -DADD(DADD(DMUL(n[0], hm[0]), DMUL(n[1], hm[1])), DMUL(n[2], hm[2]));
-    const double ia = acos(DDIV(iv2, t));
+    const double ci = DDIV(iv2, t);
     const size_t o = (size_t)f * ntau + s;
-    if (MODE == MODE_FP64) static_cast<double*>(a.s.cosil)[o] = cos(ia);
-    else static_cast<float*>(a.s.cosil)[o] = (float)cos(ia);
-    a.s.shadow[o] = (ia > (3.141592653589793 / 2.0)) ? 0 : 1;
+    if (MODE == MODE_FAST) {
+        // FAST: the cosine itself (cos(acos(x)) is x up to its last bits,
+        // and the FP64 transcendentals are most of this kernel's time on a
+        // part whose FP64 rate is 1/64 of FP32); dark when it is negative
+        static_cast<float*>(a.s.cosil)[o] = (float)ci;
+        a.s.shadow[o] = ci < 0.0 ? 0 : 1;
+    } else {
+        const double ia = acos(ci);
+        if (MODE == MODE_FP64) static_cast<double*>(a.s.cosil)[o] = cos(ia);
+        else static_cast<float*>(a.s.cosil)[o] = (float)cos(ia);
+        a.s.shadow[o] = (ia > (3.141592653589793 / 2.0)) ? 0 : 1;
+    }
     double* hmo = a.g.hm + o * 3;
     double* no = a.g.nrm + o * 3;
 #pragma unroll
@@ -566,6 +575,7 @@ int launch_geometry(const DevSolve& s, const GeomWork& g, stream_t stv) {
     const long long nvt = (long long)s.nv * s.ntau, nft = (long long)s.nf * s.ntau;
     k_geom_vertices<<<(unsigned)((nvt + 255) / 256), 256, 0, st>>>(a);
     if (s.mode == MODE_FP64) k_geom_facets<MODE_FP64><<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a);
+    else if (s.mode == MODE_FAST) k_geom_facets<MODE_FAST><<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a);
     else k_geom_facets<MODE_REF><<<(unsigned)((nft + 255) / 256), 256, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }

@@ -64,6 +64,7 @@ _SIGS = {
     "atpm_get_illumination": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_get_surface_temperature": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "atpm_get_surface_temperature64": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "atpm_get_surface_temperatures": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "atpm_get_depth_temperature": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_get_converged": (C.c_int, [C.c_void_p, C.c_void_p]),
     "atpm_energy_balance": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -456,6 +457,24 @@ def batch_run(solves):
     counts = np.zeros((n, cap), np.int32)
     _ck(load().atpm_batch_run(arr, n, _p(nrev), _p(counts)))
     return [counts[i, : nrev[i]].copy() for i in range(n)]
+
+
+def result_temperatures(solves, outs=None):
+    """The Thermal stage's result of several solves at once
+    (atpm_get_surface_temperatures): each solve's [nf][ntau] FP32 surface
+    temperatures, their copies to the host overlapping.  ``outs``: arrays to
+    fill (page-locked ones from host_buffer copy fastest)."""
+    n = len(solves)
+    if outs is None:
+        outs = [_host_out((s.nf, s.ntau), np.float32) for s in solves]
+    else:
+        outs = [_out_arg(o, (s.nf, s.ntau), np.float32, "out") for s, o in zip(solves, outs)]
+    if len(outs) != n:
+        raise ValueError("one output per solve")
+    arr = (C.c_void_p * n)(*[s.h.value for s in solves])
+    ptrs = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+    _ck(load().atpm_get_surface_temperatures(arr, n, ptrs))
+    return outs
 
 
 def footprint(problem, precision: int, revcap: int = 301) -> int:

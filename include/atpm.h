@@ -161,6 +161,11 @@ ATPM_API atpm_status atpm_get_shadow(atpm_solve* s, int32_t* out);
 ATPM_API atpm_status atpm_get_illumination(atpm_solve* s, float* out);
 ATPM_API atpm_status atpm_get_surface_temperature(atpm_solve* s, float* stemp1, float* stemp0);
 ATPM_API atpm_status atpm_get_surface_temperature64(atpm_solve* s, double* stemp1);
+/* The Thermal stage's result of n solves at once: stemp1[i] receives solve
+ * i's surface temperatures as atpm_get_surface_temperature does ([nf][ntau]
+ * FP32).  Each solve's transpose and copy run on its own stream, so the
+ * copies to the host overlap; the call returns when all have landed. */
+ATPM_API atpm_status atpm_get_surface_temperatures(atpm_solve* const* solves, int32_t n, float* const* stemp1);
 ATPM_API atpm_status atpm_get_depth_temperature(atpm_solve* s, float* temp /* [nf][nx+1] */);
 /* (float)cos of the Sun angle of every facet and step ([nf][ntau]). */
 ATPM_API atpm_status atpm_get_cosillum(atpm_solve* s, float* out);

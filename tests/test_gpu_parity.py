@@ -233,3 +233,23 @@ def test_albedo_change_on_a_clone_matches_a_fresh_solve(gpu_ctx, precision):
     assert np.array_equal(c.surface_temperature()[0].view(np.uint32), f.surface_temperature()[0].view(np.uint32))
     for x in (s0, c, f):
         x.close()
+
+
+def test_surface_temperatures_of_several_solves_at_once(gpu_ctx):
+    """atpm_get_surface_temperatures (overlapping copies, one stream per
+    solve) returns each solve's result exactly as the one-solve getter."""
+    from binarytpm_gb300 import lib
+
+    prob, ref = golden("binary_s3s1")
+    solves = []
+    for prec, ti in ((lib.REFERENCE, 200.0), (lib.FAST, 50.0), (lib.FP64, 400.0)):
+        s = lib.Solve(gpu_ctx, prob, precision=prec, revcap=8)
+        s.set_forcing(ref["shadow"], ref["illumination"])
+        s.set_thermal_inertia(ti)
+        s.initialise_temperatures()
+        s.run()
+        solves.append(s)
+    many = lib.result_temperatures(solves)
+    for s, t in zip(solves, many):
+        assert np.array_equal(t.view(np.uint32), s.result_temperature().view(np.uint32))
+        s.close()
