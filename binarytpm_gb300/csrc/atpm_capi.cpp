@@ -313,6 +313,18 @@ int warp_tail_per_sm() {
     return v >= 1 && v <= 64 ? v : 12;
 }
 
+// Device memory of solves and batches comes from the device's
+// stream-ordered pool (cudaMallocAsync), which the context sets to keep
+// released memory for reuse: a job that creates and destroys solves then
+// allocates from what the previous job released instead of mapping new
+// pages.  The stream is synchronised, so the memory is usable from any
+// stream when this returns.
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t st) {
+    cudaError_t e = cudaMallocAsync(p, bytes, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
 // Fewest list entries a (128-row, 64-column) cell needs to become a
 // tensor-core tile (ATPM_TC_MIN_ENTRIES, 1..8192, default 32).  The entries of
 // sparser cells form the per-row remainder, summed in FP32 against W32 by
@@ -397,7 +409,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     {
         std::vector<unsigned> cmax(ncell), cmask(ncell), cnt(ncell);
         unsigned* dc = nullptr;
-        CK(cudaMalloc((void**)&dc, ncell * 4 * sizeof(unsigned)));
+        CK(cudaMallocAsync((void**)&dc, ncell * 4 * sizeof(unsigned), s->st));
         cudaError_t e = cudaMemsetAsync(dc, 0, ncell * 4 * sizeof(unsigned), s->st);
         if (e == cudaSuccess && launch_tc_cells(s->ds, nkb, dc, dc + ncell, dc + 3 * ncell, s->st))
             e = cudaGetLastError();
@@ -410,7 +422,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(cnt.data(), dc + 3 * ncell, ncell * sizeof(unsigned), cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-        cudaFree(dc);
+        cudaFreeAsync(dc, s->st);
         if (e != cudaSuccess) return fail(ATPM_E_CUDA, "tile structure: %s", cudaGetErrorString(e));
         for (size_t c = 0; c < ncell; ++c) {
             if (!cmax[c] || cnt[c] < min_entries) continue;  // empty, or left to the remainder
@@ -453,8 +465,8 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     tc->tiles = ntiles;
     tc->rb_tiles.resize(nmb);
     for (int mb = 0; mb < nmb; ++mb) tc->rb_tiles[mb] = tptr[mb + 1] - tptr[mb];
-    CK(cudaMalloc(&tc->mem, tc->bytes));
-    CK(cudaMalloc(&s->wb_mem, b_w));
+    CK(pool_alloc(&tc->mem, tc->bytes, s->st));
+    CK(pool_alloc(&s->wb_mem, b_w, s->st));
     s->wb_bytes = b_w;
     char* m = static_cast<char*>(tc->mem);
     char* p_lo = m + b_tiles + b_ptr + b_col;
@@ -472,19 +484,19 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     const size_t b_rptr = align256((size_t)(nf + 1) * 4);
     {
         int* cnt_d = nullptr;
-        CK(cudaMalloc((void**)&cnt_d, (size_t)nf * 4));
+        CK(cudaMallocAsync((void**)&cnt_d, (size_t)nf * 4, s->st));
         std::vector<int> rptr(nf + 1, 0);
         int rc = launch_rem_count(s->ds, nkb, d_slot, cnt_d, s->st);
         cudaError_t e = rc ? cudaGetLastError() : cudaMemcpyAsync(rptr.data() + 1, cnt_d, (size_t)nf * 4,
                                                                    cudaMemcpyDeviceToHost, s->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-        cudaFree(cnt_d);
+        cudaFreeAsync(cnt_d, s->st);
         if (e != cudaSuccess) return fail(ATPM_E_CUDA, "remainder count: %s", cudaGetErrorString(e));
         for (int f = 0; f < nf; ++f) rptr[f + 1] += rptr[f];
         rnnz = (size_t)rptr[nf];
         if (rnnz) {
             const size_t b_ridx = align256(rnnz * 4), b_rrow = align256(rnnz);
-            CK(cudaMalloc(&tc->rem_mem, b_rptr + 2 * b_ridx + b_rrow));
+            CK(pool_alloc(&tc->rem_mem, b_rptr + 2 * b_ridx + b_rrow, s->st));
             char* p = static_cast<char*>(tc->rem_mem);
             CK(cudaMemcpyAsync(p, rptr.data(), (size_t)(nf + 1) * 4, cudaMemcpyHostToDevice, s->st));
             if (launch_rem_fill(s->ds, nkb, d_slot, reinterpret_cast<int*>(p), reinterpret_cast<int*>(p + b_rptr),
@@ -496,7 +508,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
             s->ds.rem_vf = reinterpret_cast<const float*>(p + b_rptr + b_ridx);
             s->ds.rem_row = reinterpret_cast<const uint8_t*>(p + b_rptr + 2 * b_ridx);
             s->w32_bytes = align256((size_t)nf * w32_ld * 4);
-            CK(cudaMalloc(&s->w32_mem, s->w32_bytes));
+            CK(pool_alloc(&s->w32_mem, s->w32_bytes, s->st));
             CK(cudaMemsetAsync(s->w32_mem, 0, s->w32_bytes, s->st));
             CK(cudaStreamSynchronize(s->st));  // rptr must outlive its copy
         }
@@ -522,7 +534,7 @@ atpm_status build_tc(atpm_solve* s, const atpm_shape* sh) {
     atpm_solve* one[1] = {s};
     build_tc_items(one, 1, q);
     tc_map_extend(q);
-    CK(cudaMalloc(&s->qmap, q.size() * sizeof(int4)));
+    CK(pool_alloc(reinterpret_cast<void**>(&s->qmap), q.size() * sizeof(int4), s->st));
     CK(cudaMemcpy(s->qmap, q.data(), q.size() * sizeof(int4), cudaMemcpyHostToDevice));
     s->nq = (int)q.size();  // map entries (items, list, counters)
     return ATPM_OK;
@@ -620,7 +632,7 @@ atpm_status make_batch_for(atpm_solve* const* solves, int n, Batch* out, void** 
     const size_t bf = align256(fm.size() * sizeof(int2));
     tc_map_extend(qm);
     const size_t bq = align256(std::max<size_t>(qm.size(), 1) * sizeof(int4));
-    CK(cudaMalloc(tmp, bt + bw + bf + bq));
+    CK(pool_alloc(tmp, bt + bw + bf + bq, s0->st));
     char* t = static_cast<char*>(*tmp);
     CK(cudaMemcpy(t, tab.data(), n * sizeof(DevSolve), cudaMemcpyHostToDevice));
     if (!wm.empty()) CK(cudaMemcpy(t + bt, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice));
@@ -968,6 +980,13 @@ ATPM_API atpm_status atpm_context_create(int32_t device, atpm_context** out) {
     CK(cudaSetDevice(device));
     int sms = 1;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    // the stream-ordered pool the solves allocate from keeps what they
+    // release for the next ones (a per-process allocator setting)
+    cudaMemPool_t pool = nullptr;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     auto* c = new atpm_context();
     c->device = device;
     c->sm_count = sms;
@@ -1065,13 +1084,22 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     Layout L = layout(s->nv, s->nf, s->nnz, *P);
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) { atpm_context_release(s->ctx); delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
-    e = cudaMalloc(&s->arena, L.total);
+    e = pool_alloc(&s->arena, L.total, s->st);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s->st);
         atpm_context_release(s->ctx); delete s;
         return fail(ATPM_E_NOMEM, "cudaMalloc(%zu): %s", L.total, cudaGetErrorString(e));
     }
     s->arena_bytes = L.total;
+    // every array starts at zero, as the reference's do (the pool hands out
+    // memory that earlier solves used)
+    e = cudaMemsetAsync(s->arena, 0, L.total, s->st);
+    if (e != cudaSuccess) {
+        cudaFree(s->arena);
+        cudaStreamDestroy(s->st);
+        atpm_context_release(s->ctx); delete s;
+        return fail(ATPM_E_CUDA, "arena clear: %s", cudaGetErrorString(e));
+    }
     char* a = static_cast<char*>(s->arena);
     DevSolve& d = s->ds;
     d.nf = s->nf; d.nv = s->nv; d.ntau = P->ntau; d.nx = P->nx; d.revcap = P->revcap;
@@ -1092,7 +1120,7 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
     if (e != cudaSuccess) goto cuda_fail;
     e = cudaMemsetAsync(d.rb_act, 1, (size_t)(s->nf + 127) / 128, s->st);  // every row block active
     if (e != cudaSuccess) goto cuda_fail;
-    e = cudaMalloc(&s->ds_dev, sizeof(DevSolve));
+    e = pool_alloc(reinterpret_cast<void**>(&s->ds_dev), sizeof(DevSolve), s->st);
     if (e != cudaSuccess) goto cuda_fail;
     {
         std::vector<int4> wm;
@@ -1100,9 +1128,9 @@ ATPM_API atpm_status atpm_solve_create(atpm_context* ctx, const atpm_shape* sh, 
         build_maps(s->nf, P->ntau, 0, wm, fm);
         s->nw = s->nnz > 0 ? (int)wm.size() : 0;
         s->nfb = (int)fm.size();
-        e = cudaMalloc(&s->wmap, std::max<size_t>(wm.size(), 1) * sizeof(int4));
+        e = pool_alloc(reinterpret_cast<void**>(&s->wmap), std::max<size_t>(wm.size(), 1) * sizeof(int4), s->st);
         if (e != cudaSuccess) goto cuda_fail;
-        e = cudaMalloc(&s->fmap, fm.size() * sizeof(int2));
+        e = pool_alloc(reinterpret_cast<void**>(&s->fmap), fm.size() * sizeof(int2), s->st);
         if (e != cudaSuccess) goto cuda_fail;
         e = cudaMemcpyAsync(s->wmap, wm.data(), wm.size() * sizeof(int4), cudaMemcpyHostToDevice, s->st);
         if (e != cudaSuccess) goto cuda_fail;
@@ -1181,7 +1209,7 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
     s->ds = src->ds;  // scalars; device pointers rebased below
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) { atpm_context_release(s->ctx); delete s; return fail(ATPM_E_CUDA, "stream: %s", cudaGetErrorString(e)); }
-    e = cudaMalloc(&s->arena, src->arena_bytes);
+    e = pool_alloc(&s->arena, src->arena_bytes, s->st);
     if (e != cudaSuccess) {
         cudaStreamDestroy(s->st);
         atpm_context_release(s->ctx); delete s;
@@ -1190,9 +1218,9 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
     s->arena_bytes = src->arena_bytes;
     wire_arena(s, layout(s->nv, s->nf, s->nnz, s->P));
     e = cudaMemcpyAsync(s->arena, src->arena, s->arena_bytes, cudaMemcpyDeviceToDevice, s->st);
-    if (e == cudaSuccess) e = cudaMalloc(&s->ds_dev, sizeof(DevSolve));
-    if (e == cudaSuccess) e = cudaMalloc(&s->wmap, std::max<size_t>((size_t)s->nw, 1) * sizeof(int4));
-    if (e == cudaSuccess) e = cudaMalloc(&s->fmap, (size_t)s->nfb * sizeof(int2));
+    if (e == cudaSuccess) e = pool_alloc(reinterpret_cast<void**>(&s->ds_dev), sizeof(DevSolve), s->st);
+    if (e == cudaSuccess) e = pool_alloc(reinterpret_cast<void**>(&s->wmap), std::max<size_t>((size_t)s->nw, 1) * sizeof(int4), s->st);
+    if (e == cudaSuccess) e = pool_alloc(reinterpret_cast<void**>(&s->fmap), (size_t)s->nfb * sizeof(int2), s->st);
     if (e == cudaSuccess && s->nw)
         e = cudaMemcpyAsync(s->wmap, src->wmap, (size_t)s->nw * sizeof(int4), cudaMemcpyDeviceToDevice, s->st);
     if (e == cudaSuccess)
@@ -1201,7 +1229,7 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
         // the tiles are read-only: shared; W is this solve's own
         s->tc = src->tc;
         ++s->tc->refs;
-        e = cudaMalloc(&s->wb_mem, src->wb_bytes);
+        e = pool_alloc(&s->wb_mem, src->wb_bytes, s->st);
         if (e == cudaSuccess) {
             s->wb_bytes = src->wb_bytes;
             e = cudaMemcpyAsync(s->wb_mem, src->wb_mem, s->wb_bytes, cudaMemcpyDeviceToDevice, s->st);
@@ -1209,7 +1237,7 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
         }
         s->ds.W32 = nullptr;
         if (e == cudaSuccess && src->w32_mem) {
-            e = cudaMalloc(&s->w32_mem, src->w32_bytes);
+            e = pool_alloc(&s->w32_mem, src->w32_bytes, s->st);
             if (e == cudaSuccess) {
                 s->w32_bytes = src->w32_bytes;
                 e = cudaMemcpyAsync(s->w32_mem, src->w32_mem, s->w32_bytes, cudaMemcpyDeviceToDevice, s->st);
@@ -1218,7 +1246,7 @@ ATPM_API atpm_status atpm_solve_clone(atpm_solve* src, atpm_solve** out) {
         }
     }
     if (e == cudaSuccess && src->qmap) {
-        e = cudaMalloc(&s->qmap, (size_t)s->nq * sizeof(int4));
+        e = pool_alloc(reinterpret_cast<void**>(&s->qmap), (size_t)s->nq * sizeof(int4), s->st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(s->qmap, src->qmap, (size_t)s->nq * sizeof(int4), cudaMemcpyDeviceToDevice, s->st);
     }
