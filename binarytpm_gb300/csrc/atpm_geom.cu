@@ -18,7 +18,8 @@
 // inside its bounding box: a box test (FP32, padded far beyond the FP64
 // test's rounding) rejects every other pair before the exact FP64 test.
 //   k_proj           projected vertex coordinates of every step
-//   k_shadow_dep_cull the dependent-list driver with the box test in front
+//   k_window_box     each facet's box over every window of 32 steps
+//   k_shadow_dep_cull the dependent-list driver with the box tests in front
 //   k_grid_*         a uniform grid per step over the projected facets
 //                    (one cell per facet, by its box centre; cell size the
 //                    largest box), built by counting sort
@@ -221,6 +222,7 @@ struct ProjArgs {
     float pad;                  // box padding (km)
     float2* uv;                 // [nv][ntau]
     unsigned* stats;            // [0] max |u|,|v| (float bits), [1] max box extent, [2] bad-projection flag
+    float4* wbox;               // [nf][ceil(ntau/32)] union of each facet's padded boxes over 32 steps (or null)
 };
 
 __global__ void __launch_bounds__(256) k_proj(GeomArgs a, ProjArgs p) {
@@ -245,6 +247,23 @@ __device__ __forceinline__ float4 facet_box(const GeomArgs& a, const ProjArgs& p
                  q2 = p.uv[(size_t)hv[2] * ntau + s];
     return make_float4(fminf(q0.x, fminf(q1.x, q2.x)) - p.pad, fmaxf(q0.x, fmaxf(q1.x, q2.x)) + p.pad,
                        fminf(q0.y, fminf(q1.y, q2.y)) - p.pad, fmaxf(q0.y, fmaxf(q1.y, q2.y)) + p.pad);
+}
+
+// each facet's padded box over every window of 32 steps (the union of its
+// 32 per-step boxes): a warp of the dependent-list driver covers one window,
+// and an occluder whose window box misses the box around the warp's lit
+// points cannot pass any lane's per-step box test
+__global__ void __launch_bounds__(256) k_window_box(GeomArgs a, ProjArgs p) {
+    const int ntau = a.s.ntau, nw = (ntau + 31) / 32;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)a.s.nf * nw) return;
+    const int h = (int)(i / nw), w = (int)(i % nw);
+    float4 u = make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+    for (int s = w * 32; s < min(ntau, w * 32 + 32); ++s) {
+        const float4 b = facet_box(a, p, h, s);
+        u = make_float4(fminf(u.x, b.x), fmaxf(u.y, b.y), fminf(u.z, b.z), fmaxf(u.w, b.w));
+    }
+    p.wbox[i] = u;
 }
 
 __device__ __forceinline__ float2 mid_uv(const GeomArgs& a, const ProjArgs& p, int g, int s) {
@@ -283,9 +302,23 @@ __global__ void __launch_bounds__(256) k_shadow_dep_cull(GeomArgs a, ProjArgs p)
     const double gd = a.g.dist[o];
     const float2 q = valid ? mid_uv(a, p, g, s) : make_float2(0.f, 0.f);
     unsigned ntest = 0;
+    // the box around this warp's lit points (empty when none is lit)
+    float4 qb = lit ? make_float4(q.x, q.x, q.y, q.y) : make_float4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+    for (int o2 = 16; o2 > 0; o2 >>= 1) {
+        qb.x = fminf(qb.x, __shfl_xor_sync(0xffffffffu, qb.x, o2));
+        qb.y = fmaxf(qb.y, __shfl_xor_sync(0xffffffffu, qb.y, o2));
+        qb.z = fminf(qb.z, __shfl_xor_sync(0xffffffffu, qb.z, o2));
+        qb.w = fmaxf(qb.w, __shfl_xor_sync(0xffffffffu, qb.w, o2));
+    }
+    const float4* wb = p.wbox ? p.wbox + blockIdx.x : nullptr;  // this warp's step window
+    const int nw = (ntau + 31) / 32;
     for (int k = d0; k < d1; ++k) {
         if (!__any_sync(0xffffffffu, lit)) break;
         const int h = __ldg(&a.s.dep_idx[k]);
+        if (wb) {  // warp-uniform: h's window box misses every lit point of the warp
+            const float4 u = __ldg(wb + (size_t)h * nw);
+            if (u.x > qb.y || u.y < qb.x || u.z > qb.w || u.w < qb.z) continue;
+        }
         if (lit && in_box(q, facet_box(a, p, h, s))) {
             const double hd = a.g.dist[(size_t)h * ntau + s];
             if (gd > hd) {
@@ -466,8 +499,17 @@ int launch_shadow_culled(const DevSolve& s, const GeomWork& g, bool all_pairs, s
     }
     int rc = 0;
     if (!all_pairs) {
+        const long long nwt = (long long)s.nf * ((s.ntau + 31) / 32);
+        void* wm = nullptr;
+        if (cudaMallocAsync(&wm, (size_t)nwt * sizeof(float4), st) == cudaSuccess) {
+            p.wbox = static_cast<float4*>(wm);
+            k_window_box<<<(unsigned)((nwt + 255) / 256), 256, 0, st>>>(a, p);
+        } else {
+            cudaGetLastError();  // without window boxes: the per-step tests alone (same flags)
+        }
         dim3 blk(32, 8), grd((s.ntau + 31) / 32, (s.nf + 7) / 8);
         k_shadow_dep_cull<<<grd, blk, 0, st>>>(a, p);
+        if (wm) cudaFreeAsync(wm, st);
     } else {
         float umax, ext;
         memcpy(&umax, &stats[0], 4);
