@@ -114,3 +114,19 @@ def test_noalloc_entry_point_rejects_bad_arguments_before_any_device_work():
     assert b"status" in L.atpm_last_error()
     assert call(600_000, 1, p, p, 0, p) == 4        # ATPM_E_UNSUPPORTED: nf beyond the launch grid
     assert call(2048, 1024, p, p, 0, p) == 4        # ATPM_E_UNSUPPORTED: nf * ntau beyond the scratch
+
+
+def test_surface_temperatures_of_many_checks_arguments_first():
+    """atpm_get_surface_temperatures rejects null arrays before any device
+    call, and an empty request is a no-op (no GPU needed for either)."""
+    import ctypes as C
+
+    from binarytpm_gb300 import build, lib
+
+    build.build()
+    L = lib.load()
+    assert L.atpm_get_surface_temperatures(None, 1, None) != 0
+    one = (C.c_void_p * 1)(None)
+    assert L.atpm_get_surface_temperatures(one, 1, one) != 0  # null solve
+    assert L.atpm_get_surface_temperatures(one, -1, one) != 0
+    assert L.atpm_get_surface_temperatures(one, 0, one) == 0
