@@ -890,13 +890,14 @@ def _tile_stats(prob, slices=False):
 
 def _roofline(kern, n, prob, hbm, bf16, kind, cond_variant=4):
     """Dominant kernel of the revolution loop: the self-heating product
-    (k_spmm_tc over the tensor-core tiles, then k_spmm_rem over the FP32
-    sparse remainder; timed together).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
+    (k_spmm_tc over the tensor-core tiles, k_spmm_rem over the FP32 sparse
+    remainder beside it on a second stream, then k_rem_add; timed together
+    on the launch stream).  Its algorithmic intensity, 2 nnz NTAU FLOP over nnz (2 B
     BF16 + 4 B index) + 8 F NTAU bytes per solve, is ~65 FLOP/B, below the
     GB300 ridge (~290), so the bound is HBM: achieved = algorithmic bytes per
     launch (view factors once, shared by the batch's clones; W read and Q
-    written per solve) / CUDA-event duration; traffic = both kernels' ncu
-    DRAM bytes per batch revolution, measured on the headline binary.  The tensor-pipe figures are
+    written per solve) / CUDA-event duration; traffic = the three kernels'
+    ncu DRAM bytes per batch revolution, measured on the headline binary.  The tensor-pipe figures are
     beside it: algorithmic FLOP/s, and executed = every issued 128x16 K
     slice x step chunk x (2 or 3 BF16 products for the hi/lo compensation).
     The conduction sweep is reported beside it."""
@@ -925,7 +926,8 @@ def _roofline(kern, n, prob, hbm, bf16, kind, cond_variant=4):
                "note": "algorithmic bytes = nnz x 6 B + solves x 8 B x F x NTAU; executed tensor FLOP count the "
                        f"zero padding of the issued 128x16 K slices ({sl} of the {4 * tiles} in {tiles} tiles; "
                        f"{sl_lo} in the {lo} tiles with residual) and the hi/lo products; {rem} of {prob.nnz} "
-                       f"entries (cells with < {_tc_min_entries()} entries) are summed in FP32 by k_spmm_rem"}
+                       f"entries (cells with < {_tc_min_entries()} entries) are summed in FP32 by k_spmm_rem beside "
+                       "the product and added to Q by k_rem_add"}
     c = kern.get("conduction")
     if c and c["ms"]:
         nx = prob.nx
