@@ -767,7 +767,7 @@ def serving(ctx, n_requests: int, rate: float, seed: int = 5):
 CRATER_FIXTURE = ROOT / "tests" / "golden" / "rough_s1s1.npz"  # carries the reference's crater model files
 
 
-def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: int = 1280):
+def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: int = 1280, group: int = 4):
     """The batched-sweep configuration: ``n_solves`` binary solves advanced in
     one batch (every kernel launch spans all of them).  Each solve: a primary
     icosphere of subdivision 3, 4 or 5 (1,280 / 5,120 / 20,480 facets,
@@ -783,8 +783,8 @@ def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: 
     the crater model natively -- its forcing from the solve on the device,
     partial shadows, scattering, global heating from the batch's final
     temperatures, starting temperatures, then ``rough_revs`` crater
-    revolutions -- in parts of ``part`` facets through one crater object,
-    timed as sub-facet-steps/s."""
+    revolutions -- in parts of ``part`` facets, ``group`` parts (of any of
+    the solves) sharing one crater's launches, timed as sub-facet-steps/s."""
     from binarytpm_gb300 import formats, lib, workloads
 
     rng = np.random.default_rng(seed)
@@ -816,42 +816,51 @@ def batched_sweep(ctx, n_solves: int, seed: int = 7, rough_revs: int = 2, part: 
            "facet_steps": int(fs), "device_ms": ms, "facet_steps_per_s": fs / (ms / 1e3),
            "gpu_launches": int(launches), "setup_s": setup_s,
            "all_active": all(len(c) == HEADLINE_REVS for c in counts)}
-    # roughness: one solve of each primary size, crater model in parts
+    # roughness: one solve of each primary size, its parts of ``part`` facets
+    # packed ``group`` at a time into one crater (parts of different solves
+    # share the crater's launches, each facet with its own inertia and albedo)
     fx = np.load(CRATER_FIXTURE)
     texts = {str(k): str(v) for k, v in zip(fx["crater_names"], fx["crater_texts"])}
     cv, cf, V = formats.crater_model(texts["new_crater2.txt"], texts["new_crater2_selfheating_list.txt"])
-    crater = lib.Crater(ctx, part, 720, 48, precision=lib.FAST)
-    crater.set_surface(cv, cf, V, 11.9 * 3600.0)
-    forcing_s, rev_s, sub_steps, sampled = 0.0, 0.0, 0, []
+    sampled, parts = [], []
     for p in (3, 4, 5):
         i = int(np.flatnonzero(subs == p)[0])
-        s, prob = solves[i], protos[p][0]
-        alb = np.full(part, albs[i], np.float32)
-        for f0 in range(0, prob.nf, part):
-            tf = time.perf_counter()
-            crater.forcing(s, f0, prob.meta["dep_vec"])
-            crater.set_properties(np.zeros(part, np.uint8), alb, np.full(part, tis[i], np.float32))
-            crater.partial_shadow()
-            crater.scattering(s.solar(), prob.scattering_accuracy, multiple=True)
-            crater.global_heating(s, f0)
-            crater.initialise_temperatures(prob.emissivity, 5.67e-8)
-            tr = time.perf_counter()
-            for _ in range(rough_revs):
-                crater.inertia_difference(prob.emissivity, 5.67e-8, prob.tacc)
-            crater.update_converged(prob.tacc)
-            rev_s += time.perf_counter() - tr
-            forcing_s += tr - tf
-            sub_steps += part * 100 * 720 * rough_revs
+        prob = protos[p][0]
+        parts += [(i, prob, f0) for f0 in range(0, prob.nf, part)]
         sampled.append({"primary_subdiv": p, "facets": prob.nf, "thermal_inertia": float(tis[i]),
                         "albedo": float(albs[i]), "roughness_fraction": float(fracs[i])})
+    crater = lib.Crater(ctx, part * group, 720, 48, precision=lib.FAST)
+    crater.set_surface(cv, cf, V, 11.9 * 3600.0)
+    forcing_s, rev_s, sub_steps, craters = 0.0, 0.0, 0, 0
+    for g0 in range(0, len(parts), group):
+        grp = parts[g0:g0 + group]
+        n = part * len(grp)
+        tf = time.perf_counter()
+        crater.set_properties(np.zeros(part * group, np.uint8),
+                              np.repeat([albs[i] for i, _, _ in grp] + [0.0] * (group - len(grp)), part).astype(np.float32),
+                              np.repeat([tis[i] for i, _, _ in grp] + [1.0] * (group - len(grp)), part).astype(np.float32))
+        for k, (i, prob, f0) in enumerate(grp):
+            crater.prepare_part(solves[i], f0, k * part, part, prob.meta["dep_vec"])
+        crater.partial_shadow()
+        crater.scattering(solves[grp[0][0]].solar(), grp[0][1].scattering_accuracy, multiple=True)
+        crater.initialise_temperatures(grp[0][1].emissivity, 5.67e-8)
+        tr = time.perf_counter()
+        for _ in range(rough_revs):
+            crater.inertia_difference(grp[0][1].emissivity, 5.67e-8, grp[0][1].tacc)
+        crater.update_converged(grp[0][1].tacc)
+        rev_s += time.perf_counter() - tr
+        forcing_s += tr - tf
+        sub_steps += n * 100 * 720 * rough_revs
+        craters += 1
     crater.close()
-    out["rough"] = {"sampled": sampled, "part_facets": part, "revolutions": rough_revs,
-                    "sub_facet_steps": sub_steps, "sub_facet_steps_per_s": sub_steps / rev_s,
+    out["rough"] = {"sampled": sampled, "part_facets": part, "parts_per_crater": group, "crater_runs": craters,
+                    "revolutions": rough_revs, "sub_facet_steps": sub_steps, "sub_facet_steps_per_s": sub_steps / rev_s,
                     "forcing_s": forcing_s,
-                    "what": "crater model run natively per part of the sampled solves: forcing on the device from "
-                            "the solve (sub-facet geometry, global view factors, illumination and heating), partial "
-                            "shadows, scattering, starting temperatures (forcing_s), then crater revolutions "
-                            "(host clock around synchronous calls)"}
+                    "what": "crater model run natively for every part of the sampled solves, parts of different "
+                            "solves packed into one crater (atpm_crater_prepare_part) and advanced in the same "
+                            "launches: forcing and global heating on the device from each solve, partial shadows, "
+                            "scattering, starting temperatures (forcing_s), then crater revolutions (host clock "
+                            "around synchronous calls; the last crater run's unused facets, if any, still advance)"}
     for s in solves:
         s.close()
     for _, s in protos.values():

@@ -262,6 +262,90 @@ ATPM_API atpm_status atpm_crater_forcing(atpm_solve* s, atpm_crater* c, int32_t 
     return ATPM_OK;
 }
 
+namespace {
+// the crater's arrays of facets c0 .. c0 + n - 1 as a crater of n facets
+CraterDev crater_view(const CraterDev& d, int c0, int n) {
+    CraterDev v = d;
+    v.nf = n;
+    const size_t fs = (size_t)d.ntau * d.nsf;
+    auto off = [](auto* p, size_t k) { return p ? p + k : p; };
+    v.numrevs = off(d.numrevs, (size_t)c0);
+    v.conv = off(d.conv, (size_t)c0);
+    v.albedo = off(d.albedo, (size_t)c0);
+    v.ti = off(d.ti, (size_t)c0);
+    v.hot = off(d.hot, (size_t)c0);
+    v.shadow = off(d.shadow, (size_t)c0 * d.ntau);
+    v.sfc_shadow = off(d.sfc_shadow, c0 * fs);
+    v.illumvec = off(d.illumvec, (size_t)c0 * d.ntau * 3);
+    v.illumangle = off(d.illumangle, c0 * fs);
+    v.RI = off(d.RI, c0 * fs);
+    v.RGI = off(d.RGI, c0 * fs);
+    v.RGH = off(d.RGH, c0 * fs);
+    v.stemp0 = off(d.stemp0, c0 * fs);
+    v.stemp1 = off(d.stemp1, c0 * fs);
+    v.temp = off(d.temp, (size_t)c0 * (d.nx + 1) * d.nsf);
+    return v;
+}
+}  // namespace
+
+ATPM_API atpm_status atpm_crater_prepare_part(atpm_solve* s, atpm_crater* c, int32_t f0, int32_t c0, int32_t n,
+                                              const float* dep_vec) {
+    if (!s || !c || n < 1 || f0 < 0 || c0 < 0 || f0 + n > s->nf || c0 + n > c->nf || c->ntau != s->P.ntau)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_prepare_part: facets f0 .. f0+n-1 of the solve into "
+                                                 "facets c0 .. c0+n-1 of the crater");
+    if (!c->cnorm) return atpm::fail_status(ATPM_E_STATE, "crater_prepare_part: set the crater surface first");
+    if (c->nx == 0) return atpm::fail_status(ATPM_E_STATE, "crater_prepare_part: shadow-only crater");
+    if (s->rs != 4) return atpm::fail_status(ATPM_E_UNSUPPORTED, "crater_prepare_part: FP32 solves (REFERENCE or FAST)");
+    if (!s->have_forcing)
+        return atpm::fail_status(ATPM_E_STATE, "crater_prepare_part: run the solve's geometry and scattering first");
+    if (s->ctx->device != c->ctx->device) return atpm::fail_status(ATPM_E_INVALID, "crater_prepare_part: different devices");
+    CC(cudaSetDevice(c->ctx->device), "device");
+    CC(cudaStreamSynchronize(s->st), "solve stream");
+    const CraterDev v = crater_view(c->d, c0, n);
+    atpm_status r = solve_crater_sun(s, f0, n, const_cast<float*>(v.illumvec), const_cast<int*>(v.shadow), c->st);
+    if (r) return r;
+    if (launch_crater_surface(v, const_cast<float*>(v.illumangle), c->st))
+        return atpm::fail_status(ATPM_E_CUDA, "crater_prepare_part: surface launch");
+    std::vector<int32_t> ptr(2);
+    CC(cudaMemcpy(ptr.data(), s->ds.dep_ptr + f0, 4, cudaMemcpyDeviceToHost), "list bounds");
+    CC(cudaMemcpy(ptr.data() + 1, s->ds.dep_ptr + f0 + n, 4, cudaMemcpyDeviceToHost), "list bounds");
+    const size_t ne = (size_t)(ptr[1] - ptr[0]);
+    if (ne > 0 && !dep_vec)
+        return atpm::fail_status(ATPM_E_INVALID, "crater_prepare_part: the list entries' vectors are needed");
+    if (ne > c->gvf_cap) {
+        if (c->gvf) cudaFree(c->gvf);
+        if (c->vec) cudaFree(c->vec);
+        c->gvf = nullptr;
+        c->vec = nullptr;
+        c->gvf_cap = 0;
+        CC(cudaMalloc((void**)&c->gvf, ne * c->nsf * 4), "allocation");
+        CC(cudaMalloc((void**)&c->vec, ne * 12), "allocation");
+        c->gvf_cap = ne;
+    }
+    if (ne > 0) {
+        CC(cudaMemcpyAsync(c->vec, dep_vec + 3 * (size_t)ptr[0], ne * 12, cudaMemcpyHostToDevice, c->st), "vectors");
+        if (launch_crater_gvf(v, s->ds.vert, s->ds.fac, s->ds.dep_ptr, s->ds.dep_vf, f0, c->vec, c->gvf, c->st))
+            return atpm::fail_status(ATPM_E_CUDA, "crater_prepare_part: view-factor launch");
+    }
+    if (launch_crater_gsum(v, s->ds.dep_ptr, s->ds.dep_idx, f0, c->gvf, static_cast<const float*>(s->ds.Efm),
+                           s->P.ntau, 0, s->ds.alb, 0.0f, 0.0f, const_cast<float*>(v.RGI), c->st))
+        return atpm::fail_status(ATPM_E_CUDA, "crater_prepare_part: global illumination launch");
+    // global heating from the solve's current surface temperatures
+    const size_t nt = (size_t)s->nf * s->P.ntau;
+    float* tfm = nullptr;
+    CC(cudaMallocAsync((void**)&tfm, nt * 4, c->st), "allocation");
+    int rc = launch_transpose_sf(static_cast<const float*>(s->ds.stemp1), s->P.ntau, s->nf, tfm, c->st);
+    if (!rc)
+        rc = launch_crater_gsum(v, s->ds.dep_ptr, s->ds.dep_idx, f0, c->gvf, tfm, s->P.ntau, 1, 0.0f,
+                                (float)s->P.emissivity, 5.67e-8f, const_cast<float*>(v.RGH), c->st);
+    cudaFreeAsync(tfm, c->st);
+    CC(cudaStreamSynchronize(c->st), "prepare part");
+    if (rc) return atpm::fail_status(ATPM_E_CUDA, "crater_prepare_part: global heating launch");
+    c->fsolve = nullptr;  // the view factors held belong to a part, not to the whole crater
+    c->ff0 = -1;
+    return ATPM_OK;
+}
+
 ATPM_API atpm_status atpm_crater_global_heating(atpm_solve* s, atpm_crater* c, int32_t f0) {
     if (!s || !c) return atpm::fail_status(ATPM_E_INVALID, "crater_global_heating: null argument");
     if (c->fsolve != s || c->ff0 != f0)

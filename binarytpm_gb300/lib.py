@@ -120,6 +120,7 @@ _SIGS = {
                                        C.c_void_p, C.c_void_p, C.c_double, C.c_int32, C.c_void_p, C.c_void_p]),
     "atpm_crater_set_surface": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float]),
     "atpm_crater_forcing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "atpm_crater_prepare_part": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "atpm_crater_global_heating": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "atpm_solve_solar": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "atpm_set_albedo": (C.c_int, [C.c_void_p, C.c_float]),
@@ -629,6 +630,14 @@ class Crater:
     def global_heating(self, solve: "Solve", f0: int = 0):
         """Array 6 from the solve's current surface temperatures."""
         _ck(load().atpm_crater_global_heating(solve.h, self.h, int(f0)))
+
+    def prepare_part(self, solve: "Solve", f0: int, c0: int, n: int, dep_vec=None):
+        """Facets f0 .. f0+n-1 of ``solve`` into facets c0 .. c0+n-1 of this
+        crater: their forcing and their global heating from the solve's current
+        surface temperatures (parts of several solves then share the crater's
+        launches)."""
+        d = None if dep_vec is None else np.ascontiguousarray(np.asarray(dep_vec, np.float32).reshape(-1, 3))
+        _ck(load().atpm_crater_prepare_part(solve.h, self.h, int(f0), int(c0), int(n), _p(d)))
 
     def set_properties(self, converged=None, albedo=None, thermal_inertia=None):
         c = None if converged is None else np.ascontiguousarray(converged, np.uint8)

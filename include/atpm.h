@@ -365,6 +365,18 @@ ATPM_API atpm_status atpm_crater_forcing(atpm_solve* s, atpm_crater* c, int32_t 
  * (load_GPU_roughness_globalheating, main.cpp:2069-2103), with the view
  * factors of the last atpm_crater_forcing on the same solve and f0. */
 ATPM_API atpm_status atpm_crater_global_heating(atpm_solve* s, atpm_crater* c, int32_t f0);
+/* One crater for parts of several solves (rough solves of a batch sharing
+ * the crater launches): facets f0 .. f0 + n - 1 of solve s go to facets
+ * c0 .. c0 + n - 1 of the crater, whose forcing (as atpm_crater_forcing) and
+ * global heating from the solve's current surface temperatures (as
+ * atpm_crater_global_heating) are computed for that range alone.  Each
+ * facet keeps its own thermal inertia and albedo (atpm_crater_set_properties);
+ * the parts share NTAU, NX, the crater model, its rotation period and the
+ * solar flux given to atpm_crater_scattering.  The crater revolutions then
+ * advance every part in the same launches, each facet's columns exactly as
+ * in a crater of that part alone. */
+ATPM_API atpm_status atpm_crater_prepare_part(atpm_solve* s, atpm_crater* c, int32_t f0, int32_t c0, int32_t n,
+                                              const float* dep_vec);
 ATPM_API atpm_status atpm_crater_set_ir_absorptivity(atpm_crater* c, float ir_abs);
 /* GPU_sfcpartialshadow (909-921): every step in one launch */
 ATPM_API atpm_status atpm_crater_partial_shadow(atpm_crater* c);
